@@ -1,0 +1,146 @@
+/* gbpf.h -- C ABI of the GB300-native batched polar Newton-Raphson power-flow solver.
+ *
+ * Drop-in boundary for the batched Newton path of e2nIEE/parallel-pandapower-solver
+ * (p3s 1.2.2). Every entry point replaces one call the reference's Python layer makes
+ * into its compiled solvers; the reference interface each one replaces is cited next to
+ * it. All arrays are caller-owned, C order; complex128 arrays are passed as interleaved
+ * (re, im) doubles. Host-pointer entry points copy to and from the device themselves;
+ * the *_device variants take device pointers. Functions return 0 on success and a
+ * negative code on error, with a message from gbpf_last_error() (never an exception).
+ * Non-convergence is not an error: it is reported per case in `converged`.
+ */
+#ifndef GBPF_H
+#define GBPF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbpf_solver gbpf_solver;
+
+/* Per-call solve parameters (nr_klu.cpp:1049-1052 keyword arguments, and the
+ * PolarNewtonSolverCUDA attributes precision / mixed_switch / line_search,
+ * p3s/cuda/nr_polar_solver.py:309-330). */
+typedef struct gbpf_params {
+    int max_iter;        /* 30 */
+    double tol;          /* 1e-8: infinity norm of the mismatch, p.u. */
+    int line_search;     /* 1: Armijo backtracking (nr_klu.cpp:541-567) */
+    int precision;       /* 0: double factors; 1: mixed (float factors while the vote asks) */
+    double mixed_switch; /* mismatch above which a case factors in float (mixed only) */
+    int check_v0;        /* 1: reject non-finite / out-of-range start voltages like solve_batch */
+} gbpf_params;
+
+/* Topology / schedule facts of a solver (for stats, rooflines and tests). */
+typedef struct gbpf_info {
+    int n_bus, nnz_ybus, n_var_bus, n_blocks, n_levels, n_back_levels;
+    int cases_per_cta, threads_per_cta, workers;
+    long long factor_pairs, forward_pairs, backward_pairs;
+    double rcond0;
+} gbpf_info;
+
+/* Counters of the last solve (the reference's last_stats, nr_polar_solver.py:671-681). */
+typedef struct gbpf_stats {
+    unsigned long long single_factorizations, double_factorizations;
+    unsigned long long single_rejected, double_rejected, macro_steps;
+    int grid, cases_per_cta;
+    double kernel_ms; /* device time of the Newton kernel, CUDA events on the solver's stream */
+} gbpf_stats;
+
+const char* gbpf_last_error(void);
+int gbpf_version(void);
+int gbpf_device_count(void);
+
+/* Solver for one grid topology: pattern, bus types, fill-reducing order, symbolic
+ * factorization and schedule, device upload.
+ * Replaces nr_klu.Solver(Yp, Yj, Yx, pv, pq) (nr_klu.cpp:964-994, build_topology :732-759)
+ * and PolarNewtonSolverCUDA(Yp, Yj, Yx, pv, pq) (nr_polar_solver.py:285-378).
+ * cases_per_cta: 0 = automatic, else a power of two in 1..32. Returns NULL on error. */
+gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
+                         int npv, const int32_t* pq, int npq, int cases_per_cta);
+void gbpf_destroy(gbpf_solver* s);
+
+/* Values-only Ybus refresh. Replaces Solver.update_Y (nr_klu.cpp:999-1011) and
+ * PolarNewtonSolverCUDA.update_Y (nr_polar_solver.py:569-587). */
+int gbpf_update_Y(gbpf_solver* s, const double* Yx, int nnz);
+
+int gbpf_get_info(gbpf_solver* s, gbpf_info* out);
+int gbpf_get_stats(gbpf_solver* s, gbpf_stats* out);
+/* Ybus nnz -> Jacobian block position (-1 for slack rows/columns), length nnz. */
+int gbpf_get_posmap(gbpf_solver* s, int32_t* out);
+
+/* Batch of operating points on one topology (time series).
+ * S: (n, T) complex (s_per_col = 1) or (n,) shared; V0: (n, T) (v0_per_col = 1) or (n,).
+ * Out: V (n, T) complex, iterations (T,), converged (T,).
+ * Replaces Solver.solve_batch (nr_klu.cpp:1049-1166) and
+ * PolarNewtonSolverCUDA.solve_batch (nr_polar_solver.py:466-481). */
+int gbpf_solve_batch(gbpf_solver* s, int T, const double* S, int s_per_col, const double* V0, int v0_per_col,
+                     const gbpf_params* p, double* V, int32_t* iterations, uint8_t* converged);
+int gbpf_solve_batch_device(gbpf_solver* s, int T, const double* dS, int s_per_col, const double* dV0,
+                            int v0_per_col, const gbpf_params* p, double* dV, int32_t* d_iterations,
+                            uint8_t* d_converged);
+
+/* Warm-start lanes: hours offsets[l] .. offsets[l+1]-1 of lane l are solved in order,
+ * each from the converged voltage of the previous hour of its lane (from V0 for a
+ * lane's first hour and after a non-converged hour). S (n, T); V0 (n,).
+ * Extends solve_batch with per-column start voltages (nr_klu.cpp:1070-1090): the chain
+ * is resolved on the device. */
+int gbpf_solve_lanes(gbpf_solver* s, int T, const double* S, const double* V0, int K, const int64_t* offsets,
+                     const gbpf_params* p, double* V, int32_t* iterations, uint8_t* converged);
+int gbpf_solve_lanes_device(gbpf_solver* s, int T, const double* dS, const double* dV0, int K,
+                            const int64_t* d_offsets, const gbpf_params* p, double* dV, int32_t* d_iterations,
+                            uint8_t* d_converged);
+
+/* N-1 batch: per-case Ybus values on the shared pattern, per-case pin mask.
+ * S: (n,) complex; V0: (n, L) complex; pin: (n, L) uint8 (NULL = none).
+ * Per-case Ybus either dense Yd (nnz, L) complex (replaces
+ * Solver.solve_batch_contingency, nr_klu.cpp:1184-1281, and
+ * PolarNewtonSolverCUDA.solve_batch_contingency[_cx], nr_polar_solver.py:483-527) or, with
+ * Yd == NULL, the base Ybus minus sparse stamps: case c subtracts st_val[e] at CSR
+ * position st_k[e] for e in [st_ptr[c], st_ptr[c+1]) (replaces
+ * solve_batch_contingency_stamp, nr_polar_solver.py:529-557). */
+int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double* V0, const uint8_t* pin,
+                           const double* Yd, const int32_t* st_ptr, const int32_t* st_k, const double* st_val,
+                           const gbpf_params* p, double* V, int32_t* iterations, uint8_t* converged);
+
+/* Jacobian blocks (n_blocks x 4, row-major 2x2 [dP/dth dP/dVm; dQ/dth dQ/dVm]) and residual
+ * (n_var_bus x 2, block-row order, S - S(V)) evaluated on the device at one voltage.
+ * Backs debug_J (nr_klu.cpp:1283-1304, 1332-1342). */
+int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const uint8_t* pin, double* blocks,
+                       double* residual);
+/* Block row of each bus (-1 for slack), length n. */
+int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
+
+/* Page-locked host memory for fast transfers. */
+void* gbpf_host_alloc(size_t bytes);
+void gbpf_host_free(void* p);
+
+/* Islanding of N-1 cases on the device (case_generator.py:355-430 semantics).
+ * Graph: n buses, m branches (f[e], t[e]); live[e] != 0 if the branch couples its ends.
+ * Case c removes branches out_idx[out_ptr[c] .. out_ptr[c+1]). Labels are the connected
+ * components numbered by their smallest bus (scipy's connected_components order).
+ * Reference buses: slack buses (is_slack) keep their island served; with reslack, an
+ * island without a slack is served from its generator bus of highest priority
+ * (gen_prio[bus] > 0, ties to the lowest bus index); other islands are unserved.
+ * Out: labels (n, L) int32, served (n, L) uint8, ref_bus (n, L) int32 (-1 if unserved),
+ * reslack_bus (L,) int32 (-1 if none; the first re-slacked bus of the case). */
+int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
+                 const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
+                 int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands);
+
+/* Host-only check of the planner and the device schedule (runs without a GPU): plan for
+ * `workers` workers, Jacobian at (Vm, Va) with injections S (n complex), the schedule
+ * executed serially with a structural race check per level. dx (n x 2): Newton step per
+ * bus (angle, magnitude). shape (7): n_var_bus, n_blocks, levels, back levels, factor /
+ * forward / backward pairs. No reference counterpart: the reference's numpy plan executor
+ * (lean_lu_plan.py:324-360) plays this role for its own plan. */
+int gbpf_plan_selftest(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
+                       int npv, const int32_t* pq, int npq, int workers, const double* Vm, const double* Va,
+                       const double* S, double* dx, int32_t* shape, char* msg, int msglen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

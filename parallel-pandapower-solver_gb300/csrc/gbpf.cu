@@ -1,0 +1,652 @@
+// gbpf.cu -- host orchestration and C ABI (include/gbpf.h) of the batched Newton solver.
+//
+// The GB300 replacement of the reference's host drivers: nr_klu.cpp's Solver class
+// (:964-1313) and PolarNewtonSolverCUDA's chunk loop (nr_polar_solver.py:598-1068). A
+// solve is ONE launch of the persistent Newton kernel over the whole batch: no memory
+// chunking (the per-CTA scratch is reused case after case, so device memory does not grow
+// with the batch), no per-pass status read-back, no CPU hand-off.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gbpf.h"
+#include "gbpf_device.h"
+#include "plan.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(const std::string& m) {
+    g_err = m;
+    return -1;
+}
+
+#define CK(x)                                                                                       \
+    do {                                                                                            \
+        cudaError_t e_ = (x);                                                                       \
+        if (e_ != cudaSuccess) return fail(std::string(#x) + " failed: " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(b, 16));
+        if (e == cudaSuccess) bytes = std::max<size_t>(b, 16);
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+template <typename T>
+cudaError_t upload(DBuf& b, const std::vector<T>& v) {
+    cudaError_t e = b.ensure(v.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return cudaSuccess;
+}
+
+int ilog2(int g) {
+    int l = 0;
+    while ((1 << l) < g) ++l;
+    return l;
+}
+
+}  // namespace
+
+void gbpf::set_error(const std::string& msg) { g_err = msg; }
+
+struct gbpf_solver {
+    gbpf::Plan plan;
+    int n = 0, nnz = 0;
+    std::vector<int> Yp, Yj;
+    std::vector<double> Yx;  // interleaved complex
+    int device = 0, nsm = 0, occ = 1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int G = 8, lg = 3, NT = 512;
+    // topology on the device
+    DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dpairs,
+        drow_pq, dbus_of_row, ddpos;
+    gbpf::DevPlan dp{};
+    // scratch (per CTA, grow-only)
+    DBuf fac64, fac32, R, y64, y32, Vc, Vt, Et, V32, spin;
+    size_t sc_ctas = 0;
+    bool sc_mixed = false;
+    // per-call buffers (grow-only)
+    DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin;
+    gbpf_stats last{};
+    ~gbpf_solver() {
+        for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dtaskA, &dptrA, &dscl, &dptrB,
+                        &dtaskC, &dptrC, &dpairs, &drow_pq, &dbus_of_row, &ddpos, &fac64, &fac32, &R, &y64, &y32,
+                        &Vc, &Vt, &Et, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
+                        &bYd, &bpin})
+            b->release();
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int upload_values(gbpf_solver* s) {
+    std::vector<double> y(s->Yx);
+    std::vector<float> y32(s->Yx.size());
+    for (size_t i = 0; i < y.size(); ++i) y32[i] = (float)y[i];
+    CK(upload(s->dY, y));
+    CK(upload(s->dY32, y32));
+    return 0;
+}
+
+// Pivot ratio of the frozen order on the base-grid Jacobian at a flat voltage, the
+// reference value every later factorization is judged against (nr_klu.cpp:713-729,
+// nr_polar_solver.py:409-427).
+int compute_rcond0(gbpf_solver* s) {
+    gbpf::Plan& p = s->plan;
+    std::vector<double> Vm(s->n, 1.0), Va(s->n, 0.0), S(2 * (size_t)s->n, 0.0), blk(4 * (size_t)p.nblk),
+        R(2 * (size_t)std::max(p.nv, 1));
+    gbpf::host_eval(p, s->Yp.data(), s->Yj.data(), s->Yx.data(), Vm.data(), Va.data(), S.data(), nullptr, blk.data(),
+                    R.data());
+    double mn = 0, mx = 0;
+    if (p.nv == 0) {
+        p.rcond0 = 1.0;
+        return 0;
+    }
+    if (!gbpf::host_factor(p, blk.data(), &mn, &mx) || !(mx > 0.0) || !(mn > 0.0) || !std::isfinite(mx))
+        return fail(
+            "lean LU: the Jacobian has a zero or non-finite diagonal pivot at flat start, so the static pivot order "
+            "cannot be used for this grid");
+    p.rcond0 = mn / mx;
+    return 0;
+}
+
+int setup(gbpf_solver* s, int cases_per_cta) {
+    CK(cudaGetDevice(&s->device));
+    CK(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&s->e0));
+    CK(cudaEventCreate(&s->e1));
+    s->NT = gbpf::newton_max_threads();
+    int G = cases_per_cta;
+    if (G <= 0) {
+        // cases per CTA: enough slots to keep the CTA's workers busy on small grids,
+        // few enough that the per-CTA working set of large grids stays L2-friendly
+        const int nv = std::max(1, (int)s->plan.nv);
+        G = nv <= 160 ? 32 : (nv <= 640 ? 16 : 8);
+    }
+    if (G < 1 || G > gbpf::MAX_SLOTS || (G & (G - 1))) return fail("cases_per_cta must be a power of two in 1..32");
+    s->G = G;
+    s->lg = ilog2(G);
+    int occ = 1;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(), s->NT, 0));
+    s->occ = std::max(1, occ);
+    return 0;
+}
+
+int upload_plan(gbpf_solver* s) {
+    const gbpf::Plan& p = s->plan;
+    CK(upload(s->dYp, s->Yp));
+    CK(upload(s->dYj, s->Yj));
+    CK(upload(s->dposmap, p.posmap));
+    CK(upload(s->drow_of_bus, p.row_of_bus));
+    CK(upload(s->dbus_pq, p.bus_pq));
+    // DIAG tasks carry the "two real pivots" flag (PQ row) in bit 5 of their code
+    std::vector<int> tA = p.taskA;
+    for (size_t t = 0; t < tA.size() / 4; ++t) {
+        if ((tA[4 * t + 1] & 3) == gbpf::TK_DIAG) {
+            const int dst = tA[4 * t];
+            const int row = (int)(std::upper_bound(p.base.begin(), p.base.end(), dst) - p.base.begin()) - 1;
+            if (p.row_pq[row]) tA[4 * t + 1] |= 32;
+        }
+    }
+    CK(upload(s->dtaskA, tA));
+    CK(upload(s->dptrA, p.ptrA));
+    CK(upload(s->dscl, p.scl));
+    CK(upload(s->dptrB, p.ptrB));
+    CK(upload(s->dtaskC, p.taskC));
+    CK(upload(s->dptrC, p.ptrC));
+    CK(upload(s->dpairs, p.pairs));
+    CK(upload(s->drow_pq, p.row_pq));
+    CK(upload(s->dbus_of_row, p.bus_of_row));
+    std::vector<int> dpos(p.base.begin(), p.base.begin() + p.nv);
+    CK(upload(s->ddpos, dpos));
+    if (int rc = upload_values(s)) return rc;
+    gbpf::DevPlan& d = s->dp;
+    d.n = p.n;
+    d.nv = p.nv;
+    d.nblk = p.nblk;
+    d.W = p.W;
+    d.nlev = p.nlev;
+    d.nblev = p.nblev;
+    d.nnzY = p.nnzY;
+    d.Yp = s->dYp.as<int>();
+    d.Yj = s->dYj.as<int>();
+    d.Y = s->dY.as<double2>();
+    d.Y32 = s->dY32.as<float2>();
+    d.posmap = s->dposmap.as<int>();
+    d.row_of_bus = s->drow_of_bus.as<int>();
+    d.bus_pq = s->dbus_pq.as<uint8_t>();
+    d.taskA = s->dtaskA.as<int4>();
+    d.ptrA = s->dptrA.as<int>();
+    d.scl = s->dscl.as<int2>();
+    d.ptrB = s->dptrB.as<int>();
+    d.taskC = s->dtaskC.as<int4>();
+    d.ptrC = s->dptrC.as<int>();
+    d.pairs = s->dpairs.as<int2>();
+    d.row_pq = s->drow_pq.as<uint8_t>();
+    d.bus_of_row = s->dbus_of_row.as<int>();
+    d.dpos = s->ddpos.as<int>();
+    return 0;
+}
+
+int ensure_scratch(gbpf_solver* s, size_t ctas, bool mixed) {
+    if (ctas <= s->sc_ctas && (!mixed || s->sc_mixed)) return 0;
+    ctas = std::max(ctas, s->sc_ctas);
+    mixed = mixed || s->sc_mixed;
+    const size_t G = s->G, nb = s->plan.nblk, nv = std::max(1, s->plan.nv), n = s->n;
+    CK(s->fac64.ensure(ctas * nb * G * 32));
+    CK(s->R.ensure(ctas * nv * G * 16));
+    CK(s->y64.ensure(ctas * nv * G * 16));
+    CK(s->Vc.ensure(ctas * n * G * 32));
+    CK(s->Vt.ensure(ctas * n * G * 32));
+    CK(s->Et.ensure(ctas * n * G * 16));
+    CK(s->V32.ensure(ctas * n * G * 16));
+    CK(s->spin.ensure(ctas * n * G));
+    if (mixed) {
+        CK(s->fac32.ensure(ctas * nb * G * 16));
+        CK(s->y32.ensure(ctas * nv * G * 8));
+    }
+    s->sc_ctas = ctas;
+    s->sc_mixed = mixed;
+    return 0;
+}
+
+gbpf::Scratch scratch_view(gbpf_solver* s) {
+    gbpf::Scratch sc{};
+    sc.G = s->G;
+    sc.log2G = s->lg;
+    sc.blk_stride = (size_t)s->plan.nblk * s->G;
+    sc.row_stride = (size_t)std::max(1, s->plan.nv) * s->G;
+    sc.bus_stride = (size_t)s->n * s->G;
+    sc.fac64 = s->fac64.as<double4_32a>();
+    sc.fac32 = s->sc_mixed ? s->fac32.as<float4>() : nullptr;
+    sc.R = s->R.as<double2>();
+    sc.y64 = s->y64.as<double2>();
+    sc.y32 = s->sc_mixed ? s->y32.as<float2>() : nullptr;
+    sc.Vc = s->Vc.as<double4_32a>();
+    sc.Vt = s->Vt.as<double4_32a>();
+    sc.Et = s->Et.as<double2>();
+    sc.V32 = s->V32.as<float4>();
+    sc.pin = s->spin.as<uint8_t>();
+    return sc;
+}
+
+gbpf_params default_params() {
+    gbpf_params p;
+    p.max_iter = 30;
+    p.tol = 1e-8;
+    p.line_search = 1;
+    p.precision = 0;
+    p.mixed_switch = 1e-3;
+    p.check_v0 = 0;
+    return p;
+}
+
+int check_params(const gbpf_params& p, const char* who) {
+    if (p.max_iter <= 0) return fail(std::string(who) + ": max_iter must be > 0");
+    if (!(p.tol > 0.0)) return fail(std::string(who) + ": tol must be > 0");
+    if (p.precision != 0 && p.precision != 1) return fail(std::string(who) + ": precision must be 0 (double) or 1 (mixed)");
+    return 0;
+}
+
+// Run the persistent kernel over `units` work items (cases, or lanes) and wait for it.
+int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
+    if (units <= 0) return fail(std::string(who) + ": empty batch");
+    const long long want = (units + s->G - 1) / s->G;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)s->nsm * s->occ));
+    if (int rc = ensure_scratch(s, grid, b.mixed != 0)) return rc;
+    CK(s->bctl.ensure(64 * sizeof(unsigned long long)));
+    auto* ctl = s->bctl.as<unsigned long long>();
+    CK(cudaMemsetAsync(ctl, 0, 64 * sizeof(unsigned long long), s->stream));
+    b.counter = reinterpret_cast<int*>(ctl + 16);
+    b.stats = ctl;
+    b.err = reinterpret_cast<int*>(ctl + 24);
+    gbpf::Scratch sc = scratch_view(s);
+    CK(cudaEventRecord(s->e0, s->stream));
+    CK(gbpf::launch_newton(s->dp, b, sc, grid, s->NT, s->stream));
+    CK(cudaEventRecord(s->e1, s->stream));
+    unsigned long long host_ctl[32];
+    CK(cudaMemcpyAsync(host_ctl, ctl, sizeof host_ctl, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
+    s->last.single_factorizations = host_ctl[0];
+    s->last.double_factorizations = host_ctl[1];
+    s->last.single_rejected = host_ctl[2];
+    s->last.double_rejected = host_ctl[3];
+    s->last.macro_steps = host_ctl[4];
+    s->last.grid = grid;
+    s->last.cases_per_cta = s->G;
+    s->last.kernel_ms = ms;
+    const int* err = reinterpret_cast<const int*>(host_ctl + 24);
+    if (err[0] == gbpf::DE_V0_NONFINITE)
+        return fail(std::string(who) + ": invalid initial voltage at bus " + std::to_string(err[1]) + ", step " +
+                    std::to_string(err[2]));
+    if (err[0] == gbpf::DE_V0_MAGNITUDE)
+        return fail(std::string(who) + ": invalid voltage magnitude at bus " + std::to_string(err[1]) + ", step " +
+                    std::to_string(err[2]));
+    if (err[0] == gbpf::DE_STAMPS)
+        return fail(std::string(who) + ": case " + std::to_string(err[2]) + " has " + std::to_string(err[1]) +
+                    " outage stamp entries, more than the " + std::to_string(gbpf::MAX_STAMPS) + " supported");
+    return 0;
+}
+
+void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
+    b.max_iter = p.max_iter;
+    b.tol = p.tol;
+    b.line_search = p.line_search;
+    b.mixed = p.precision == 1;
+    b.mixed_switch = p.mixed_switch;
+    b.check_v0 = p.check_v0;
+    b.rcond_min64 = 1e-3 * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO
+    b.rcond_min32 = 1e-3 * s->plan.rcond0;
+}
+
+}  // namespace
+
+// =============================================================================== C ABI
+extern "C" {
+
+const char* gbpf_last_error(void) { return g_err.c_str(); }
+
+int gbpf_version(void) { return 100; }
+
+int gbpf_device_count(void) {
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
+                         int npv, const int32_t* pq, int npq, int cases_per_cta) {
+    if (n <= 0 || !Yp || (nnz > 0 && (!Yj || !Yx)) || npv < 0 || npq < 0) {
+        fail("gbpf_create: invalid arguments");
+        return nullptr;
+    }
+    std::unique_ptr<gbpf_solver> s(new gbpf_solver);
+    s->n = n;
+    s->nnz = nnz;
+    s->Yp.assign(Yp, Yp + n + 1);
+    s->Yj.assign(Yj, Yj + nnz);
+    s->Yx.assign(Yx, Yx + 2 * (size_t)nnz);
+    // workers depend on the slot count; choose the slot count first from the bus count
+    {
+        gbpf::Plan probe;
+        std::string e = gbpf::build_plan(probe, n, Yp, Yj, nnz, pv, npv, pq, npq, 1);
+        if (!e.empty()) {
+            fail("gbpf_create: " + e);
+            return nullptr;
+        }
+        s->plan.nv = probe.nv;
+    }
+    if (setup(s.get(), cases_per_cta)) return nullptr;
+    std::string e = gbpf::build_plan(s->plan, n, Yp, Yj, nnz, pv, npv, pq, npq, s->NT / s->G);
+    if (!e.empty()) {
+        fail("gbpf_create: " + e);
+        return nullptr;
+    }
+    if (compute_rcond0(s.get())) return nullptr;
+    if (upload_plan(s.get())) return nullptr;
+    return s.release();
+}
+
+void gbpf_destroy(gbpf_solver* s) { delete s; }
+
+int gbpf_update_Y(gbpf_solver* s, const double* Yx, int nnz) {
+    if (!s) return fail("null solver");
+    if (nnz != s->nnz) return fail("update_Y: nnz mismatch (topology changed; rebuild Solver)");
+    s->Yx.assign(Yx, Yx + 2 * (size_t)nnz);
+    if (int rc = compute_rcond0(s)) return rc;
+    return upload_values(s);
+}
+
+int gbpf_get_info(gbpf_solver* s, gbpf_info* o) {
+    if (!s || !o) return fail("null argument");
+    const gbpf::Plan& p = s->plan;
+    o->n_bus = p.n;
+    o->nnz_ybus = p.nnzY;
+    o->n_var_bus = p.nv;
+    o->n_blocks = p.nblk;
+    o->n_levels = p.nlev;
+    o->n_back_levels = p.nblev;
+    o->cases_per_cta = s->G;
+    o->threads_per_cta = s->NT;
+    o->workers = p.W;
+    o->factor_pairs = p.n_factor_pairs;
+    o->forward_pairs = p.n_fwd_pairs;
+    o->backward_pairs = p.n_bwd_pairs;
+    o->rcond0 = p.rcond0;
+    return 0;
+}
+
+int gbpf_get_stats(gbpf_solver* s, gbpf_stats* o) {
+    if (!s || !o) return fail("null argument");
+    *o = s->last;
+    return 0;
+}
+
+int gbpf_get_posmap(gbpf_solver* s, int32_t* out) {
+    if (!s || !out) return fail("null argument");
+    std::copy(s->plan.posmap.begin(), s->plan.posmap.end(), out);
+    return 0;
+}
+
+int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out) {
+    if (!s || !out) return fail("null argument");
+    std::copy(s->plan.row_of_bus.begin(), s->plan.row_of_bus.end(), out);
+    return 0;
+}
+
+int gbpf_solve_batch_device(gbpf_solver* s, int T, const double* dS, int s_per_col, const double* dV0,
+                            int v0_per_col, const gbpf_params* pp, double* dV, int32_t* dit, uint8_t* dcv) {
+    if (!s) return fail("null solver");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (T <= 0) return fail("solve_batch: T (time steps) must be > 0");
+    if (int rc = check_params(p, "solve_batch")) return rc;
+    gbpf::Batch b{};
+    b.B = T;
+    b.S = reinterpret_cast<const double2*>(dS);
+    b.s_shared = !s_per_col;
+    b.sS = T;
+    b.V0 = reinterpret_cast<const double2*>(dV0);
+    b.v0_shared = !v0_per_col;
+    b.sV0 = T;
+    b.ymode = 0;
+    b.Vout = reinterpret_cast<double2*>(dV);
+    b.sV = T;
+    b.iters = dit;
+    b.conv = dcv;
+    fill_common(b, s, p);
+    return run(s, b, T, "solve_batch");
+}
+
+int gbpf_solve_batch(gbpf_solver* s, int T, const double* S, int s_per_col, const double* V0, int v0_per_col,
+                     const gbpf_params* pp, double* V, int32_t* it, uint8_t* cv) {
+    if (!s) return fail("null solver");
+    if (T <= 0) return fail("solve_batch: T (time steps) must be > 0");
+    const size_t n = s->n;
+    const size_t sb = n * (s_per_col ? T : 1) * 16, vb = n * (v0_per_col ? T : 1) * 16, ob = n * (size_t)T * 16;
+    CK(s->bS.ensure(sb));
+    CK(s->bV0.ensure(vb));
+    CK(s->bV.ensure(ob));
+    CK(s->bit.ensure((size_t)T * 4));
+    CK(s->bcv.ensure((size_t)T));
+    CK(cudaMemcpyAsync(s->bS.p, S, sb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bV0.p, V0, vb, cudaMemcpyHostToDevice, s->stream));
+    if (int rc = gbpf_solve_batch_device(s, T, s->bS.as<double>(), s_per_col, s->bV0.as<double>(), v0_per_col, pp,
+                                         s->bV.as<double>(), s->bit.as<int32_t>(), s->bcv.as<uint8_t>()))
+        return rc;
+    CK(cudaMemcpyAsync(V, s->bV.p, ob, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(it, s->bit.p, (size_t)T * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(cv, s->bcv.p, (size_t)T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int gbpf_solve_lanes_device(gbpf_solver* s, int T, const double* dS, const double* dV0, int K, const int64_t* doff,
+                            const gbpf_params* pp, double* dV, int32_t* dit, uint8_t* dcv) {
+    if (!s) return fail("null solver");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (T <= 0) return fail("solve_lanes: T (time steps) must be > 0");
+    if (K <= 0) return fail("solve_lanes: K (lanes) must be > 0");
+    if (int rc = check_params(p, "solve_lanes")) return rc;
+    gbpf::Batch b{};
+    b.B = T;
+    b.lanes = 1;
+    b.K = K;
+    b.lane_off = reinterpret_cast<const long long*>(doff);
+    b.S = reinterpret_cast<const double2*>(dS);
+    b.s_shared = 0;
+    b.sS = T;
+    b.V0 = reinterpret_cast<const double2*>(dV0);
+    b.v0_shared = 1;
+    b.sV0 = 0;
+    b.ymode = 0;
+    b.Vout = reinterpret_cast<double2*>(dV);
+    b.sV = T;
+    b.iters = dit;
+    b.conv = dcv;
+    fill_common(b, s, p);
+    return run(s, b, K, "solve_lanes");
+}
+
+int gbpf_solve_lanes(gbpf_solver* s, int T, const double* S, const double* V0, int K, const int64_t* off,
+                     const gbpf_params* pp, double* V, int32_t* it, uint8_t* cv) {
+    if (!s) return fail("null solver");
+    if (T <= 0 || K <= 0) return fail("solve_lanes: T and K must be > 0");
+    if (off[0] != 0 || off[K] != T) return fail("solve_lanes: offsets must start at 0 and end at T");
+    for (int l = 0; l < K; ++l)
+        if (off[l + 1] < off[l]) return fail("solve_lanes: offsets must be non-decreasing");
+    const size_t n = s->n;
+    const size_t sb = n * (size_t)T * 16, vb = n * 16;
+    CK(s->bS.ensure(sb));
+    CK(s->bV0.ensure(vb));
+    CK(s->bV.ensure(sb));
+    CK(s->bit.ensure((size_t)T * 4));
+    CK(s->bcv.ensure((size_t)T));
+    CK(s->blane.ensure((size_t)(K + 1) * 8));
+    CK(cudaMemcpyAsync(s->bS.p, S, sb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bV0.p, V0, vb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->blane.p, off, (size_t)(K + 1) * 8, cudaMemcpyHostToDevice, s->stream));
+    if (int rc = gbpf_solve_lanes_device(s, T, s->bS.as<double>(), s->bV0.as<double>(), K, s->blane.as<int64_t>(), pp,
+                                         s->bV.as<double>(), s->bit.as<int32_t>(), s->bcv.as<uint8_t>()))
+        return rc;
+    CK(cudaMemcpyAsync(V, s->bV.p, sb, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(it, s->bit.p, (size_t)T * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(cv, s->bcv.p, (size_t)T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double* V0, const uint8_t* pin,
+                           const double* Yd, const int32_t* st_ptr, const int32_t* st_k, const double* st_val,
+                           const gbpf_params* pp, double* V, int32_t* it, uint8_t* cv) {
+    if (!s) return fail("null solver");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (L <= 0) return fail("solve_batch_contingency: no cases");
+    if (int rc = check_params(p, "solve_batch_contingency")) return rc;
+    const size_t n = s->n, nnz = s->nnz;
+    CK(s->bS.ensure(n * 16));
+    CK(s->bV0.ensure(n * (size_t)L * 16));
+    CK(s->bV.ensure(n * (size_t)L * 16));
+    CK(s->bit.ensure((size_t)L * 4));
+    CK(s->bcv.ensure((size_t)L));
+    CK(cudaMemcpyAsync(s->bS.p, S, n * 16, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bV0.p, V0, n * (size_t)L * 16, cudaMemcpyHostToDevice, s->stream));
+    gbpf::Batch b{};
+    b.B = L;
+    b.S = s->bS.as<double2>();
+    b.s_shared = 1;
+    b.V0 = s->bV0.as<double2>();
+    b.v0_shared = 0;
+    b.sV0 = L;
+    if (pin) {
+        CK(s->bpin.ensure(n * (size_t)L));
+        CK(cudaMemcpyAsync(s->bpin.p, pin, n * (size_t)L, cudaMemcpyHostToDevice, s->stream));
+        b.pin = s->bpin.as<uint8_t>();
+        b.spin = L;
+    }
+    if (Yd) {
+        CK(s->bYd.ensure(nnz * (size_t)L * 16));
+        CK(cudaMemcpyAsync(s->bYd.p, Yd, nnz * (size_t)L * 16, cudaMemcpyHostToDevice, s->stream));
+        b.ymode = 2;
+        b.Yd = s->bYd.as<double2>();
+        b.sYd = L;
+    } else if (st_ptr) {
+        const int ne = st_ptr[L];
+        for (int c = 0; c < L; ++c)
+            if (st_ptr[c + 1] - st_ptr[c] > gbpf::MAX_STAMPS)
+                return fail("solve_batch_contingency_stamp: case " + std::to_string(c) + " has more than " +
+                            std::to_string(gbpf::MAX_STAMPS) + " stamp entries");
+        for (int e = 0; e < ne; ++e)
+            if (st_k[e] < 0 || st_k[e] >= (int)nnz) return fail("solve_batch_contingency_stamp: stamp row out of range");
+        CK(s->bstp.ensure((size_t)(L + 1) * 4));
+        CK(s->bstk.ensure((size_t)std::max(ne, 1) * 4));
+        CK(s->bstv.ensure((size_t)std::max(ne, 1) * 16));
+        CK(cudaMemcpyAsync(s->bstp.p, st_ptr, (size_t)(L + 1) * 4, cudaMemcpyHostToDevice, s->stream));
+        if (ne) {
+            CK(cudaMemcpyAsync(s->bstk.p, st_k, (size_t)ne * 4, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(s->bstv.p, st_val, (size_t)ne * 16, cudaMemcpyHostToDevice, s->stream));
+        }
+        b.ymode = 1;
+        b.st_ptr = s->bstp.as<int>();
+        b.st_k = s->bstk.as<int>();
+        b.st_v = s->bstv.as<double2>();
+    }
+    b.Vout = s->bV.as<double2>();
+    b.sV = L;
+    b.iters = s->bit.as<int32_t>();
+    b.conv = s->bcv.as<uint8_t>();
+    fill_common(b, s, p);
+    if (int rc = run(s, b, L, "solve_batch_contingency")) return rc;
+    CK(cudaMemcpyAsync(V, s->bV.p, n * (size_t)L * 16, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(it, s->bit.p, (size_t)L * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(cv, s->bcv.p, (size_t)L, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const uint8_t* pin, double* blocks,
+                       double* residual) {
+    if (!s) return fail("null solver");
+    const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv);
+    DBuf dV, dSb, dpin, dVt, dEt, dV32, dblk, dR;
+    auto cleanup = [&]() {
+        for (DBuf* b : {&dV, &dSb, &dpin, &dVt, &dEt, &dV32, &dblk, &dR}) b->release();
+    };
+    struct Guard {
+        std::function<void()> f;
+        ~Guard() { f(); }
+    } guard{cleanup};
+    CK(dV.ensure(n * 16));
+    CK(dSb.ensure(n * 16));
+    CK(dVt.ensure(n * 32));
+    CK(dEt.ensure(n * 16));
+    CK(dV32.ensure(n * 16));
+    CK(dblk.ensure(nb * 32));
+    CK(dR.ensure(nv * 16));
+    CK(cudaMemcpy(dV.p, V, n * 16, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dSb.p, S, n * 16, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dblk.p, 0, nb * 32));
+    CK(cudaMemset(dR.p, 0, nv * 16));
+    if (pin) {
+        CK(dpin.ensure(n));
+        CK(cudaMemcpy(dpin.p, pin, n, cudaMemcpyHostToDevice));
+    }
+    CK(gbpf::launch_eval_debug(s->dp, dV.as<double2>(), dSb.as<double2>(), pin ? dpin.as<uint8_t>() : nullptr,
+                               dVt.as<double4_32a>(), dEt.as<double2>(), dV32.as<float4>(), dblk.as<double4_32a>(),
+                               dR.as<double2>(), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(blocks, dblk.p, nb * 32, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(residual, dR.p, (size_t)s->plan.nv * 16, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+void* gbpf_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+        fail("cudaMallocHost failed");
+        return nullptr;
+    }
+    return p;
+}
+
+void gbpf_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

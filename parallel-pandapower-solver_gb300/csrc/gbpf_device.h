@@ -1,0 +1,118 @@
+// gbpf_device.h -- structures shared by the host orchestration and the sm_103a kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+namespace gbpf {
+
+// slot states of the persistent Newton kernel
+enum SlotState : int {
+    SL_EMPTY = 0,      // needs a case
+    SL_FRESH = 1,      // case loaded: evaluate at the start point
+    SL_ACTIVE = 2,     // take a Newton step (factor + solve + full step)
+    SL_BACKTRACK = 3,  // line search trial: mismatch only
+    SL_NEEDJ = 4,      // line search done: mismatch + Jacobian at the accepted point
+    SL_FINISH = 5,     // write the result back
+    SL_RETIRED = 6,    // no more work
+};
+
+constexpr int MAX_SLOTS = 32;    // cases per CTA (G) upper bound
+constexpr int MAX_STAMPS = 32;   // outage-stamp entries per case held in shared memory
+
+// error codes written to Batch::err[0] (first error wins; err[1..2] = bus, case)
+enum DevError : int {
+    DE_NONE = 0,
+    DE_V0_NONFINITE = 1,
+    DE_V0_MAGNITUDE = 2,
+    DE_STAMPS = 3,
+};
+
+struct DevPlan {
+    int n, nv, nblk, W, nlev, nblev, nnzY;
+    const int* Yp;
+    const int* Yj;
+    const double2* Y;        // base Ybus values (G + jB)
+    const float2* Y32;       // float copy
+    const int* posmap;       // Ybus nnz -> block, -1
+    const int* row_of_bus;   // bus -> block row, -1 for slack
+    const uint8_t* bus_pq;
+    const int4* taskA;
+    const int* ptrA;
+    const int2* scl;
+    const int* ptrB;
+    const int4* taskC;
+    const int* ptrC;
+    const int2* pairs;
+    const uint8_t* row_pq;   // block row is PQ (two real pivots)
+    const int* bus_of_row;
+    const int* dpos;         // block row -> its diagonal block (base)
+};
+
+struct Batch {
+    int B;                   // cases (independent mode) or total hours (lanes mode)
+    int lanes;               // 0: independent cases; 1: warm-start lanes
+    int K;                   // lanes
+    const long long* lane_off;
+    const double2* S;        // injections: S[bus * sS + case] or S[bus] if s_shared
+    int s_shared;
+    long long sS;
+    const double2* V0;       // start voltage: V0[bus * sV0 + case] or V0[bus] if shared
+    int v0_shared;
+    long long sV0;
+    int check_v0;            // validate V0 like nr_klu's solve_batch
+    int ymode;               // 0 base Ybus, 1 base minus per-case stamps, 2 dense per case
+    const int* st_ptr;       // stamps of case c: [st_ptr[c], st_ptr[c+1])
+    const int* st_k;
+    const double2* st_v;
+    const double2* Yd;       // dense per-case Ybus Yd[k * sYd + case]
+    long long sYd;
+    const uint8_t* pin;      // pin[bus * spin + case] or null
+    long long spin;
+    double2* Vout;           // result Vout[bus * sV + case]
+    long long sV;
+    int* iters;
+    uint8_t* conv;
+    int max_iter;
+    double tol;
+    int line_search;
+    int mixed;               // 0: all factorizations double; 1: vote per case
+    double mixed_switch;
+    double rcond_min64;
+    double rcond_min32;
+    int* counter;            // work counter, zero before launch
+    unsigned long long* stats;  // [0] fp32 factorizations [1] fp64 [2] fp32 rejected [3] fp64 rejected [4] macro steps
+    int* err;                // [0] code [1] bus [2] case
+};
+
+struct Scratch {
+    int G, log2G;
+    size_t blk_stride;       // per-CTA elements (blocks) of the factor arrays = nblk*G
+    size_t row_stride;       // nv*G
+    size_t bus_stride;       // n*G
+    double4_32a* fac64;          // [cta][blk][slot] (a00 a01 a10 a11)
+    float4* fac32;
+    double2* R;              // [cta][row][slot] residual (P, Q) = S - S(V)
+    double2* y64;            // [cta][row][slot] step
+    float2* y32;
+    double4_32a* Vc;             // committed point (Vm, Va, cos, sin)
+    double4_32a* Vt;             // evaluation point (Vm, Va, cos, sin)
+    double2* Et;             // evaluation point rectangular (e, f)
+    float4* V32;             // evaluation point (Vm, cos, sin, 0) in float
+    uint8_t* pin;            // [cta][bus][slot]
+};
+
+// host-side launchers (gbpf_kernels.cu)
+cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
+                          cudaStream_t stream);
+cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
+                              double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R,
+                              cudaStream_t stream);
+int newton_max_threads();
+void set_error(const std::string& msg);  // message returned by gbpf_last_error()
+const void* newton_kernel_ptr();
+
+}  // namespace gbpf

@@ -1,0 +1,800 @@
+// gbpf_kernels.cu -- GB300 (sm_103a) kernels of the batched polar Newton-Raphson solver.
+//
+// One PERSISTENT kernel runs the whole Newton iteration of nr_klu.cpp:569-711 on the
+// device for a batch of cases (time steps, outages, scenarios). Each CTA owns G case
+// "slots" and loops: refill empty slots from a global work counter -> batched 2x2-block
+// LU + substitutions for the slots that take a step -> voltage update -> fused mismatch /
+// Jacobian evaluation -> per-slot Armijo/convergence decision -> write back finished
+// cases. Cases retire independently and their slot is refilled at once (continuous
+// batching inside the launch); there is no host round trip per Newton pass (the
+// reference reads a status word back every pass, nr_polar_solver.py:932-933), no
+// per-iteration launches, and no inter-CTA waiting of any kind (the only cross-CTA
+// operation is the atomicAdd that hands out work).
+//
+// The per-CTA working set lives in global memory and is reused case after case (it stays
+// L2-resident): factor blocks [blk][slot] (the G slots of one block are contiguous, so a
+// worker's G lanes read one 128/256-byte line per operand), residual and step [row][slot],
+// voltage state [bus][slot].
+//
+// Precision: mismatch, power injections, convergence norm and voltage update are always
+// double. With `mixed`, a slot's Jacobian, factors and substitutions are float while its
+// vote says so (the vote rules of nr_polar_kernels.cu:209-228), double otherwise; a float
+// factorization that fails the pivot check is redone in double within the same step.
+#include <cfloat>
+#include <cstdint>
+
+#include "gbpf_device.h"
+
+namespace gbpf {
+
+#define NT_NEWTON 512
+
+constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
+constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
+constexpr double BIG = DBL_MAX;    // nr_klu.cpp:434 NONFINITE_NORM
+
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ double bitsd(unsigned long long b) { return __longlong_as_double((long long)b); }
+__device__ __forceinline__ bool finite_d(double x) {
+    return (dbits(x) & 0x7ff0000000000000ULL) != 0x7ff0000000000000ULL;
+}
+
+// cos/sin of a small angle |d| <= 1/4 from their Maclaurin series (Horner in d^2); the
+// truncation error is below 3e-18 on that range. Used to ROTATE a bus phasor by the
+// Newton angle increment instead of evaluating sincos of the full angle.
+__device__ __forceinline__ void sincos_small(double d, double* s, double* c) {
+    const double z = d * d;
+    double ps = -1.0 / 39916800.0;
+    ps = fma(ps, z, 1.0 / 362880.0);
+    ps = fma(ps, z, -1.0 / 5040.0);
+    ps = fma(ps, z, 1.0 / 120.0);
+    ps = fma(ps, z, -1.0 / 6.0);
+    *s = fma(ps * z, d, d);
+    double pc = 1.0 / 479001600.0;
+    pc = fma(pc, z, -1.0 / 3628800.0);
+    pc = fma(pc, z, 1.0 / 40320.0);
+    pc = fma(pc, z, -1.0 / 720.0);
+    pc = fma(pc, z, 1.0 / 24.0);
+    pc = fma(pc, z, -0.5);
+    *c = fma(pc, z, 1.0);
+}
+
+// --------------------------------------------------------------------------------------
+// Evaluation of one bus row for one slot. Off-diagonal Ybus entry (i, j), phasors u = V/|V|:
+//   X = u_i conj(Y_ij u_j) = |Y| e^{j delta},  delta = th_i - angle(Y_ij) - th_j,
+//   W = Vm_i Vm_j X        (real / imaginary part: the P / Q flow term of the entry).
+// Jacobian block (i, j) = [dP/dth_j dP/dVm_j; dQ/dth_j dQ/dVm_j] = [Im W, Vm_i Re X;
+// -Re W, Vm_i Im X]; the diagonal block accumulates the negated off-diagonal angle terms
+// and the magnitude terms: the formulas of nr_klu.cpp:344-378 in this notation. PV buses
+// carry an identity dummy in their magnitude column and Q row; pinned buses
+// (nr_klu.cpp:398-423) get identity rows and a zero residual.
+// --------------------------------------------------------------------------------------
+struct EvalCtx {
+    const DevPlan* P;
+    const double4_32a* Vt;   // [bus][slot] (Vm, Va, cos, sin)
+    const double2* Et;   // [bus][slot] (e, f)
+    const float4* V32;   // [bus][slot] (Vm, cos, sin, 0)
+    int lg;
+    int ymode;
+    const double2* Yd;
+    long long sYd;
+    int ncase;
+    int nst;
+    const int* stk;
+    const double2* stv;
+};
+
+__device__ __forceinline__ unsigned row_stamp_mask(const EvalCtx& c, int k0, int k1) {
+    unsigned mask = 0;
+    if (c.ymode == 1)
+        for (int e = 0; e < c.nst; ++e)
+            if (c.stk[e] >= k0 && c.stk[e] < k1) mask |= 1u << e;
+    return mask;
+}
+
+__device__ __forceinline__ double2 ybus_val(const EvalCtx& c, int k, unsigned mask) {
+    double2 y = c.ymode == 2 ? c.Yd[(size_t)k * c.sYd + c.ncase] : c.P->Y[k];
+    if (mask) {
+        for (int e = 0; e < c.nst; ++e)
+            if (((mask >> e) & 1u) && c.stk[e] == k) {
+                y.x -= c.stv[e].x;
+                y.y -= c.stv[e].y;
+            }
+    }
+    return y;
+}
+
+__device__ __forceinline__ void put_block(double4_32a* fac, size_t at, double4_32a o) { fac[at] = o; }
+__device__ __forceinline__ void put_block(float4* fac, size_t at, double4_32a o) {
+    fac[at] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
+}
+
+// Double-precision row: mismatch from the W terms, Jacobian (if WJ) into `fac`.
+template <bool WJ, typename FacT>
+__device__ double eval_row_x(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp,
+                             FacT* fac, double2* R, bool write_r) {
+    const DevPlan& P = *c.P;
+    const double4_32a vi4 = c.Vt[((size_t)i << c.lg) + s];
+    const double vi = vi4.x, ci = vi4.z, si = vi4.w;
+    double Pc = 0.0, Qc = 0.0, dPa = 0.0, dQa = 0.0, dPm = 0.0, dQm = 0.0;
+    const int k0 = P.Yp[i], k1 = P.Yp[i + 1];
+    const unsigned mask = row_stamp_mask(c, k0, k1);
+    for (int k = k0; k < k1; ++k) {
+        const int j = P.Yj[k];
+        const double2 y = ybus_val(c, k, mask);
+        if (j != i) {
+            const double4_32a vj4 = c.Vt[((size_t)j << c.lg) + s];
+            const double vj = vj4.x, cj = vj4.z, sj = vj4.w;
+            const double wr = y.x * cj - y.y * sj, wi = y.x * sj + y.y * cj;
+            const double xr = ci * wr + si * wi, xi = si * wr - ci * wi;
+            const double vx = vi * xr, vy = vi * xi;
+            const double Wr = vx * vj, Wi = vy * vj;
+            Pc += Wr;
+            Qc += Wi;
+            if (WJ) {
+                dPa -= Wi;
+                dQa += Wr;
+                dPm += vj * xr;
+                dQm += vj * xi;
+                const int q = P.posmap[k];
+                if (q >= 0) {
+                    const bool pq_j = P.bus_pq[j] != 0;
+                    double4_32a o;
+                    if (pinned) {
+                        o = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+                    } else {
+                        o.x = Wi;
+                        o.y = pq_j ? vx : 0.0;
+                        o.z = pq_i ? -Wr : 0.0;
+                        o.w = (pq_i && pq_j) ? vy : 0.0;
+                    }
+                    put_block(fac, ((size_t)q << c.lg) + s, o);
+                }
+            }
+        } else {
+            Pc += vi * vi * y.x;
+            Qc -= vi * vi * y.y;
+            if (WJ) {
+                dPm += 2.0 * vi * y.x;
+                dQm -= 2.0 * vi * y.y;
+            }
+        }
+    }
+    if (WJ) {
+        const double4_32a o = pinned ? make_double4_32a(1.0, 0.0, 0.0, 1.0)
+                                 : make_double4_32a(dPa, pq_i ? dPm : 0.0, pq_i ? dQa : 0.0, pq_i ? dQm : 1.0);
+        put_block(fac, ((size_t)P.dpos[row] << c.lg) + s, o);
+    }
+    const double rp = pinned ? 0.0 : Ssp.x - Pc;
+    const double rq = (pinned || !pq_i) ? 0.0 : Ssp.y - Qc;
+    if (write_r) R[((size_t)row << c.lg) + s] = make_double2(rp, rq);
+    const double a = fabs(rp), b = fabs(rq);
+    return (b > a || b != b) ? b : a;
+}
+
+// Mixed-precision row: mismatch in double from rectangular coordinates,
+//   I_i = sum_j Y_ij V_j,  P + jQ = V_i conj(I_i),
+// (four double FMAs per entry), and the Jacobian (if WJ) in float from the float copy of
+// the state (same formulas as eval_row_x).
+template <bool WJ>
+__device__ double eval_row_mixed(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp,
+                                 float4* fac, double2* R) {
+    const DevPlan& P = *c.P;
+    const double2 ei = c.Et[((size_t)i << c.lg) + s];
+    double Ir = 0.0, Ii = 0.0;
+    float dPa = 0.f, dQa = 0.f, dPm = 0.f, dQm = 0.f;
+    float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (WJ) vi32 = c.V32[((size_t)i << c.lg) + s];
+    const int k0 = P.Yp[i], k1 = P.Yp[i + 1];
+    const unsigned mask = row_stamp_mask(c, k0, k1);
+    for (int k = k0; k < k1; ++k) {
+        const int j = P.Yj[k];
+        const double2 y = ybus_val(c, k, mask);
+        const double2 ej = c.Et[((size_t)j << c.lg) + s];
+        Ir = fma(y.x, ej.x, fma(-y.y, ej.y, Ir));
+        Ii = fma(y.x, ej.y, fma(y.y, ej.x, Ii));
+        if (WJ) {
+            float gx, gy;
+            if (c.ymode == 0 && !mask) {
+                const float2 y32 = P.Y32[k];
+                gx = y32.x;
+                gy = y32.y;
+            } else {
+                gx = (float)y.x;
+                gy = (float)y.y;
+            }
+            if (j != i) {
+                const float4 vj = c.V32[((size_t)j << c.lg) + s];
+                const float wr = gx * vj.y - gy * vj.z, wi = gx * vj.z + gy * vj.y;
+                const float xr = vi32.y * wr + vi32.z * wi, xi = vi32.z * wr - vi32.y * wi;
+                const float vx = vi32.x * xr, vy = vi32.x * xi;
+                const float Wr = vx * vj.x, Wi = vy * vj.x;
+                dPa -= Wi;
+                dQa += Wr;
+                dPm += vj.x * xr;
+                dQm += vj.x * xi;
+                const int q = P.posmap[k];
+                if (q >= 0) {
+                    const bool pq_j = P.bus_pq[j] != 0;
+                    float4 o;
+                    if (pinned) {
+                        o = make_float4(0.f, 0.f, 0.f, 0.f);
+                    } else {
+                        o.x = Wi;
+                        o.y = pq_j ? vx : 0.f;
+                        o.z = pq_i ? -Wr : 0.f;
+                        o.w = (pq_i && pq_j) ? vy : 0.f;
+                    }
+                    fac[((size_t)q << c.lg) + s] = o;
+                }
+            } else {
+                dPm += 2.f * vi32.x * gx;
+                dQm -= 2.f * vi32.x * gy;
+            }
+        }
+    }
+    if (WJ) {
+        const float4 o = pinned ? make_float4(1.f, 0.f, 0.f, 1.f)
+                                : make_float4(dPa, pq_i ? dPm : 0.f, pq_i ? dQa : 0.f, pq_i ? dQm : 1.f);
+        fac[((size_t)P.dpos[row] << c.lg) + s] = o;
+    }
+    const double Pc = fma(ei.x, Ir, ei.y * Ii);
+    const double Qc = fma(ei.y, Ir, -ei.x * Ii);
+    const double rp = pinned ? 0.0 : Ssp.x - Pc;
+    const double rq = (pinned || !pq_i) ? 0.0 : Ssp.y - Qc;
+    R[((size_t)row << c.lg) + s] = make_double2(rp, rq);
+    const double a = fabs(rp), b = fabs(rq);
+    return (b > a || b != b) ? b : a;
+}
+
+// ---------------------------------------------------------------------------- block LU
+template <typename T>
+struct V4;
+template <>
+struct V4<double> {
+    using t = double4_32a;
+    using t2 = double2;
+};
+template <>
+struct V4<float> {
+    using t = float4;
+    using t2 = float2;
+};
+
+template <typename T>
+__device__ __forceinline__ T z4() {
+    T r;
+    r.x = r.y = r.z = r.w = 0;
+    return r;
+}
+
+// acc -= a * b (2x2 blocks, row-major)
+template <typename B4>
+__device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
+    acc.x -= a.x * b.x + a.y * b.z;
+    acc.y -= a.x * b.y + a.y * b.w;
+    acc.z -= a.z * b.x + a.w * b.z;
+    acc.w -= a.z * b.y + a.w * b.w;
+}
+
+// One batched factorization + substitution pass over the slots flagged in `on` (G <= 32).
+// Worker w = (warp, lane / G) runs its task list of every level for its G slot lanes;
+// the CTA meets at a barrier after each level's entry phase and scale phase, and after
+// each backward level. Pivot statistics per slot go to smin / smax (as ordered bits).
+template <typename real>
+__device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
+                        const int* on, int lg, unsigned long long* smin, unsigned long long* smax) {
+    using B4 = typename V4<real>::t;
+    using B2 = typename V4<real>::t2;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int s = lane & ((1 << lg) - 1);
+    const int w = (tid >> 5) * (32 >> lg) + (lane >> lg);
+    const int W = P.W;
+    const bool act = on[s] != 0;
+    double pmin = DBL_MAX, pmax = 0.0;
+    for (int h = 0; h < P.nlev; ++h) {
+        if (act) {
+            const int t0 = P.ptrA[h * W + w], t1 = P.ptrA[h * W + w + 1];
+            for (int t = t0; t < t1; ++t) {
+                const int4 task = P.taskA[t];
+                const int kind = task.y & 3;
+                if (kind == 3) {  // forward substitution of block row task.x
+                    const double2 r = R[((size_t)task.x << lg) + s];
+                    real y0 = (real)r.x, y1 = (real)r.y;
+                    for (int p = task.z; p < task.w; ++p) {
+                        const int2 pr = P.pairs[p];
+                        const B4 l = fac[((size_t)pr.x << lg) + s];
+                        const B2 ys = y[((size_t)pr.y << lg) + s];
+                        y0 -= l.x * ys.x + l.y * ys.y;
+                        y1 -= l.z * ys.x + l.w * ys.y;
+                    }
+                    B2 o;
+                    o.x = y0;
+                    o.y = y1;
+                    y[((size_t)task.x << lg) + s] = o;
+                    continue;
+                }
+                B4 acc = (task.y & 16) ? z4<B4>() : fac[((size_t)task.x << lg) + s];
+                for (int p = task.z; p < task.w; ++p) {
+                    const int2 pr = P.pairs[p];
+                    const B4 a = fac[((size_t)pr.x << lg) + s];
+                    const B4 b = fac[((size_t)pr.y << lg) + s];
+                    mm_sub(acc, a, b);
+                }
+                if (kind == 0) {
+                    const real det = acc.x * acc.w - acc.y * acc.z;
+                    const double u0 = fabs((double)acc.x);
+                    pmin = fmin(pmin, u0);
+                    pmax = (u0 > pmax || u0 != u0) ? u0 : pmax;
+                    if (task.y & 32) {
+                        const double u1 = fabs((double)det / (double)acc.x);
+                        pmin = fmin(pmin, u1);
+                        pmax = (u1 > pmax || u1 != u1) ? u1 : pmax;
+                    }
+                    const real inv = (real)1 / det;
+                    B4 o;
+                    o.x = acc.w * inv;
+                    o.y = -acc.y * inv;
+                    o.z = -acc.z * inv;
+                    o.w = acc.x * inv;
+                    fac[((size_t)task.x << lg) + s] = o;
+                } else {
+                    fac[((size_t)task.x << lg) + s] = acc;
+                }
+            }
+        }
+        __syncthreads();
+        if (act) {
+            const int t0 = P.ptrB[h * W + w], t1 = P.ptrB[h * W + w + 1];
+            for (int t = t0; t < t1; ++t) {
+                const int2 sc = P.scl[t];
+                const B4 l = fac[((size_t)sc.x << lg) + s];
+                const B4 d = fac[((size_t)sc.y << lg) + s];
+                B4 o;
+                o.x = l.x * d.x + l.y * d.z;
+                o.y = l.x * d.y + l.y * d.w;
+                o.z = l.z * d.x + l.w * d.z;
+                o.w = l.z * d.y + l.w * d.w;
+                fac[((size_t)sc.x << lg) + s] = o;
+            }
+        }
+        __syncthreads();
+    }
+    for (int h = 0; h < P.nblev; ++h) {
+        if (act) {
+            const int t0 = P.ptrC[h * W + w], t1 = P.ptrC[h * W + w + 1];
+            for (int t = t0; t < t1; ++t) {
+                const int4 task = P.taskC[t];
+                const B2 yr = y[((size_t)task.x << lg) + s];
+                real r0 = yr.x, r1 = yr.y;
+                for (int p = task.z; p < task.w; ++p) {
+                    const int2 pr = P.pairs[p];
+                    const B4 u = fac[((size_t)pr.x << lg) + s];
+                    const B2 yj = y[((size_t)pr.y << lg) + s];
+                    r0 -= u.x * yj.x + u.y * yj.y;
+                    r1 -= u.z * yj.x + u.w * yj.y;
+                }
+                const B4 d = fac[((size_t)task.y << lg) + s];
+                B2 o;
+                o.x = d.x * r0 + d.y * r1;
+                o.y = d.z * r0 + d.w * r1;
+                y[((size_t)task.x << lg) + s] = o;
+            }
+        }
+        __syncthreads();
+    }
+    if (act) {
+        atomicMin(&smin[s], dbits(pmin));
+        atomicMax(&smax[s], dbits(pmax));
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long long bmax, double rc) {
+    if (bmax >= 0x7ff0000000000000ULL) return false;  // NaN / Inf pivot
+    const double mn = bitsd(bmin), mx = bitsd(bmax);
+    return mn > 0.0 && mn >= rc * mx;
+}
+
+// ------------------------------------------------------------------------- the kernel
+__global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
+    const int G = Sc.G, lg = Sc.log2G;
+    const int tid = threadIdx.x;
+    const int NT = blockDim.x;
+    const size_t cta = blockIdx.x;
+    double4_32a* fac64 = Sc.fac64 ? Sc.fac64 + cta * Sc.blk_stride : nullptr;
+    float4* fac32 = Sc.fac32 ? Sc.fac32 + cta * Sc.blk_stride : nullptr;
+    double2* R = Sc.R + cta * Sc.row_stride;
+    double2* y64 = Sc.y64 + cta * Sc.row_stride;
+    float2* y32 = Sc.y32 ? Sc.y32 + cta * Sc.row_stride : nullptr;
+    double4_32a* Vc = Sc.Vc + cta * Sc.bus_stride;
+    double4_32a* Vt = Sc.Vt + cta * Sc.bus_stride;
+    double2* Et = Sc.Et + cta * Sc.bus_stride;
+    float4* V32 = Sc.V32 + cta * Sc.bus_stride;
+    uint8_t* spin = Sc.pin + cta * Sc.bus_stride;
+    const int n = P.n;
+    const int nG = n << lg;
+
+    __shared__ int s_st[MAX_SLOTS], s_case[MAX_SLOTS], s_it[MAX_SLOTS], s_vote[MAX_SLOTS], s_trial[MAX_SLOTS];
+    __shared__ int s_conv[MAX_SLOTS], s_jprec[MAX_SLOTS], s_yprec[MAX_SLOTS], s_warm[MAX_SLOTS];
+    __shared__ int s_on32[MAX_SLOTS], s_on64[MAX_SLOTS], s_reeval[MAX_SLOTS];
+    __shared__ long long s_lcur[MAX_SLOTS], s_lend[MAX_SLOTS];
+    __shared__ double s_nrm[MAX_SLOTS], s_alpha[MAX_SLOTS], s_balpha[MAX_SLOTS], s_bnrm[MAX_SLOTS];
+    __shared__ unsigned long long s_res[MAX_SLOTS], s_pmin[MAX_SLOTS], s_pmax[MAX_SLOTS];
+    __shared__ int s_nst[MAX_SLOTS];
+    __shared__ int s_stk[MAX_SLOTS][MAX_STAMPS];
+    __shared__ double2 s_stv[MAX_SLOTS][MAX_STAMPS];
+
+    if (tid < G) {
+        s_st[tid] = SL_EMPTY;
+        s_lcur[tid] = s_lend[tid] = 0;
+        s_warm[tid] = 0;
+        s_nst[tid] = 0;
+        s_jprec[tid] = 0;
+        s_vote[tid] = 0;
+    }
+    __syncthreads();
+
+    for (;;) {
+        // ---------------------------------------------------------------- refill
+        if (tid < G) {
+            const int s = tid;
+            if (s_st[s] == SL_EMPTY) {
+                long long c = -1;
+                if (Bt.lanes) {
+                    if (s_lcur[s] < s_lend[s]) {
+                        c = s_lcur[s]++;
+                    } else {
+                        for (;;) {  // bounded: every pass consumes one lane
+                            const int l = atomicAdd(Bt.counter, 1);
+                            if (l >= Bt.K) break;
+                            s_lcur[s] = Bt.lane_off[l];
+                            s_lend[s] = Bt.lane_off[l + 1];
+                            s_warm[s] = 0;
+                            if (s_lcur[s] < s_lend[s]) {
+                                c = s_lcur[s]++;
+                                break;
+                            }
+                        }
+                    }
+                } else {
+                    const int ci = atomicAdd(Bt.counter, 1);
+                    if (ci < Bt.B) c = ci;
+                }
+                if (c < 0) {
+                    s_st[s] = SL_RETIRED;
+                } else {
+                    s_case[s] = (int)c;
+                    s_st[s] = SL_FRESH;
+                    s_it[s] = 0;
+                    s_conv[s] = 0;
+                    s_vote[s] = Bt.mixed ? 1 : 0;
+                    int nst = 0;
+                    if (Bt.ymode == 1) {
+                        const int e0 = Bt.st_ptr[c], e1 = Bt.st_ptr[c + 1];
+                        nst = e1 - e0;
+                        if (nst > MAX_STAMPS) {
+                            if (atomicCAS(&Bt.err[0], 0, DE_STAMPS) == 0) {
+                                Bt.err[1] = nst;
+                                Bt.err[2] = (int)c;
+                            }
+                            nst = MAX_STAMPS;
+                        }
+                        for (int e = 0; e < nst; ++e) {
+                            s_stk[s][e] = Bt.st_k[e0 + e];
+                            s_stv[s][e] = Bt.st_v[e0 + e];
+                        }
+                    }
+                    s_nst[s] = nst;
+                }
+            }
+            if (s_st[s] == SL_ACTIVE) s_it[s] += 1;
+        }
+        const int alive = __syncthreads_or(tid < G && s_st[tid] != SL_RETIRED);
+        if (!alive) break;
+
+        // ---------------------------------------------------------------- load
+        for (int idx = tid; idx < nG; idx += NT) {
+            const int s = idx & (G - 1);
+            if (s_st[s] != SL_FRESH) continue;
+            const int bus = idx >> lg;
+            const int c = s_case[s];
+            double vm, va;
+            if (s_warm[s]) {
+                const double4_32a v = Vt[idx];
+                vm = v.x;
+                va = v.y;
+            } else {
+                const double2 v0 = Bt.v0_shared ? Bt.V0[bus] : Bt.V0[(size_t)bus * Bt.sV0 + c];
+                if (Bt.check_v0 && (!finite_d(v0.x) || !finite_d(v0.y))) {
+                    if (atomicCAS(&Bt.err[0], 0, DE_V0_NONFINITE) == 0) {
+                        Bt.err[1] = bus;
+                        Bt.err[2] = c;
+                    }
+                }
+                vm = hypot(v0.x, v0.y);
+                va = atan2(v0.y, v0.x);
+                if (Bt.check_v0 && (vm <= 0.0 || vm > 10.0) && finite_d(vm)) {
+                    if (atomicCAS(&Bt.err[0], 0, DE_V0_MAGNITUDE) == 0) {
+                        Bt.err[1] = bus;
+                        Bt.err[2] = c;
+                    }
+                }
+            }
+            double sn, cs;
+            sincos(va, &sn, &cs);
+            const double4_32a v = make_double4_32a(vm, va, cs, sn);
+            Vc[idx] = v;
+            Vt[idx] = v;
+            Et[idx] = make_double2(vm * cs, vm * sn);
+            V32[idx] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+            spin[idx] = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
+        }
+
+        // ---------------------------------------------------------------- linear solve
+        if (tid < G) {
+            const int s = tid;
+            const bool act = s_st[s] == SL_ACTIVE;
+            const bool f32 = act && Bt.mixed && s_vote[s] == 1 && s_jprec[s] == 1;
+            s_on32[s] = f32;
+            s_on64[s] = act && !f32;
+            s_reeval[s] = act && !f32 && s_jprec[s] == 1;
+            s_pmin[s] = ~0ULL;
+            s_pmax[s] = 0ULL;
+        }
+        const int any32 = __syncthreads_or(tid < G && s_on32[tid]);
+        if (any32) {
+            lu_pass<float>(P, fac32, R, y32, s_on32, lg, s_pmin, s_pmax);
+            if (tid < G && s_on32[tid]) {
+                const int s = tid;
+                atomicAdd(&Bt.stats[0], 1ULL);
+                if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min32)) {
+                    atomicAdd(&Bt.stats[2], 1ULL);
+                    s_vote[s] = -1;
+                    s_on32[s] = 0;
+                    s_on64[s] = 1;
+                    s_reeval[s] = 1;
+                }
+                s_pmin[s] = ~0ULL;
+                s_pmax[s] = 0ULL;
+            }
+        }
+        const int anyre = __syncthreads_or(tid < G && s_reeval[tid]);
+        if (anyre) {  // this step's factorization is double but the Jacobian was built in float
+            for (int idx = tid; idx < nG; idx += NT) {
+                const int s = idx & (G - 1);
+                if (!s_reeval[s]) continue;
+                const int bus = idx >> lg;
+                const int row = P.row_of_bus[bus];
+                if (row < 0) continue;
+                EvalCtx ec{&P, Vt, Et, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
+                eval_row_x<true>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0), fac64,
+                                 R, false);
+            }
+            __syncthreads();
+            if (tid < G && s_reeval[tid]) s_jprec[tid] = 0;
+        }
+        const int any64 = __syncthreads_or(tid < G && s_on64[tid]);
+        if (any64) {
+            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax);
+            if (tid < G && s_on64[tid]) {
+                const int s = tid;
+                atomicAdd(&Bt.stats[1], 1ULL);
+                if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min64)) {
+                    atomicAdd(&Bt.stats[3], 1ULL);
+                    s_st[s] = SL_FINISH;  // no pivoting fallback on the device: not converged
+                    s_conv[s] = 0;
+                }
+            }
+        }
+        if (tid < G && (s_on32[tid] || s_on64[tid])) s_yprec[tid] = s_on64[tid] ? 0 : 1;
+        __syncthreads();
+
+        // ---------------------------------------------------------------- step
+        for (int idx = tid; idx < nG; idx += NT) {
+            const int s = idx & (G - 1);
+            const int st = s_st[s];
+            if (st != SL_ACTIVE && st != SL_BACKTRACK && st != SL_NEEDJ) continue;
+            const int bus = idx >> lg;
+            const int row = P.row_of_bus[bus];
+            if (row < 0) continue;
+            double4_32a vc;
+            double a;
+            if (st == SL_ACTIVE) {  // the point evaluated last was accepted: commit it
+                vc = Vt[idx];
+                Vc[idx] = vc;
+                a = 1.0;
+            } else {
+                vc = Vc[idx];
+                a = s_alpha[s];
+            }
+            double dth, dvm;
+            if (s_yprec[s]) {
+                const float2 d = y32[((size_t)row << lg) + s];
+                dth = d.x;
+                dvm = d.y;
+            } else {
+                const double2 d = y64[((size_t)row << lg) + s];
+                dth = d.x;
+                dvm = d.y;
+            }
+            const double va = vc.y + a * dth;  // nr_klu.cpp:665-669 (form_trial)
+            const double vm = P.bus_pq[bus] ? vc.x + a * dvm : vc.x;
+            double cs, sn;
+            const double d = a * dth;
+            if (fabs(d) <= 0.25) {
+                double sd, cd;
+                sincos_small(d, &sd, &cd);
+                cs = vc.z * cd - vc.w * sd;
+                sn = vc.w * cd + vc.z * sd;
+            } else {
+                sincos(va, &sn, &cs);
+            }
+            Vt[idx] = make_double4_32a(vm, va, cs, sn);
+            Et[idx] = make_double2(vm * cs, vm * sn);
+            V32[idx] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+        }
+        if (tid < G) {
+            const int st = s_st[tid];
+            if (st == SL_FRESH || st == SL_ACTIVE || st == SL_NEEDJ) s_jprec[tid] = (Bt.mixed && s_vote[tid] == 1) ? 1 : 0;
+            s_res[tid] = 0ULL;
+        }
+        __syncthreads();
+
+        // ---------------------------------------------------------------- evaluate
+        for (int idx = tid; idx < nG; idx += NT) {
+            const int s = idx & (G - 1);
+            const int st = s_st[s];
+            if (st != SL_FRESH && st != SL_ACTIVE && st != SL_NEEDJ && st != SL_BACKTRACK) continue;
+            const int bus = idx >> lg;
+            const int row = P.row_of_bus[bus];
+            if (row < 0) continue;
+            const int c = s_case[s];
+            const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
+            const bool pinned = spin[idx] != 0;
+            const bool pq = P.bus_pq[bus] != 0;
+            EvalCtx ec{&P, Vt, Et, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
+            double worst;
+            if (!Bt.mixed) {
+                if (st == SL_BACKTRACK)
+                    worst = eval_row_x<false>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
+                else
+                    worst = eval_row_x<true>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
+            } else if (st == SL_BACKTRACK) {
+                worst = eval_row_mixed<false>(ec, bus, s, row, pinned, pq, Ssp, fac32, R);
+            } else if (s_jprec[s]) {
+                worst = eval_row_mixed<true>(ec, bus, s, row, pinned, pq, Ssp, fac32, R);
+            } else {
+                worst = eval_row_x<true>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
+            }
+            atomicMax(&s_res[s], dbits(worst));
+        }
+        __syncthreads();
+
+        // ---------------------------------------------------------------- decide
+        if (tid < G) {
+            const int s = tid;
+            const int st = s_st[s];
+            double nw = bitsd(s_res[s]);
+            if (!(nw < BIG)) nw = BIG;
+            bool top = false;
+            if (st == SL_FRESH) {
+                s_nrm[s] = nw;
+                s_vote[s] = (Bt.mixed && nw > Bt.mixed_switch) ? 1 : 0;
+                top = true;
+            } else if (st == SL_ACTIVE) {
+                const double old = s_nrm[s];
+                if (!Bt.line_search || nw <= (1.0 - ARMIJO_C) * old) {
+                    if (Bt.mixed && s_vote[s] >= 0) {
+                        if (s_vote[s] == 1 && !(nw <= 0.5 * old))
+                            s_vote[s] = -1;
+                        else
+                            s_vote[s] = nw > Bt.mixed_switch ? 1 : 0;
+                    }
+                    s_nrm[s] = nw;
+                    top = true;
+                } else {
+                    s_balpha[s] = 1.0;
+                    s_bnrm[s] = nw;
+                    s_alpha[s] = 0.5;
+                    s_trial[s] = 1;
+                    s_st[s] = SL_BACKTRACK;
+                    if (Bt.mixed) s_vote[s] = -1;
+                }
+            } else if (st == SL_BACKTRACK) {
+                const double a = s_alpha[s];
+                if (nw < s_bnrm[s]) {
+                    s_bnrm[s] = nw;
+                    s_balpha[s] = a;
+                }
+                if (nw <= (1.0 - ARMIJO_C * a) * s_nrm[s]) {
+                    s_st[s] = SL_NEEDJ;
+                } else if (s_trial[s] >= LS_MAX_TRIALS) {
+                    s_alpha[s] = s_balpha[s];
+                    s_st[s] = SL_NEEDJ;
+                } else {
+                    s_trial[s] += 1;
+                    s_alpha[s] = 0.5 * a;
+                }
+            } else if (st == SL_NEEDJ) {
+                s_nrm[s] = nw;
+                top = true;
+            }
+            if (top) {  // nr_klu.cpp:590-595 loop head
+                if (s_it[s] >= Bt.max_iter) {
+                    s_st[s] = SL_FINISH;
+                    s_conv[s] = 0;
+                } else if (s_nrm[s] < Bt.tol) {
+                    s_st[s] = SL_FINISH;
+                    s_conv[s] = 1;
+                } else if (s_nrm[s] >= BIG) {
+                    s_st[s] = SL_FINISH;
+                    s_conv[s] = 0;
+                } else {
+                    s_st[s] = SL_ACTIVE;
+                }
+            }
+        }
+        if (tid == 0) atomicAdd(&Bt.stats[4], 1ULL);
+        __syncthreads();
+
+        // ---------------------------------------------------------------- write back
+        for (int idx = tid; idx < nG; idx += NT) {
+            const int s = idx & (G - 1);
+            if (s_st[s] != SL_FINISH) continue;
+            const int bus = idx >> lg;
+            const double4_32a v = Vt[idx];
+            Bt.Vout[(size_t)bus * Bt.sV + s_case[s]] = make_double2(v.x * v.z, v.x * v.w);
+        }
+        __syncthreads();
+        if (tid < G && s_st[tid] == SL_FINISH) {
+            const int s = tid;
+            Bt.iters[s_case[s]] = s_it[s];
+            Bt.conv[s_case[s]] = (uint8_t)s_conv[s];
+            s_warm[s] = Bt.lanes && s_conv[s];
+            s_st[s] = SL_EMPTY;
+        }
+        __syncthreads();
+    }
+}
+
+// Jacobian blocks and residual at one given voltage (G = 1): debug_J and tests.
+__global__ void eval_debug_kernel(const DevPlan P, const double2* V, const double2* Sbus, const uint8_t* pin,
+                                  double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R) {
+    const int n = P.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double vm = hypot(V[i].x, V[i].y), va = atan2(V[i].y, V[i].x);
+        double sn, cs;
+        sincos(va, &sn, &cs);
+        Vt[i] = make_double4_32a(vm, va, cs, sn);
+        Et[i] = make_double2(vm * cs, vm * sn);
+        V32[i] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+    }
+    __syncthreads();  // single-CTA launch
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int row = P.row_of_bus[i];
+        if (row < 0) continue;
+        EvalCtx ec{&P, Vt, Et, V32, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
+        eval_row_x<true>(ec, i, 0, row, pin && pin[i], P.bus_pq[i] != 0, Sbus[i], blocks, R, true);
+    }
+}
+
+cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
+                          cudaStream_t stream) {
+    newton_kernel<<<grid, threads, 0, stream>>>(P, B, S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
+                              double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R,
+                              cudaStream_t stream) {
+    eval_debug_kernel<<<1, 256, 0, stream>>>(P, V, Sbus, pin, Vt, Et, V32, blocks, R);
+    return cudaGetLastError();
+}
+
+int newton_max_threads() { return NT_NEWTON; }
+
+const void* newton_kernel_ptr() { return (const void*)newton_kernel; }
+
+}  // namespace gbpf

@@ -1,0 +1,77 @@
+// plan.h -- topology-only setup of the batched polar Newton solver (host side).
+//
+// Counterpart of the reference's one-off setup: nr_klu.cpp:732-759 (build_topology,
+// build_J_pattern), p3s/cuda/polar_topology.py:100-194 (Jacobian pattern + inverse map)
+// and p3s/cuda/lean_lu_plan.py:205-321 (fill-reducing order, symbolic factorization,
+// level schedule). Re-designed for the GB300 kernel:
+//
+//  * The Jacobian is factored in 2x2 BUS BLOCKS. Every non-slack bus owns the variable
+//    pair (angle, magnitude) and the equation pair (P, Q); a PV bus's magnitude column
+//    and Q row are carried as an identity dummy. A block pivot is a whole bus, so one
+//    block multiply-subtract does 8 FMAs on 8 loaded values (the scalar form needs 16
+//    loads for the same 8 FMAs), and the elimination tree is the bus graph's -- half the
+//    height of the scalar one, i.e. half the barriers per factorization.
+//  * The fill-reducing order is a minimum-degree order of the bus graph.
+//  * Factor entries are computed in Crout form, one task per block; tasks are grouped by
+//    elimination-tree height (level) and dealt to the CTA's workers longest-first onto
+//    the least-loaded worker. The forward substitution rides along in the same levels.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace gbpf {
+
+enum TaskKind { TK_DIAG = 0, TK_U = 1, TK_L = 2, TK_FWD = 3 };
+constexpr int TASK_FILL = 1 << 4;  // block not in the Jacobian: accumulate from zero
+
+struct Plan {
+    int n = 0;    // buses
+    int nnzY = 0;
+    int nv = 0;   // variable (non-slack) buses = block rows
+    std::vector<int> vbus;          // v -> bus (pv then pq)
+    std::vector<int> vidx;          // bus -> v, -1 for slack
+    std::vector<uint8_t> bus_pq;    // bus is PQ
+    std::vector<int> perm, pinv;    // pivot order over v
+    std::vector<int> row_of_bus;    // bus -> block row (pivot index) or -1
+    std::vector<int> bus_of_row;    // block row -> bus
+    std::vector<uint8_t> row_pq;    // block row is a PQ bus
+    // symbolic (block level, pivot numbering)
+    std::vector<int> Lp, Li;        // strict lower structure of each pivot column, ascending
+    std::vector<int> parent, height, depth;
+    std::vector<int> base;          // first block of each pivot (its diagonal), size nv+1
+    int nblk = 0;
+    std::vector<int> posmap;        // Ybus nnz -> block position, -1 if a slack is involved
+    std::vector<int> ydiag;         // bus -> CSR index of its diagonal, -1 if none
+    // schedule for W workers
+    int W = 0;
+    int nlev = 0, nblev = 0;
+    std::vector<int> taskA;         // 4 ints per task: dst, kind|flags, p0, p1
+    std::vector<int> ptrA;          // nlev*W + 1
+    std::vector<int> scl;           // 2 ints: L block, diagonal block
+    std::vector<int> ptrB;          // nlev*W + 1
+    std::vector<int> taskC;         // backward: 4 ints: row, diag block, p0, p1
+    std::vector<int> ptrC;          // nblev*W + 1
+    std::vector<int> pairs;         // 2 ints per pair
+    // statistics
+    long long n_factor_pairs = 0, n_fwd_pairs = 0, n_bwd_pairs = 0;
+    double rcond0 = 0.0;            // pivot ratio of the flat-start factorization
+    std::vector<int> level_work;    // per level: max worker load (critical path estimate)
+};
+
+// Build everything topology-only. Returns an empty string on success, else the error.
+std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, const int* pv, int npv,
+                       const int* pq, int npq, int workers);
+
+// Host replica of the device algorithm (double precision): Jacobian blocks at (Vm, Va)
+// written to `blocks` (nblk*4, zero where not in the Jacobian) and residual R (nv*2).
+void host_eval(const Plan& p, const int* Yp, const int* Yj, const double* Yx, const double* Vm, const double* Va,
+               const double* S, const uint8_t* pin, double* blocks, double* R);
+// Serial block LU with the plan (in place); returns min/max real pivot in pmin/pmax and
+// false on a zero / non-finite pivot.
+bool host_factor(const Plan& p, double* blocks, double* pmin, double* pmax);
+// Solve with factored blocks: b (nv*2, block-row order) -> x in place.
+void host_solve(const Plan& p, const double* blocks, double* b);
+
+}  // namespace gbpf

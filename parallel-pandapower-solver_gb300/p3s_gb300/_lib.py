@@ -1,0 +1,154 @@
+"""ctypes binding of the C ABI in include/gbpf.h (libgbpf.so, built in-tree).
+
+The library is the product path: there is no CPU fallback. Loading fails loudly when the
+library is missing or no CUDA device is visible.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_bp = C.POINTER(C.c_uint8)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("max_iter", C.c_int),
+        ("tol", C.c_double),
+        ("line_search", C.c_int),
+        ("precision", C.c_int),
+        ("mixed_switch", C.c_double),
+        ("check_v0", C.c_int),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("n_bus", C.c_int),
+        ("nnz_ybus", C.c_int),
+        ("n_var_bus", C.c_int),
+        ("n_blocks", C.c_int),
+        ("n_levels", C.c_int),
+        ("n_back_levels", C.c_int),
+        ("cases_per_cta", C.c_int),
+        ("threads_per_cta", C.c_int),
+        ("workers", C.c_int),
+        ("factor_pairs", C.c_longlong),
+        ("forward_pairs", C.c_longlong),
+        ("backward_pairs", C.c_longlong),
+        ("rcond0", C.c_double),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("single_factorizations", C.c_ulonglong),
+        ("double_factorizations", C.c_ulonglong),
+        ("single_rejected", C.c_ulonglong),
+        ("double_rejected", C.c_ulonglong),
+        ("macro_steps", C.c_ulonglong),
+        ("grid", C.c_int),
+        ("cases_per_cta", C.c_int),
+        ("kernel_ms", C.c_double),
+    ]
+
+
+# exported symbols and their signatures (restype, argtypes)
+SIGNATURES = {
+    "gbpf_last_error": (C.c_char_p, []),
+    "gbpf_version": (C.c_int, []),
+    "gbpf_device_count": (C.c_int, []),
+    "gbpf_create": (_vp, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int]),
+    "gbpf_destroy": (None, [_vp]),
+    "gbpf_update_Y": (C.c_int, [_vp, _dp, C.c_int]),
+    "gbpf_get_info": (C.c_int, [_vp, C.POINTER(Info)]),
+    "gbpf_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
+    "gbpf_get_posmap": (C.c_int, [_vp, _ip]),
+    "gbpf_get_row_of_bus": (C.c_int, [_vp, _ip]),
+    "gbpf_solve_batch": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.POINTER(Params), _dp, _ip, _bp]),
+    "gbpf_solve_batch_device": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.POINTER(Params), _vp, _vp,
+                                          _vp]),
+    "gbpf_solve_lanes": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, _lp, C.POINTER(Params), _dp, _ip, _bp]),
+    "gbpf_solve_lanes_device": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int, _vp, C.POINTER(Params), _vp, _vp, _vp]),
+    "gbpf_solve_contingency": (C.c_int, [_vp, C.c_int, _dp, _dp, _bp, _dp, _ip, _ip, _dp, C.POINTER(Params), _dp,
+                                         _ip, _bp]),
+    "gbpf_eval_jacobian": (C.c_int, [_vp, _dp, _dp, _bp, _dp, _dp]),
+    "gbpf_host_alloc": (_vp, [C.c_size_t]),
+    "gbpf_host_free": (None, [_vp]),
+    "gbpf_plan_selftest": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int, _dp, _dp,
+                                     _dp, _dp, _ip, C.c_char_p, C.c_int]),
+    "gbpf_islands": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
+                               _ip, _ip]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """The loaded library (built first if missing and a CUDA toolkit is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or (build_if_missing and not _build.up_to_date()):
+        if not build_if_missing:
+            raise RuntimeError(f"libgbpf.so not built ({path}); run p3s_gb300.build.build()")
+        _build.build()
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def require_device():
+    L = load()
+    if L.gbpf_device_count() <= 0:
+        raise RuntimeError("p3s_gb300: no CUDA device visible; the GPU solver has no CPU fallback")
+    return L
+
+
+def last_error() -> str:
+    return load().gbpf_last_error().decode(errors="replace")
+
+
+def check(rc: int, what: str = ""):
+    if rc != 0:
+        msg = last_error()
+        raise RuntimeError(msg if msg else f"{what} failed ({rc})")
+
+
+def d(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def i32(a: np.ndarray):
+    return a.ctypes.data_as(_ip)
+
+
+def i64(a: np.ndarray):
+    return a.ctypes.data_as(_lp)
+
+
+def u8(a: np.ndarray):
+    return a.ctypes.data_as(_bp)
+
+
+def cview(a: np.ndarray):
+    """complex128 array as its interleaved float64 pointer"""
+    return a.view(np.float64).ctypes.data_as(_dp)

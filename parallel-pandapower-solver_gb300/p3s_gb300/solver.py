@@ -1,0 +1,175 @@
+"""Python owner of one device solver (C ABI of include/gbpf.h).
+
+`GpuSolver` is the shared core behind both reference-facing surfaces
+(``p3s_gb300.nr_klu`` and ``p3s_gb300.cuda.nr_polar_solver``): numpy arrays in, numpy
+arrays out, every solve one launch of the persistent sm_103a Newton kernel.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .topology import jacobian_pattern, scalar_residual_order
+
+
+def c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class GpuSolver:
+    """One grid topology resident on the device."""
+
+    def __init__(self, Yp, Yj, Yx, pv, pq, cases_per_cta: int = 0):
+        L = _lib.require_device()
+        self.Yp = np.ascontiguousarray(Yp, dtype=np.int32)
+        self.Yj = np.ascontiguousarray(Yj, dtype=np.int32)
+        self.Yx = c128(Yx)
+        self.pv = np.ascontiguousarray(np.asarray(pv).ravel(), dtype=np.int32)
+        self.pq = np.ascontiguousarray(np.asarray(pq).ravel(), dtype=np.int32)
+        self.n = len(self.Yp) - 1
+        self.nnz = len(self.Yj)
+        if self.Yx.shape != (self.nnz,):
+            raise ValueError("Yx must have one value per Ybus nonzero")
+        h = L.gbpf_create(self.n, _lib.i32(self.Yp), _lib.i32(self.Yj), _lib.cview(self.Yx), self.nnz,
+                          _lib.i32(self.pv), len(self.pv), _lib.i32(self.pq), len(self.pq), int(cases_per_cta))
+        if not h:
+            raise RuntimeError(_lib.last_error())
+        self._h = h
+        self._pattern = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().gbpf_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -------------------------------------------------------------- facts
+    @property
+    def info(self) -> dict:
+        o = _lib.Info()
+        _lib.check(_lib.load().gbpf_get_info(self._h, C.byref(o)), "gbpf_get_info")
+        return {f: getattr(o, f) for f, _ in o._fields_}
+
+    @property
+    def stats(self) -> dict:
+        o = _lib.Stats()
+        _lib.check(_lib.load().gbpf_get_stats(self._h, C.byref(o)), "gbpf_get_stats")
+        return {f: getattr(o, f) for f, _ in o._fields_}
+
+    def posmap(self) -> np.ndarray:
+        out = np.empty(self.nnz, dtype=np.int32)
+        _lib.check(_lib.load().gbpf_get_posmap(self._h, _lib.i32(out)))
+        return out
+
+    def row_of_bus(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.int32)
+        _lib.check(_lib.load().gbpf_get_row_of_bus(self._h, _lib.i32(out)))
+        return out
+
+    @staticmethod
+    def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False):
+        if precision not in ("double", "mixed"):
+            raise ValueError(f"precision must be 'double' or 'mixed', got {precision!r}")
+        return _lib.Params(int(max_iter), float(tol), int(bool(line_search)), 1 if precision == "mixed" else 0,
+                           float(mixed_switch), int(bool(check_v0)))
+
+    # -------------------------------------------------------------- values
+    def update_Y(self, Yx):
+        Yx = c128(Yx)
+        if Yx.shape != (self.nnz,):
+            raise ValueError("update_Y: nnz mismatch (topology changed; rebuild the solver)")
+        _lib.check(_lib.load().gbpf_update_Y(self._h, _lib.cview(Yx), self.nnz), "update_Y")
+        self.Yx = Yx
+
+    # -------------------------------------------------------------- solves
+    def solve_batch(self, S, V0, p: _lib.Params):
+        """S (n, T) or (n,) with T given by V0; V0 (n,) or (n, T)."""
+        S = c128(S)
+        V0 = c128(V0)
+        T = S.shape[1] if S.ndim == 2 else V0.shape[1]
+        V = np.empty((self.n, T), dtype=np.complex128)
+        it = np.empty(T, dtype=np.int32)
+        cv = np.empty(T, dtype=np.uint8)
+        rc = _lib.load().gbpf_solve_batch(self._h, T, _lib.cview(S), int(S.ndim == 2), _lib.cview(V0),
+                                          int(V0.ndim == 2), C.byref(p), _lib.cview(V), _lib.i32(it), _lib.u8(cv))
+        _lib.check(rc, "solve_batch")
+        return {"V": V, "iterations": it, "converged": cv.astype(bool)}
+
+    def solve_lanes(self, S, V0, offsets, p: _lib.Params):
+        S = c128(S)
+        V0 = c128(V0).ravel()
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        T = S.shape[1]
+        K = len(off) - 1
+        V = np.empty((self.n, T), dtype=np.complex128)
+        it = np.empty(T, dtype=np.int32)
+        cv = np.empty(T, dtype=np.uint8)
+        rc = _lib.load().gbpf_solve_lanes(self._h, T, _lib.cview(S), _lib.cview(V0), K, _lib.i64(off), C.byref(p),
+                                          _lib.cview(V), _lib.i32(it), _lib.u8(cv))
+        _lib.check(rc, "solve_lanes")
+        return {"V": V, "iterations": it, "converged": cv.astype(bool)}
+
+    def solve_contingency(self, S, V0, pin, p: _lib.Params, Yd=None, stamps=None):
+        """S (n,), V0 (n, L), pin (n, L) or None; per-case Ybus: Yd (nnz, L) complex or
+        stamps = (ptr (L+1,), k (E,), val (E,) complex) subtracted from the base values."""
+        S = c128(np.asarray(S).ravel())
+        V0 = c128(V0)
+        L = V0.shape[1]
+        pin_a = None if pin is None else np.ascontiguousarray(pin, dtype=np.uint8)
+        V = np.empty((self.n, L), dtype=np.complex128)
+        it = np.empty(L, dtype=np.int32)
+        cv = np.empty(L, dtype=np.uint8)
+        Ydp = None
+        sp_ = sk = sv = None
+        if Yd is not None:
+            Yd = c128(Yd)
+            Ydp = _lib.cview(Yd)
+        elif stamps is not None:
+            ptr, k, val = stamps
+            ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+            k = np.ascontiguousarray(k, dtype=np.int32)
+            val = c128(val)
+            sp_, sk, sv = _lib.i32(ptr), _lib.i32(k), _lib.cview(val)
+        rc = _lib.load().gbpf_solve_contingency(self._h, L, _lib.cview(S), _lib.cview(V0),
+                                                None if pin_a is None else _lib.u8(pin_a), Ydp, sp_, sk, sv,
+                                                C.byref(p), _lib.cview(V), _lib.i32(it), _lib.u8(cv))
+        _lib.check(rc, "solve_batch_contingency")
+        return {"V": V, "iterations": it, "converged": cv.astype(bool)}
+
+    # -------------------------------------------------------------- Jacobian
+    def eval_blocks(self, S, V, pin=None):
+        """Device Jacobian blocks (n_blocks, 4) and residual (n_var_bus, 2) at one voltage."""
+        S = c128(np.asarray(S).ravel())
+        V = c128(np.asarray(V).ravel())
+        info = self.info
+        blk = np.empty((info["n_blocks"], 4), dtype=np.float64)
+        R = np.empty((max(info["n_var_bus"], 1), 2), dtype=np.float64)
+        pin_a = None if pin is None else np.ascontiguousarray(pin, dtype=np.uint8)
+        rc = _lib.load().gbpf_eval_jacobian(self._h, _lib.cview(S), _lib.cview(V),
+                                            None if pin_a is None else _lib.u8(pin_a), _lib.d(blk), _lib.d(R))
+        _lib.check(rc, "eval_jacobian")
+        return blk, R[: info["n_var_bus"]]
+
+    def debug_J(self, S, V):
+        """The reference's debug_J result (CSC Jp, Ji, Jx, m) from the device Jacobian, plus
+        the mismatch F = S(V) - S in the reference's row order."""
+        if self._pattern is None:
+            self._pattern = jacobian_pattern(self.Yp, self.Yj, self.pv, self.pq)
+        Jp, Ji, sk, sb, m = self._pattern
+        blk, R = self.eval_blocks(S, V)
+        pm = self.posmap()
+        Jx = blk[pm[sk], sb]
+        rob = self.row_of_bus()
+        row_p, row_q = scalar_residual_order(self.pv, self.pq, self.n)
+        F = np.zeros(m)
+        bus = np.nonzero(row_p >= 0)[0]
+        F[row_p[bus]] = -R[rob[bus], 0]
+        bq = np.nonzero(row_q >= 0)[0]
+        F[row_q[bq]] = -R[rob[bq], 1]
+        return {"Jp": Jp, "Ji": Ji, "Jx": Jx, "m": m, "F": F}
