@@ -1,0 +1,455 @@
+"""Benchmark: batched AC power flow solves/s on one GB300 (the 2,000-bus x 8,760-hour series).
+
+One step = one pass of the Newton path over the whole workload: the 2,000-bus grid's
+8,760 hourly cases, chained hour to hour in warm-start lanes, solved to <= 1e-8 p.u.
+mismatch by ONE launch of the persistent sm_103a kernel.
+
+  value : solves/s with inputs resident in HBM (CUDA events around the kernel, solver stream)
+  e2e   : solves/s through the public API (p3s_gb300.solver.GpuSolver.solve_lanes) from
+          pinned host memory, host->device inputs and device->host results inside the timed
+          region (CUDA events from the first copy in to the last copy out)
+  fp64  : the same for the plain double-precision path (the headline value is the mixed path)
+
+N > 1 (torchrun): every rank solves its own 8,760-hour series (weak scaling, no collective on
+the data path); value = all ranks' solves / the slowest rank's time.
+`--impl reference` times the CPU oracle (the restatement of the reference's nr_klu solver,
+all host cores) on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "parallel-pandapower-solver_gb300"), ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "solves/s on 1 GB300, mixed vs FP64 at ≤1e-8 pu mismatch; p50/p99 latency"
+N_BUS, HOURS = 2000, 8760
+
+
+def shard(B: int, rank: int, world: int):
+    """Contiguous [lo, hi) share of B cases for `rank` of `world` (every case exactly once)."""
+    base, extra = divmod(B, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
+# ----------------------------------------------------------------------------- distributed
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- workload
+def workload(rank: int = 0, hours: int = HOURS):
+    from p3s_gb300.synthetic import grid_2000, lanes, timeseries_injections
+
+    g = grid_2000(0)
+    S = timeseries_injections(g, hours, seed=1 + rank)
+    return g, S
+
+
+def n_lanes(g, cases_per_cta=8):
+    import torch
+
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
+    return nsm * cases_per_cta
+
+
+def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
+    """Bytes a case-iteration must move (the hot path's per-unit traffic model): eval (V state,
+    S, Jacobian write, residual), refactor (read A, write LU), solve (read LU and residual,
+    write step), step (read step, rewrite the state). Index arrays are shared by the batch
+    and excluded. b = 8 (double path) or 4 (float Jacobian/LU in the mixed path)."""
+    n = g.n
+    m = len(g.pv) + 2 * len(g.pq)  # scalar unknowns
+    from p3s_gb300.topology import jacobian_pattern
+
+    nnzJ = len(jacobian_pattern(g.Yp, g.Yj, g.pv, g.pq)[1])
+    nnzLU = 4 * info["n_blocks"]
+    b = 4 if mixed else 8
+    return (3 * n * 8 + 2 * n * 8 + b * nnzJ + 8 * m) + (b * nnzJ + b * nnzLU) + (b * nnzLU + 16 * m) + (
+        8 * m + 6 * n * 8)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv",
+                                          "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()[1:]]
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1].split()[0]))
+                mx.append(float(r[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def load_traffic():
+    """DRAM bytes per case-iteration of the Newton kernel from the committed ncu summary."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "newton_kernel_traffic.json")))
+    except Exception:
+        return {}
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, local):
+    import torch
+
+    from p3s_gb300 import _lib
+    from p3s_gb300.solver import GpuSolver, pinned_empty
+    from p3s_gb300.synthetic import lanes
+
+    torch.cuda.set_device(local)
+    _lib.require_device()
+    g, S = workload(rank, args.hours)
+    T = S.shape[1]
+    solver = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    info = solver.info
+    K = args.lanes or n_lanes(g, info["cases_per_cta"])
+    off = lanes(T, K).astype(np.int64)
+    dev = torch.device("cuda", local)
+    dS = torch.from_numpy(S.view(np.float64).copy()).to(dev)
+    dV0 = torch.from_numpy(g.V0.view(np.float64).copy()).to(dev)
+    doff = torch.from_numpy(off).to(dev)
+    dV = torch.empty(2 * g.n * T, dtype=torch.float64, device=dev)
+    dit = torch.empty(T, dtype=torch.int32, device=dev)
+    dcv = torch.empty(T, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def dev_step(p):
+        solver.solve_lanes_device(dS.data_ptr(), dV0.data_ptr(), doff.data_ptr(), T, len(off) - 1, p, dV.data_ptr(),
+                                  dit.data_ptr(), dcv.data_ptr())
+        return solver.stats
+
+    out = {}
+    for prec in ("mixed", "double"):
+        p = GpuSolver.params(precision=prec, mixed_switch=args.mixed_switch)
+        for _ in range(args.warmup):
+            dev_step(p)
+        barrier(world)
+        torch.cuda.synchronize()
+        ms, its, stats = [], [], None
+        clocks = Clocks(local)
+        with clocks:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                stats = dev_step(p)
+                ms.append(stats["kernel_ms"])
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        barrier(world)
+        it = dit.cpu().numpy()
+        cv = dcv.cpu().numpy().astype(bool)
+        out[prec] = dict(ms=float(np.mean(ms)), wall_ms=wall * 1e3 / args.steps, it=it, cv=cv, stats=stats,
+                         clocks=clocks.summary())
+
+    # accuracy of the mixed result against the oracle's mismatch on a few hours
+    p = GpuSolver.params(precision="mixed", mixed_switch=args.mixed_switch)
+    dev_step(p)
+    V = dV.cpu().numpy().view(np.complex128).reshape(g.n, T)
+    from oracle import cpu
+
+    osv = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    hrs = np.linspace(0, T - 1, 8).astype(int)
+    worst_mis = max(float(np.abs(osv.debug_J_at(S[:, h], V[:, h])["F"]).max()) for h in hrs)
+
+    # end to end through the public API, pinned host buffers
+    Sh = pinned_empty(S.shape, np.complex128)
+    Sh[...] = S
+    V0h = pinned_empty(g.V0.shape, np.complex128)
+    V0h[...] = g.V0
+    Vh = pinned_empty((g.n, T), np.complex128)
+    ith = pinned_empty((T,), np.int32)
+    cvh = pinned_empty((T,), np.uint8)
+    p = GpuSolver.params(precision="mixed", mixed_switch=args.mixed_switch)
+    for _ in range(args.warmup):
+        solver.solve_lanes(Sh, V0h, off, p, out=(Vh, ith, cvh))
+    barrier(world)
+    e2e_ms = []
+    for _ in range(args.steps):
+        solver.solve_lanes(Sh, V0h, off, p, out=(Vh, ith, cvh))
+        e2e_ms.append(solver.stats["call_ms"])
+    barrier(world)
+    h2d = S.nbytes + g.V0.nbytes + off.nbytes
+    d2h = Vh.nbytes + ith.nbytes + cvh.nbytes
+
+    res = dict(out=out, e2e_ms=float(np.mean(e2e_ms)), h2d=h2d, d2h=d2h, info=info, K=len(off) - 1, T=T,
+               worst_mis=worst_mis, g=g)
+    return res
+
+
+def gpu_line(args, res, rank, world):
+    out = res["out"]
+    T = res["T"]
+    mixed, dbl = out["mixed"], out["double"]
+    ms_mixed = reduce_max(mixed["ms"], world)
+    ms_dbl = reduce_max(dbl["ms"], world)
+    e2e_ms = reduce_max(res["e2e_ms"], world)
+    if rank != 0:
+        return None
+    g = res["g"]
+    info = res["info"]
+    value = world * T / (ms_mixed * 1e-3)
+    peaks = load_peaks()
+    hbm = peaks.get("hbm_gbs")
+    its_mixed = int(mixed["it"].sum())
+    B = algorithmic_bytes_per_iteration(info, g, True)
+    achieved = B * its_mixed / (mixed["ms"] * 1e-3) / 1e9
+    traffic = load_traffic()
+    tr = traffic.get("mixed_bytes_per_case_iteration")
+    roof = {
+        "bound": "hbm",
+        "achieved": round(achieved, 1),
+        "peak": hbm if hbm else 6800.0,
+        "unit": "GB/s",
+        "frac": round(achieved / (hbm if hbm else 6800.0), 4),
+        "traffic": None if tr is None else float(tr) * its_mixed,
+        "peak_source": "measured" if hbm else "fallback",
+        "kernel": "newton_kernel",
+        "algorithmic_bytes_per_case_iteration": B,
+        "case_iterations_per_launch": its_mixed,
+    }
+    # fp64 pipe roofline of the double path (GB300: ~1.2 TFLOP/s)
+    fp64 = {
+        "value": round(world * T / (ms_dbl * 1e-3), 1),
+        "ms_per_step": round(ms_dbl, 3),
+        "iterations_mean": float(dbl["it"].mean()),
+        "converged": bool(dbl["cv"].all()),
+        "achieved_GBps": round(algorithmic_bytes_per_iteration(info, g, False) * int(dbl["it"].sum())
+                               / (dbl["ms"] * 1e-3) / 1e9, 1),
+        "clocks": dbl["clocks"],
+    }
+    cb = cpu_baseline(res["g"], args)
+    line = {
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_mixed, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 Jacobian/LU + f64 mismatch/update",
+        "data": "synthetic (seeded 2,000-bus grid and 8,760-hour load/generation series)",
+        "config": {
+            "workload": f"2,000-bus grid x {T} hourly cases, warm-start lanes K={res['K']} "
+                        f"(hour h of a lane starts from hour h-1's converged voltage)",
+            "n_bus": g.n, "n_branch": g.n_branch, "n_pv": len(g.pv), "n_pq": len(g.pq), "hours": T,
+            "lanes": res["K"], "tol_pu": 1e-8, "max_iter": 30, "precision": "mixed",
+            "mixed_switch": args.mixed_switch,
+            "cases_per_cta": info["cases_per_cta"], "grid_ctas": mixed["stats"]["grid"],
+            "l2": "inputs larger than L2 (S is 280 MB per step; L2 is 129 MB)",
+            "iterations_mean": float(mixed["it"].mean()), "converged": bool(mixed["cv"].all()),
+            "max_mismatch_pu_sampled": res["worst_mis"],
+            "single_factorizations": int(mixed["stats"]["single_factorizations"]),
+            "double_factorizations": int(mixed["stats"]["double_factorizations"]),
+        },
+        "fp64": fp64,
+        "roofline": roof,
+        "cpu_baseline": cb,
+        "e2e": {"value": round(world * T / (e2e_ms * 1e-3), 1), "unit": "solves/s",
+                "h2d_bytes_per_step": int(res["h2d"]), "d2h_bytes_per_step": int(res["d2h"]),
+                "ms_per_step": round(e2e_ms, 3)},
+        "clocks": mixed["clocks"],
+        "gpu_launches": args.steps,
+        "wall_ms_per_step": round(mixed["wall_ms"], 3),
+    }
+    return line
+
+
+# ----------------------------------------------------------------------------- CPU arms
+def cpu_solve(g, S, K):
+    from oracle import cpu
+    from p3s_gb300.synthetic import lanes
+
+    s = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    off = lanes(S.shape[1], K)
+    t0 = time.perf_counter()
+    r = cpu.solve_lanes(s, S, g.V0, off)
+    return time.perf_counter() - t0, r
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(g, args):
+    """The oracle (restated nr_klu, OpenMP over all usable cores) on a bounded sample of the
+    same workload: the first `cpu_hours` hours in the same lane structure, best of 3."""
+    from oracle.build import build_oracle
+
+    build_oracle()
+    hours = min(args.cpu_hours, HOURS)
+    _, S = workload(0, hours)
+    K = max(1, round(hours * (args.lanes or 1216) / HOURS))
+    best = min(cpu_solve(g, S, K)[0] for _ in range(3))
+    return {"value": round(hours / best, 1), "unit": "solves/s", "cores": cpu_cores(), "kind": "port",
+            "sample": f"first {hours} of the {HOURS} hours, {K} warm-start lanes, best of 3, oracle/liboracle.so "
+                      f"(OpenMP, {cpu_cores()} threads)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle.build import build_oracle
+    from p3s_gb300.synthetic import grid_2000
+
+    build_oracle()
+    g = grid_2000(0)
+    hours = min(args.cpu_hours, HOURS)
+    _, S = workload(0, hours)
+    K = max(1, round(hours * (args.lanes or 1216) / HOURS))
+    for _ in range(args.warmup):
+        cpu_solve(g, S, K)
+    times = [cpu_solve(g, S, K)[0] for _ in range(args.steps)]
+    ms = float(np.mean(times)) * 1e3
+    value = hours / (ms * 1e-3)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded 2,000-bus grid and hourly load/generation series)",
+        "config": {"workload": f"2,000-bus grid x {hours} hourly cases (sample of the {HOURS}-hour series), "
+                               f"warm-start lanes K={K}", "n_bus": g.n, "hours": hours, "lanes": K,
+                   "tol_pu": 1e-8, "max_iter": 30},
+        "cpu_baseline": {"value": round(value, 1), "unit": "solves/s", "cores": cpu_cores(), "kind": "port",
+                         "sample": f"{hours} hours per step on all host cores (oracle/liboracle.so, a restatement "
+                                   f"of the reference's nr_klu; the reference's own build needs its checkout)"},
+        "e2e": {"value": round(value, 1), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--hours", type=int, default=HOURS)
+    ap.add_argument("--lanes", type=int, default=0, help="warm-start lanes (0: SMs x cases per CTA)")
+    ap.add_argument("--mixed-switch", type=float, default=1e-3)
+    ap.add_argument("--cpu-hours", type=int, default=HOURS)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":  # rank 0 alone times the CPU reference; other ranks exit at once
+        rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+        run_reference(args, rank, world)
+        return
+    rank, world, local = dist_init()
+    res = run_gpu(args, rank, world, local)
+    line = gpu_line(args, res, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -31,6 +31,8 @@ typedef struct gbpf_params {
     int precision;       /* 0: double factors; 1: mixed (float factors while the vote asks) */
     double mixed_switch; /* mismatch above which a case factors in float (mixed only) */
     int check_v0;        /* 1: reject non-finite / out-of-range start voltages like solve_batch */
+    double pivot_ratio_double; /* accept a double factorization while min|piv|/max|piv| >= this x rcond0 (1e-3) */
+    double pivot_ratio_single; /* the same bound for a float factorization (1e-3) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -47,6 +49,7 @@ typedef struct gbpf_stats {
     unsigned long long single_rejected, double_rejected, macro_steps;
     int grid, cases_per_cta;
     double kernel_ms; /* device time of the Newton kernel, CUDA events on the solver's stream */
+    double call_ms;   /* device time of the last host-pointer call: first copy in to last copy out */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);

@@ -83,7 +83,7 @@ struct gbpf_solver {
     std::vector<double> Yx;  // interleaved complex
     int device = 0, nsm = 0, occ = 1;
     cudaStream_t stream = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
     int G = 8, lg = 3, NT = 512;
     // topology on the device
     DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dpairs,
@@ -102,8 +102,8 @@ struct gbpf_solver {
                         &Vc, &Vt, &Et, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
                         &bYd, &bpin})
             b->release();
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
+        for (cudaEvent_t e : {e0, e1, c0, c1})
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -133,10 +133,13 @@ int compute_rcond0(gbpf_solver* s) {
         p.rcond0 = 1.0;
         return 0;
     }
-    if (!gbpf::host_factor(p, blk.data(), &mn, &mx) || !(mx > 0.0) || !(mn > 0.0) || !std::isfinite(mx))
-        return fail(
-            "lean LU: the Jacobian has a zero or non-finite diagonal pivot at flat start, so the static pivot order "
-            "cannot be used for this grid");
+    if (!gbpf::host_factor(p, blk.data(), &mn, &mx) || !(mx > 0.0) || !(mn > 0.0) || !std::isfinite(mx)) {
+        // no usable reference pivot ratio: every factorization on the device then fails its
+        // pivot check and the cases end not converged (nr_klu.cpp's behaviour when its plan
+        // cannot be built); gbpf_info reports rcond0 = NaN so callers can refuse the grid
+        p.rcond0 = std::nan("");
+        return 0;
+    }
     p.rcond0 = mn / mx;
     return 0;
 }
@@ -147,6 +150,8 @@ int setup(gbpf_solver* s, int cases_per_cta) {
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&s->e0));
     CK(cudaEventCreate(&s->e1));
+    CK(cudaEventCreate(&s->c0));
+    CK(cudaEventCreate(&s->c1));
     s->NT = gbpf::newton_max_threads();
     int G = cases_per_cta;
     if (G <= 0) {
@@ -270,6 +275,8 @@ gbpf_params default_params() {
     p.precision = 0;
     p.mixed_switch = 1e-3;
     p.check_v0 = 0;
+    p.pivot_ratio_double = 1e-3;
+    p.pivot_ratio_single = 1e-3;
     return p;
 }
 
@@ -322,6 +329,13 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     return 0;
 }
 
+int record_call(gbpf_solver* s) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, s->c0, s->c1));
+    s->last.call_ms = ms;
+    return 0;
+}
+
 void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.max_iter = p.max_iter;
     b.tol = p.tol;
@@ -329,8 +343,8 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.mixed = p.precision == 1;
     b.mixed_switch = p.mixed_switch;
     b.check_v0 = p.check_v0;
-    b.rcond_min64 = 1e-3 * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO
-    b.rcond_min32 = 1e-3 * s->plan.rcond0;
+    b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
+    b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
 }
 
 }  // namespace
@@ -465,6 +479,7 @@ int gbpf_solve_batch(gbpf_solver* s, int T, const double* S, int s_per_col, cons
     CK(s->bV.ensure(ob));
     CK(s->bit.ensure((size_t)T * 4));
     CK(s->bcv.ensure((size_t)T));
+    CK(cudaEventRecord(s->c0, s->stream));
     CK(cudaMemcpyAsync(s->bS.p, S, sb, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->bV0.p, V0, vb, cudaMemcpyHostToDevice, s->stream));
     if (int rc = gbpf_solve_batch_device(s, T, s->bS.as<double>(), s_per_col, s->bV0.as<double>(), v0_per_col, pp,
@@ -473,8 +488,9 @@ int gbpf_solve_batch(gbpf_solver* s, int T, const double* S, int s_per_col, cons
     CK(cudaMemcpyAsync(V, s->bV.p, ob, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(it, s->bit.p, (size_t)T * 4, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(cv, s->bcv.p, (size_t)T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaEventRecord(s->c1, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    return record_call(s);
 }
 
 int gbpf_solve_lanes_device(gbpf_solver* s, int T, const double* dS, const double* dV0, int K, const int64_t* doff,
@@ -519,6 +535,7 @@ int gbpf_solve_lanes(gbpf_solver* s, int T, const double* S, const double* V0, i
     CK(s->bit.ensure((size_t)T * 4));
     CK(s->bcv.ensure((size_t)T));
     CK(s->blane.ensure((size_t)(K + 1) * 8));
+    CK(cudaEventRecord(s->c0, s->stream));
     CK(cudaMemcpyAsync(s->bS.p, S, sb, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->bV0.p, V0, vb, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->blane.p, off, (size_t)(K + 1) * 8, cudaMemcpyHostToDevice, s->stream));
@@ -528,8 +545,9 @@ int gbpf_solve_lanes(gbpf_solver* s, int T, const double* S, const double* V0, i
     CK(cudaMemcpyAsync(V, s->bV.p, sb, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(it, s->bit.p, (size_t)T * 4, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(cv, s->bcv.p, (size_t)T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaEventRecord(s->c1, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    return record_call(s);
 }
 
 int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double* V0, const uint8_t* pin,

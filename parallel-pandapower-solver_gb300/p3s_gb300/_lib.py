@@ -30,6 +30,8 @@ class Params(C.Structure):
         ("precision", C.c_int),
         ("mixed_switch", C.c_double),
         ("check_v0", C.c_int),
+        ("pivot_ratio_double", C.c_double),
+        ("pivot_ratio_single", C.c_double),
     ]
 
 
@@ -61,6 +63,7 @@ class Stats(C.Structure):
         ("grid", C.c_int),
         ("cases_per_cta", C.c_int),
         ("kernel_ms", C.c_double),
+        ("call_ms", C.c_double),
     ]
 
 

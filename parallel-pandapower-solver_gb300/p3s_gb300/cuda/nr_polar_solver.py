@@ -39,13 +39,22 @@ class PolarNewtonSolverCUDA:
         self.fallback = "none"
         self.cpu_handoff = 0
         self.pinned_transfers = True
+        # pivot-ratio acceptance bounds relative to the flat-start factorization
+        # (nr_polar_solver.py:63-65 _RCOND_RATIO and _rcond_ratio_single)
+        self._rcond_ratio = 1e-3
+        self._rcond_ratio_single = 1e-3
         self.last_stats: dict = {}
         self._s = GpuSolver(Yp, Yj, Yx, pv, pq, cases_per_cta)
         self.n = self._s.n
+        if not np.isfinite(self._s.info["rcond0"]):
+            raise RuntimeError(
+                "lean LU: the Jacobian has a zero or non-finite diagonal pivot at flat start, so the static pivot "
+                "order cannot be used for this grid")
 
     # ------------------------------------------------------------------ helpers
     def _params(self, max_iter, tol):
-        return GpuSolver.params(max_iter, tol, self.line_search, self.precision, self.mixed_switch)
+        return GpuSolver.params(max_iter, tol, self.line_search, self.precision, self.mixed_switch,
+                                pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single)
 
     def _record(self, B, r):
         st = self._s.stats
@@ -142,6 +151,8 @@ class PolarNewtonSolverCUDA:
         if np.array_equal(Yx, self._s.Yx):
             return
         self._s.update_Y(Yx)
+        if not np.isfinite(self._s.info["rcond0"]):
+            raise RuntimeError("lean LU: the Jacobian has a zero or non-finite diagonal pivot at flat start")
 
     def free(self):
         """Device memory is released with the solver object."""

@@ -19,6 +19,38 @@ def c128(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.complex128)
 
 
+class PinnedArray(np.ndarray):
+    """numpy array over page-locked host memory (released with the array)."""
+
+    def __array_finalize__(self, obj):
+        if obj is not None:
+            self._owner = getattr(obj, "_owner", None)
+
+
+class _PinnedOwner:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            _lib.load().gbpf_host_free(self.ptr)
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype) -> np.ndarray:
+    """An uninitialised array in page-locked host memory (fast host <-> device copies)."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    ptr = _lib.load().gbpf_host_alloc(max(nbytes, 16))
+    if not ptr:
+        raise MemoryError(_lib.last_error())
+    buf = (C.c_char * max(nbytes, 16)).from_address(ptr)
+    a = np.frombuffer(buf, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape).view(PinnedArray)
+    a._owner = _PinnedOwner(ptr)
+    return a
+
+
 class GpuSolver:
     """One grid topology resident on the device."""
 
@@ -73,11 +105,13 @@ class GpuSolver:
         return out
 
     @staticmethod
-    def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False):
+    def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False,
+               pivot_ratio_double=1e-3, pivot_ratio_single=1e-3):
         if precision not in ("double", "mixed"):
             raise ValueError(f"precision must be 'double' or 'mixed', got {precision!r}")
         return _lib.Params(int(max_iter), float(tol), int(bool(line_search)), 1 if precision == "mixed" else 0,
-                           float(mixed_switch), int(bool(check_v0)))
+                           float(mixed_switch), int(bool(check_v0)), float(pivot_ratio_double),
+                           float(pivot_ratio_single))
 
     # -------------------------------------------------------------- values
     def update_Y(self, Yx):
@@ -101,19 +135,29 @@ class GpuSolver:
         _lib.check(rc, "solve_batch")
         return {"V": V, "iterations": it, "converged": cv.astype(bool)}
 
-    def solve_lanes(self, S, V0, offsets, p: _lib.Params):
+    def solve_lanes(self, S, V0, offsets, p: _lib.Params, out=None):
+        """``out`` = (V, iterations, converged) caller-owned result arrays (e.g. pinned)."""
         S = c128(S)
         V0 = c128(V0).ravel()
         off = np.ascontiguousarray(offsets, dtype=np.int64)
         T = S.shape[1]
         K = len(off) - 1
-        V = np.empty((self.n, T), dtype=np.complex128)
-        it = np.empty(T, dtype=np.int32)
-        cv = np.empty(T, dtype=np.uint8)
+        if out is None:
+            V = np.empty((self.n, T), dtype=np.complex128)
+            it = np.empty(T, dtype=np.int32)
+            cv = np.empty(T, dtype=np.uint8)
+        else:
+            V, it, cv = out
         rc = _lib.load().gbpf_solve_lanes(self._h, T, _lib.cview(S), _lib.cview(V0), K, _lib.i64(off), C.byref(p),
                                           _lib.cview(V), _lib.i32(it), _lib.u8(cv))
         _lib.check(rc, "solve_lanes")
-        return {"V": V, "iterations": it, "converged": cv.astype(bool)}
+        return {"V": V, "iterations": it, "converged": cv.view(bool) if out is not None else cv.astype(bool)}
+
+    def solve_lanes_device(self, dS: int, dV0: int, doff: int, T: int, K: int, p: _lib.Params, dV: int, dit: int,
+                           dcv: int):
+        """Device-pointer variant (inputs already resident); pointers as integers."""
+        rc = _lib.load().gbpf_solve_lanes_device(self._h, T, dS, dV0, K, doff, C.byref(p), dV, dit, dcv)
+        _lib.check(rc, "solve_lanes_device")
 
     def solve_contingency(self, S, V0, pin, p: _lib.Params, Yd=None, stamps=None):
         """S (n,), V0 (n, L), pin (n, L) or None; per-case Ybus: Yd (nnz, L) complex or

@@ -1,0 +1,269 @@
+"""GPU parity: the sm_103a path through the C ABI against the reference.
+
+Bars (written next to each comparison): the plain double path reproduces the reference's
+iteration counts and convergence flags exactly and its voltages to 1e-11; the mixed path
+reaches the same solutions (1e-9) at <= 1e-8 mismatch; island labels and served masks are
+bit-exact. Modelled on the reference's tests/cuda/test_lean_lu.py:126-326.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from oracle import cpu
+from oracle.build import build_oracle
+from p3s_gb300 import nr_klu
+from p3s_gb300.cuda.nr_polar_solver import PolarNewtonSolverCUDA
+from p3s_gb300.synthetic import grid_118, lanes, timeseries_injections
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL_V = 1e-11  # plain double path vs the reference, per bus voltage (p.u.)
+
+
+def setup_module(_):
+    build_oracle()
+
+
+def _g(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _mismatch(d, V, S):
+    """Infinity norm of the reference's mismatch F(V) per column (oracle debug_J's F)."""
+    s = cpu.Solver(d.Yp, d.Yj, d.Yx, d.pv, d.pq)
+    return np.array([np.abs(s.debug_J_at(S[:, c], V[:, c])["F"]).max() for c in range(V.shape[1])])
+
+
+@pytest.mark.parametrize("name", ["golden_118.npz", "golden_2000.npz"])
+def test_double_path_reproduces_reference(name):
+    d = _g(name)
+    r = nr_klu.Solver(d["Yp"], d["Yj"], d["Yx"], d["pv"], d["pq"]).solve_batch(d["S"], d["V0"])
+    for tag in ("fast", "strict"):
+        assert np.array_equal(r["converged"], d[f"cv_{tag}"])
+        assert np.array_equal(r["iterations"], d[f"it_{tag}"])
+        assert np.abs(r["V"] - d[f"V_{tag}"]).max() < TOL_V
+
+
+def test_double_path_matches_oracle_on_a_2000_bus_batch(grid2000):
+    S = timeseries_injections(grid2000, 192)
+    ref = cpu.Solver(grid2000.Yp, grid2000.Yj, grid2000.Yx, grid2000.pv, grid2000.pq).solve_batch(S, grid2000.V0)
+    gpu = PolarNewtonSolverCUDA(grid2000.Yp, grid2000.Yj, grid2000.Yx, grid2000.pv, grid2000.pq)
+    r = gpu.solve_batch(S, grid2000.V0)
+    assert r["converged"].all() and ref["converged"].all()
+    assert np.array_equal(r["iterations"], ref["iterations"])
+    assert np.abs(r["V"] - ref["V"]).max() < TOL_V
+    assert gpu.last_stats["single_factorizations"] == 0 and gpu.last_stats["failed_on_gpu"] == 0
+    # per-column start voltages take the same path as a shared one (bit-equal)
+    r2 = gpu.solve_batch(S, np.ascontiguousarray(np.repeat(grid2000.V0[:, None], S.shape[1], axis=1)))
+    assert np.array_equal(r2["V"], r["V"])
+
+
+@pytest.mark.parametrize("ls", [1, 0])
+def test_line_search_matches_reference_from_bad_starts(ls):
+    d = _g("golden_118.npz")
+    S = np.ascontiguousarray(np.repeat(d["Sbus"][:, None], d["V0_bad"].shape[1], axis=1))
+    gpu = PolarNewtonSolverCUDA(d["Yp"], d["Yj"], d["Yx"], d["pv"], d["pq"])
+    gpu.line_search = bool(ls)
+    r = gpu.solve_batch(S, d["V0_bad"])
+    ok = d[f"cvbad{ls}_strict"]
+    assert 0 < ok.sum() < len(ok)
+    assert np.array_equal(r["converged"], ok)
+    assert np.array_equal(r["iterations"][ok], d[f"itbad{ls}_strict"][ok])
+    assert np.abs(r["V"][:, ok] - d[f"Vbad{ls}_strict"][:, ok]).max() < 1e-10
+
+
+@pytest.mark.parametrize("switch", [1e-3, 0.0])
+def test_mixed_precision_reaches_the_same_solution(grid2000, switch):
+    g = grid2000
+    S = timeseries_injections(g, 128)
+    ref = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(S, g.V0)
+    gpu = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    double = gpu.solve_batch(S, g.V0)
+    gpu.precision = "mixed"
+    gpu.mixed_switch = switch
+    mixed = gpu.solve_batch(S, g.V0)
+    assert gpu.last_stats["single_factorizations"] > 0
+    ok = ref["converged"]
+    assert np.array_equal(mixed["converged"], ok)
+    assert np.abs(mixed["V"][:, ok] - ref["V"][:, ok]).max() < 1e-9
+    assert (_mismatch(g, mixed["V"][:, :16], S[:, :16]) <= 1e-8).all()
+    assert (mixed["iterations"][ok] <= ref["iterations"][ok] + 2).all()
+    # every float factorization rejected -> redone in double in the same step: the all-double run
+    gpu._rcond_ratio_single = 1e30
+    rejected = gpu.solve_batch(S, g.V0)
+    assert gpu.last_stats["single_rejected"] == gpu.last_stats["single_factorizations"] > 0
+    assert np.array_equal(rejected["converged"], double["converged"])
+    assert np.array_equal(rejected["iterations"], double["iterations"])
+    assert np.abs(rejected["V"] - double["V"]).max() < 1e-12
+
+
+def test_non_finite_input_fails_only_its_own_column(grid118):
+    S = timeseries_injections(grid118, 40)
+    S[3, 7] = np.nan
+    r = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq).solve_batch(S, grid118.V0)
+    expect = np.ones(40, dtype=bool)
+    expect[7] = False
+    assert np.array_equal(r["converged"], expect)
+    assert np.isfinite(r["V"][:, expect]).all()
+
+
+def test_rejected_factorization_is_reported_not_converged(grid118):
+    S = timeseries_injections(grid118, 24)
+    gpu = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq)
+    gpu._rcond_ratio = 1e30  # no factorization can pass the pivot check
+    r = gpu.solve_batch(S, grid118.V0)
+    assert not r["converged"].any()
+    assert gpu.last_stats["failed_on_gpu"] == 24
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_invalid_start_voltage_raises_like_nr_klu(grid118, bad):
+    V0 = grid118.V0.copy()
+    V0[3] = complex(bad, 0.0)
+    S = np.repeat(grid118.Sbus[:, None], 4, axis=1)
+    with pytest.raises(RuntimeError, match="invalid initial voltage"):
+        nr_klu.Solver(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq).solve_batch(S, V0)
+
+
+def test_nan_admittance_is_never_reported_converged(grid118):
+    Yx = grid118.Yx.copy()
+    row = int(grid118.pq[0])
+    k = [k for k in range(grid118.Yp[row], grid118.Yp[row + 1]) if grid118.Yj[k] == row][0]
+    Yx[k] = complex(np.nan, 0.0)
+    S = np.ascontiguousarray(np.repeat(grid118.Sbus[:, None], 4, axis=1))
+    # nr_klu surface: the solver builds, every column ends not converged (nr_klu semantics)
+    r = nr_klu.Solver(grid118.Yp, grid118.Yj, Yx, grid118.pv, grid118.pq).solve_batch(S, grid118.V0)
+    assert not r["converged"].any()
+    # PolarNewtonSolverCUDA surface: refuses the grid at construction (nr_polar_solver.py:422-426)
+    with pytest.raises(RuntimeError, match="flat start"):
+        PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, Yx, grid118.pv, grid118.pq)
+    # a NaN admittance in one case of a batch fails only that batch's NaN cases
+    gpu = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq)
+    r = gpu.solve_batch_contingency_cx(np.repeat(Yx[:, None], 4, axis=1), grid118.Sbus,
+                                       np.repeat(grid118.V0[:, None], 4, axis=1), np.zeros((118, 4), np.uint8))
+    assert not r["converged"].any()
+
+
+def test_update_Y_equals_rebuilding_the_solver(grid118):
+    S = timeseries_injections(grid118, 16)
+    Yx2 = grid118.Yx * (1.0 + 0.03 * np.random.default_rng(4).standard_normal(grid118.nnz))
+    gpu = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq)
+    before = gpu.solve_batch(S, grid118.V0)["V"]
+    gpu.update_Y(Yx2)
+    after = gpu.solve_batch(S, grid118.V0)
+    fresh = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, Yx2, grid118.pv, grid118.pq).solve_batch(S, grid118.V0)
+    assert after["converged"].all()
+    assert np.array_equal(after["V"], fresh["V"])
+    assert np.abs(after["V"] - before).max() > 1e-6
+    with pytest.raises(ValueError):
+        gpu.update_Y(Yx2[:-1])
+
+
+def test_debug_J_matches_reference():
+    d = _g("golden_118.npz")
+    j = nr_klu.debug_J(d["Yp"], d["Yj"], d["Yx"], d["Sbus"], d["V0"], d["pv"], d["pq"])
+    assert np.array_equal(j["Jp"], d["Jp"]) and np.array_equal(j["Ji"], d["Ji"])
+    assert np.abs(j["Jx"] - d["Jx"]).max() < 1e-10
+
+
+def test_solve_single_and_solve(grid118):
+    ref = cpu.solve_single(grid118.Yp, grid118.Yj, grid118.Yx, grid118.Sbus, grid118.V0, grid118.pv, grid118.pq)
+    r = nr_klu.solve_single(grid118.Yp, grid118.Yj, grid118.Yx, grid118.Sbus, grid118.V0, grid118.pv, grid118.pq)
+    assert set(r) >= {"V", "iterations", "converged", "t_setup_ms", "t_solve_ms", "t_assemble_ms", "profiled"}
+    assert r["iterations"] == ref["iterations"] and r["converged"]
+    assert np.abs(r["V"] - ref["V"]).max() < TOL_V
+
+
+def test_results_do_not_depend_on_the_batch_mix(grid2000):
+    """Continuous batching: a case gives the same bits alone, in a batch, and in a
+    differently composed batch (slots are independent)."""
+    g = grid2000
+    S = timeseries_injections(g, 300)
+    gpu = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    full = gpu.solve_batch(S, g.V0)
+    idx = np.random.default_rng(3).permutation(300)[:37]
+    part = gpu.solve_batch(np.ascontiguousarray(S[:, idx]), g.V0)
+    assert np.array_equal(part["V"], full["V"][:, idx])
+    one = gpu.solve_batch(np.ascontiguousarray(S[:, idx[:1]]), g.V0)
+    assert np.array_equal(one["V"][:, 0], full["V"][:, idx[0]])
+
+
+def test_warm_start_lanes_match_the_oracle_replay(grid2000):
+    g = grid2000
+    S = timeseries_injections(g, 120)
+    off = lanes(120, 16)
+    ref = cpu.solve_lanes(cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq), S, g.V0, off)
+    gpu = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    r = gpu.solve_timeseries_lanes(S, g.V0, off)
+    assert r["converged"].all() and ref["converged"].all()
+    assert np.array_equal(r["iterations"], ref["iterations"])
+    assert np.abs(r["V"] - ref["V"]).max() < TOL_V
+    assert r["iterations"].mean() < 6  # warm starts pay off
+
+
+def test_contingency_stamps_equal_dense_and_reference():
+    d = _g("golden_n1_118.npz")
+    L = d["pin"].shape[1]
+    Yx = np.repeat(d["Yx"][:, None], L, axis=1)
+    rows, cols, vals = [], [], []
+    for c in range(1, L):
+        b = c - 1
+        np.subtract.at(Yx[:, c], d["stamp_pos"][b], d["stamp"][b])
+        rows.append(d["stamp_pos"][b])
+        cols.append(np.full(4, c))
+        vals.append(d["stamp"][b])
+    import scipy.sparse as sp
+
+    stamp = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(len(d["Yx"]), L)).tocsc()
+    gpu = PolarNewtonSolverCUDA(d["Yp"], d["Yj"], d["Yx"], d["pv"], d["pq"])
+    dense = gpu.solve_batch_contingency_cx(Yx, d["Sbus"], d["V0n1"], d["pin"])
+    st = gpu.solve_batch_contingency_stamp(stamp, d["Sbus"], d["V0n1"], d["pin"])
+    polar = gpu.solve_batch_contingency(np.abs(Yx), np.angle(Yx), d["Sbus"], d["V0n1"], d["pin"])
+    ok = d["cv_strict"]
+    assert np.array_equal(dense["converged"], ok) and ok.any()
+    assert np.array_equal(st["V"], dense["V"])
+    assert np.array_equal(st["iterations"], d["it_strict"]) or np.array_equal(st["iterations"][ok],
+                                                                               d["it_strict"][ok])
+    assert np.abs(dense["V"][:, ok] - d["V_strict"][:, ok]).max() < 1e-10
+    assert np.abs(polar["V"][:, ok] - d["V_strict"][:, ok]).max() < 1e-10
+    # the nr_klu surface takes magnitude / angle
+    nk = nr_klu.Solver(d["Yp"], d["Yj"], d["Yx"], d["pv"], d["pq"]).solve_batch_contingency(
+        np.abs(Yx), np.angle(Yx), d["Sbus"], d["V0n1"], d["pin"])
+    assert np.array_equal(nk["converged"], ok)
+
+
+def test_islands_match_reference_bit_exact():
+    from p3s_gb300 import contingency
+
+    d = _g("golden_n1_118.npz")
+    g = grid_118()
+    assert np.array_equal(g.Yx, d["Yx"])
+    batch = contingency.build_batch(g)
+    prio = np.zeros(g.n)
+    prio[g.pv] = g.p_gen[g.pv]
+    lab, sv, rb, ni = contingency.islands(batch, True, prio)
+    assert lab.dtype == np.int32
+    assert np.array_equal(lab, d["labels"]) and np.array_equal(sv, d["served"])
+    assert np.array_equal(rb, d["ref_bus"]) and np.array_equal(ni, d["n_islands"])
+    lab0, sv0, rb0, _ = contingency.islands(batch, False, prio)
+    assert np.array_equal(lab0, d["labels"]) and (sv0 <= sv).all() and (~sv0).sum() > (~sv).sum()
+
+
+def test_contingency_driver_matches_reference():
+    from p3s_gb300 import contingency
+
+    d = _g("golden_n1_118.npz")
+    g = grid_118()
+    res = contingency.solve_contingencies(g, reslack_islands=True)
+    assert np.array_equal(res.served, d["served"])
+    ok = d["cv_strict"]
+    assert np.array_equal(res.converged, ok)
+    assert np.isnan(res.V[~res.served]).all() and np.isfinite(res.V[:, ok][res.served[:, ok]]).all()
+    Vs = np.where(d["served"], d["V_strict"], np.nan)
+    assert np.nanmax(np.abs(res.V[:, ok] - Vs[:, ok])) < 1e-10
+    mixed = contingency.solve_contingencies(g, reslack_islands=True, precision="mixed")
+    assert np.array_equal(mixed.converged, ok) and np.array_equal(mixed.served, d["served"])
+    assert np.nanmax(np.abs(mixed.V[:, ok] - Vs[:, ok])) < 1e-9

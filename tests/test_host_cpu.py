@@ -1,0 +1,103 @@
+"""Host-side pieces that need no GPU: the synthetic inputs, the planner and the device
+schedule (executed serially on the CPU), the C ABI's exported symbols, the multi-rank
+case sharding."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+from oracle import cpu
+from p3s_gb300 import _lib
+from p3s_gb300.synthetic import grid_118, grid_2000, lanes, make_grid, timeseries_injections
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_synthetic_sizes_match_the_configs(grid118, grid2000):
+    assert (grid118.n, grid118.n_branch, grid118.nnz, len(grid118.pv), len(grid118.pq)) == (118, 186, 490, 19, 98)
+    assert (grid2000.n, grid2000.n_branch, grid2000.nnz, len(grid2000.pv), len(grid2000.pq)) == (
+        2000, 3000, 8000, 300, 1699)
+    # the branch stamps sum to the Ybus
+    Y = np.zeros(grid2000.nnz, dtype=complex)
+    np.add.at(Y, grid2000.stamp_pos.ravel(), grid2000.stamp.ravel())
+    assert np.abs(Y - grid2000.Yx).max() < 1e-10
+    # deterministic
+    g2 = grid_118(0)
+    assert np.array_equal(g2.Yx, grid118.Yx) and np.array_equal(g2.pv, grid118.pv)
+
+
+def test_timeseries_and_lanes(grid118):
+    S = timeseries_injections(grid118, 48)
+    assert S.shape == (118, 48) and S.flags.c_contiguous
+    # hourly generation follows the hourly load (balanced dispatch)
+    ratio = S[grid118.pv].real.sum(axis=0) / -S[grid118.pq].real.sum(axis=0)
+    assert np.allclose(ratio, grid118.p_gen.sum() / grid118.p_load.sum())
+    off = lanes(8760, 1216)
+    assert off[0] == 0 and off[-1] == 8760 and len(off) == 1217 and set(np.diff(off)) <= {7, 8}
+
+
+def _selftest(g, workers, seed=1):
+    L = _lib.load()
+    rng = np.random.default_rng(seed)
+    Vm = np.abs(g.V0) * (1 + 0.02 * rng.standard_normal(g.n))
+    Va = np.angle(g.V0) + 0.05 * rng.standard_normal(g.n)
+    dx = np.zeros(2 * g.n)
+    shape = np.zeros(7, np.int32)
+    msg = C.create_string_buffer(256)
+    Yx = np.ascontiguousarray(g.Yx)
+    S = np.ascontiguousarray(g.Sbus)
+    rc = L.gbpf_plan_selftest(g.n, _lib.i32(g.Yp), _lib.i32(g.Yj), _lib.cview(Yx), g.nnz, _lib.i32(g.pv), len(g.pv),
+                              _lib.i32(g.pq), len(g.pq), workers, _lib.d(Vm), _lib.d(Va), _lib.cview(S), _lib.d(dx),
+                              _lib.i32(shape), msg, 256)
+    assert rc == 0, msg.value
+    d = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).debug_J_at(g.Sbus, Vm * np.exp(1j * Va))
+    J = sp.csc_matrix((d["Jx"], d["Ji"], d["Jp"]), shape=(d["m"], d["m"]))
+    x = spl.spsolve(J, -d["F"])
+    pvpq = np.r_[g.pv, g.pq]
+    ref = np.zeros((g.n, 2))
+    ref[pvpq, 0] = x[: len(pvpq)]
+    ref[g.pq, 1] = x[len(pvpq):]
+    return np.abs(dx.reshape(-1, 2) - ref).max() / max(1.0, np.abs(ref).max()), shape
+
+
+@pytest.mark.parametrize("workers", [1, 16, 64])
+def test_block_schedule_solves_the_power_flow_jacobian(workers):
+    """The device's 2x2-block LU schedule, executed serially with a race check per level,
+    solves what scipy solves (the reference's test_plan_solves_power_flow_jacobian)."""
+    for g in (grid_118(), grid_2000()):
+        err, shape = _selftest(g, workers)
+        assert err < 1e-9, err
+
+
+def test_block_schedule_large_and_irregular():
+    err, shape = _selftest(make_grid(20000, seed=3), 64)
+    assert err < 1e-9
+    err, shape = _selftest(make_grid(30, seed=4), 32)
+    assert err < 1e-9
+
+
+def test_library_exports_every_declared_symbol():
+    """libgbpf.so loads without a GPU and exports every function include/gbpf.h declares."""
+    L = _lib.load()
+    hdr = open(os.path.join(ROOT, "include", "gbpf.h")).read()
+    names = set(re.findall(r"\b(gbpf_[a-z0-9_]+)\s*\(", hdr))
+    names -= {n for n in names if n.endswith("_t")}
+    assert len(names) >= 18
+    for n in sorted(names):
+        assert hasattr(L, n), n
+        assert n in _lib.SIGNATURES, n
+    assert L.gbpf_version() >= 100
+    assert L.gbpf_device_count() >= 0
+
+
+def test_case_sharding_covers_every_case_once():
+    from bench import shard
+
+    for B, W in ((8760, 1), (8760, 2), (3001, 4), (5, 8)):
+        seen = np.concatenate([np.arange(*shard(B, r, W)) for r in range(W)])
+        assert np.array_equal(np.sort(seen), np.arange(B))
