@@ -33,6 +33,8 @@ typedef struct gbpf_params {
     int check_v0;        /* 1: reject non-finite / out-of-range start voltages like solve_batch */
     double pivot_ratio_double; /* accept a double factorization while min|piv|/max|piv| >= this x rcond0 (1e-3) */
     double pivot_ratio_single; /* the same bound for a float factorization (1e-3) */
+    int vote_rule;       /* mixed: 0 = the reference's precision votes (nr_polar_kernels.cu:209-228),
+                            1 = float until contraction stalls below mixed_switch */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */

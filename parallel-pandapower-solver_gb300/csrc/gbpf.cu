@@ -90,7 +90,7 @@ struct gbpf_solver {
         drow_pq, dbus_of_row, ddpos;
     gbpf::DevPlan dp{};
     // scratch (per CTA, grow-only)
-    DBuf fac64, fac32, R, y64, y32, Vc, Vt, Et, V32, spin;
+    DBuf fac64, fac32, R, y64, y32, Vc, Vt, Et, Ei, V32, spin;
     size_t sc_ctas = 0;
     bool sc_mixed = false;
     // per-call buffers (grow-only)
@@ -99,7 +99,7 @@ struct gbpf_solver {
     ~gbpf_solver() {
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dtaskA, &dptrA, &dscl, &dptrB,
                         &dtaskC, &dptrC, &dpairs, &drow_pq, &dbus_of_row, &ddpos, &fac64, &fac32, &R, &y64, &y32,
-                        &Vc, &Vt, &Et, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
+                        &Vc, &Vt, &Et, &Ei, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
                         &bYd, &bpin})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
@@ -236,6 +236,7 @@ int ensure_scratch(gbpf_solver* s, size_t ctas, bool mixed) {
     CK(s->Vc.ensure(ctas * n * G * 32));
     CK(s->Vt.ensure(ctas * n * G * 32));
     CK(s->Et.ensure(ctas * n * G * 16));
+    CK(s->Ei.ensure(ctas * n * G * 8));
     CK(s->V32.ensure(ctas * n * G * 16));
     CK(s->spin.ensure(ctas * n * G));
     if (mixed) {
@@ -262,6 +263,7 @@ gbpf::Scratch scratch_view(gbpf_solver* s) {
     sc.Vc = s->Vc.as<double4_32a>();
     sc.Vt = s->Vt.as<double4_32a>();
     sc.Et = s->Et.as<double2>();
+    sc.Ei = s->Ei.as<double>();
     sc.V32 = s->V32.as<float4>();
     sc.pin = s->spin.as<uint8_t>();
     return sc;
@@ -277,6 +279,7 @@ gbpf_params default_params() {
     p.check_v0 = 0;
     p.pivot_ratio_double = 1e-3;
     p.pivot_ratio_single = 1e-3;
+    p.vote_rule = 1;
     return p;
 }
 
@@ -342,6 +345,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.line_search = p.line_search;
     b.mixed = p.precision == 1;
     b.mixed_switch = p.mixed_switch;
+    b.vote_rule = p.vote_rule;
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
@@ -622,9 +626,9 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
                        double* residual) {
     if (!s) return fail("null solver");
     const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv);
-    DBuf dV, dSb, dpin, dVt, dEt, dV32, dblk, dR;
+    DBuf dV, dSb, dpin, dVt, dEt, dEi, dV32, dblk, dR;
     auto cleanup = [&]() {
-        for (DBuf* b : {&dV, &dSb, &dpin, &dVt, &dEt, &dV32, &dblk, &dR}) b->release();
+        for (DBuf* b : {&dV, &dSb, &dpin, &dVt, &dEt, &dEi, &dV32, &dblk, &dR}) b->release();
     };
     struct Guard {
         std::function<void()> f;
@@ -634,6 +638,7 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
     CK(dSb.ensure(n * 16));
     CK(dVt.ensure(n * 32));
     CK(dEt.ensure(n * 16));
+    CK(dEi.ensure(n * 8));
     CK(dV32.ensure(n * 16));
     CK(dblk.ensure(nb * 32));
     CK(dR.ensure(nv * 16));
@@ -646,7 +651,8 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
         CK(cudaMemcpy(dpin.p, pin, n, cudaMemcpyHostToDevice));
     }
     CK(gbpf::launch_eval_debug(s->dp, dV.as<double2>(), dSb.as<double2>(), pin ? dpin.as<uint8_t>() : nullptr,
-                               dVt.as<double4_32a>(), dEt.as<double2>(), dV32.as<float4>(), dblk.as<double4_32a>(),
+                               dVt.as<double4_32a>(), dEt.as<double2>(), dEi.as<double>(), dV32.as<float4>(),
+                               dblk.as<double4_32a>(),
                                dR.as<double2>(), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpy(blocks, dblk.p, nb * 32, cudaMemcpyDeviceToHost));

@@ -81,6 +81,7 @@ struct Batch {
     int line_search;
     int mixed;               // 0: all factorizations double; 1: vote per case
     double mixed_switch;
+    int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch
@@ -101,7 +102,8 @@ struct Scratch {
     double4_32a* Vc;             // committed point (Vm, Va, cos, sin)
     double4_32a* Vt;             // evaluation point (Vm, Va, cos, sin)
     double2* Et;             // evaluation point rectangular (e, f)
-    float4* V32;             // evaluation point (Vm, cos, sin, 0) in float
+    double* Ei;              // evaluation point 1 / Vm
+    float4* V32;             // evaluation point (e, f, 1 / Vm, 0) in float
     uint8_t* pin;            // [cta][bus][slot]
 };
 
@@ -109,8 +111,8 @@ struct Scratch {
 cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
                           cudaStream_t stream);
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                              double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R,
-                              cudaStream_t stream);
+                              double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                              double2* R, cudaStream_t stream);
 int newton_max_threads();
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
 const void* newton_kernel_ptr();

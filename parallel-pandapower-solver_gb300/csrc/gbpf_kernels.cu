@@ -39,11 +39,28 @@ __device__ __forceinline__ bool finite_d(double x) {
     return (dbits(x) & 0x7ff0000000000000ULL) != 0x7ff0000000000000ULL;
 }
 
-// cos/sin of a small angle |d| <= 1/4 from their Maclaurin series (Horner in d^2); the
-// truncation error is below 3e-18 on that range. Used to ROTATE a bus phasor by the
+// cos/sin of a small angle |d| <= 1/4 from their Maclaurin series (Horner in d^2), with as
+// many terms as |d| needs (the first dropped term stays below double rounding); the
+// truncation error is below 3e-18 on the whole range. Used to ROTATE a bus phasor by the
 // Newton angle increment instead of evaluating sincos of the full angle.
-__device__ __forceinline__ void sincos_small(double d, double* s, double* c) {
+__device__ __forceinline__ void sincos_small(double d, double ad, double* s, double* c) {
     const double z = d * d;
+    if (ad <= 0x1p-14) {  // next terms below 2^-100: d^5/120 and d^4/24
+        *s = fma(z * (-1.0 / 6.0), d, d);
+        *c = fma(z, -0.5, 1.0);
+        return;
+    }
+    if (ad <= 0x1p-6) {  // next terms below 2^-60 relative: d^9/9! and d^8/8!
+        double ps = -1.0 / 5040.0;
+        ps = fma(ps, z, 1.0 / 120.0);
+        ps = fma(ps, z, -1.0 / 6.0);
+        *s = fma(ps * z, d, d);
+        double pc = -1.0 / 720.0;
+        pc = fma(pc, z, 1.0 / 24.0);
+        pc = fma(pc, z, -0.5);
+        *c = fma(pc, z, 1.0);
+        return;
+    }
     double ps = -1.0 / 39916800.0;
     ps = fma(ps, z, 1.0 / 362880.0);
     ps = fma(ps, z, -1.0 / 5040.0);
@@ -60,20 +77,25 @@ __device__ __forceinline__ void sincos_small(double d, double* s, double* c) {
 }
 
 // --------------------------------------------------------------------------------------
-// Evaluation of one bus row for one slot. Off-diagonal Ybus entry (i, j), phasors u = V/|V|:
-//   X = u_i conj(Y_ij u_j) = |Y| e^{j delta},  delta = th_i - angle(Y_ij) - th_j,
-//   W = Vm_i Vm_j X        (real / imaginary part: the P / Q flow term of the entry).
-// Jacobian block (i, j) = [dP/dth_j dP/dVm_j; dQ/dth_j dQ/dVm_j] = [Im W, Vm_i Re X;
-// -Re W, Vm_i Im X]; the diagonal block accumulates the negated off-diagonal angle terms
-// and the magnitude terms: the formulas of nr_klu.cpp:344-378 in this notation. PV buses
-// carry an identity dummy in their magnitude column and Q row; pinned buses
-// (nr_klu.cpp:398-423) get identity rows and a zero residual.
+// Evaluation of one bus row for one slot, rectangular state e + jf = V.
+//   I_i = sum_j Y_ij V_j                      (4 double FMAs per entry)
+//   P_i + jQ_i = V_i conj(I_i),   residual R = S_spec - (P_i + jQ_i)
+// The mismatch is computed with the same instructions in every mode, so the float and the
+// double Jacobian paths see bit-identical residuals. Off-diagonal Jacobian block (i, j), with
+// W = V_i conj(Y_ij V_j) (its real / imaginary part: the P / Q flow term of the entry):
+//   [dP/dth_j dP/dVm_j; dQ/dth_j dQ/dVm_j] = [Im W, Re W / Vm_j; -Re W, Im W / Vm_j]
+// and the diagonal block follows from P_i, Q_i and the self term S_ii = |V_i|^2 conj(Y_ii):
+//   dP/dth_i = Q_ii - Q_i, dQ/dth_i = P_i - P_ii, dP/dVm_i = (P_i + P_ii)/Vm_i, dQ/dVm_i = (Q_i + Q_ii)/Vm_i
+// -- the derivative formulas of nr_klu.cpp:344-378 (polar form, accumulated per entry there)
+// rewritten without per-entry trigonometry. PV buses carry an identity dummy in their
+// magnitude column and Q row; pinned buses (nr_klu.cpp:398-423) get identity rows and a
+// zero residual. JM: 0 = mismatch only, 1 = double Jacobian, 2 = float Jacobian.
 // --------------------------------------------------------------------------------------
 struct EvalCtx {
     const DevPlan* P;
-    const double4_32a* Vt;   // [bus][slot] (Vm, Va, cos, sin)
     const double2* Et;   // [bus][slot] (e, f)
-    const float4* V32;   // [bus][slot] (Vm, cos, sin, 0)
+    const double* Ei;    // [bus][slot] 1 / Vm
+    const float4* V32;   // [bus][slot] (e, f, 1 / Vm, 0) in float
     int lg;
     int ymode;
     const double2* Yd;
@@ -104,66 +126,82 @@ __device__ __forceinline__ double2 ybus_val(const EvalCtx& c, int k, unsigned ma
     return y;
 }
 
-__device__ __forceinline__ void put_block(double4_32a* fac, size_t at, double4_32a o) { fac[at] = o; }
-__device__ __forceinline__ void put_block(float4* fac, size_t at, double4_32a o) {
-    fac[at] = make_float4((float)o.x, (float)o.y, (float)o.z, (float)o.w);
+__device__ __forceinline__ void put_block(double4_32a* fac, size_t at, double a, double b, double c, double d) {
+    fac[at] = make_double4_32a(a, b, c, d);
+}
+__device__ __forceinline__ void put_block(float4* fac, size_t at, double a, double b, double c, double d) {
+    fac[at] = make_float4((float)a, (float)b, (float)c, (float)d);
 }
 
-// Double-precision row: mismatch from the W terms, Jacobian (if WJ) into `fac`.
-template <bool WJ, typename FacT>
-__device__ double eval_row_x(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp,
-                             FacT* fac, double2* R, bool write_r) {
+template <int JM, typename FacT>
+__device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp, FacT* fac,
+                           double2* R, bool write_r) {
     const DevPlan& P = *c.P;
-    const double4_32a vi4 = c.Vt[((size_t)i << c.lg) + s];
-    const double vi = vi4.x, ci = vi4.z, si = vi4.w;
-    double Pc = 0.0, Qc = 0.0, dPa = 0.0, dQa = 0.0, dPm = 0.0, dQm = 0.0;
+    const size_t si = ((size_t)i << c.lg) + s;
+    const double2 ei = c.Et[si];
+    float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (JM == 2) vi32 = c.V32[si];
+    double Ir = 0.0, Ii = 0.0, gii = 0.0, bii = 0.0;
     const int k0 = P.Yp[i], k1 = P.Yp[i + 1];
     const unsigned mask = row_stamp_mask(c, k0, k1);
     for (int k = k0; k < k1; ++k) {
         const int j = P.Yj[k];
         const double2 y = ybus_val(c, k, mask);
-        if (j != i) {
-            const double4_32a vj4 = c.Vt[((size_t)j << c.lg) + s];
-            const double vj = vj4.x, cj = vj4.z, sj = vj4.w;
-            const double wr = y.x * cj - y.y * sj, wi = y.x * sj + y.y * cj;
-            const double xr = ci * wr + si * wi, xi = si * wr - ci * wi;
-            const double vx = vi * xr, vy = vi * xi;
-            const double Wr = vx * vj, Wi = vy * vj;
-            Pc += Wr;
-            Qc += Wi;
-            if (WJ) {
-                dPa -= Wi;
-                dQa += Wr;
-                dPm += vj * xr;
-                dQm += vj * xi;
-                const int q = P.posmap[k];
-                if (q >= 0) {
-                    const bool pq_j = P.bus_pq[j] != 0;
-                    double4_32a o;
-                    if (pinned) {
-                        o = make_double4_32a(0.0, 0.0, 0.0, 0.0);
-                    } else {
-                        o.x = Wi;
-                        o.y = pq_j ? vx : 0.0;
-                        o.z = pq_i ? -Wr : 0.0;
-                        o.w = (pq_i && pq_j) ? vy : 0.0;
-                    }
-                    put_block(fac, ((size_t)q << c.lg) + s, o);
-                }
-            }
+        const size_t sj = ((size_t)j << c.lg) + s;
+        const double2 ej = c.Et[sj];
+        Ir = fma(y.x, ej.x, Ir);
+        Ir = fma(-y.y, ej.y, Ir);
+        Ii = fma(y.x, ej.y, Ii);
+        Ii = fma(y.y, ej.x, Ii);
+        if (j == i) {
+            gii = y.x;
+            bii = y.y;
+            continue;
+        }
+        if (JM == 0) continue;
+        const int q = P.posmap[k];
+        if (q < 0) continue;
+        const bool pq_j = P.bus_pq[j] != 0;
+        const size_t at = ((size_t)q << c.lg) + s;
+        if (pinned) {
+            put_block(fac, at, 0.0, 0.0, 0.0, 0.0);
+            continue;
+        }
+        if (JM == 1) {
+            const double wr = fma(-y.y, ej.y, y.x * ej.x), wi = fma(y.y, ej.x, y.x * ej.y);
+            const double Wr = fma(ei.x, wr, ei.y * wi), Wi = fma(ei.y, wr, -ei.x * wi);
+            const double ivj = c.Ei[sj];
+            put_block(fac, at, Wi, pq_j ? Wr * ivj : 0.0, pq_i ? -Wr : 0.0, (pq_i && pq_j) ? Wi * ivj : 0.0);
         } else {
-            Pc += vi * vi * y.x;
-            Qc -= vi * vi * y.y;
-            if (WJ) {
-                dPm += 2.0 * vi * y.x;
-                dQm -= 2.0 * vi * y.y;
+            float gx, gy;
+            if (c.ymode == 0) {
+                const float2 y32 = P.Y32[k];
+                gx = y32.x;
+                gy = y32.y;
+            } else {
+                gx = (float)y.x;
+                gy = (float)y.y;
             }
+            const float4 vj = c.V32[sj];
+            const float wr = fmaf(-gy, vj.y, gx * vj.x), wi = fmaf(gy, vj.x, gx * vj.y);
+            const float Wr = fmaf(vi32.x, wr, vi32.y * wi), Wi = fmaf(vi32.y, wr, -vi32.x * wi);
+            reinterpret_cast<float4*>(fac)[at] =
+                make_float4(Wi, pq_j ? Wr * vj.z : 0.f, pq_i ? -Wr : 0.f, (pq_i && pq_j) ? Wi * vj.z : 0.f);
         }
     }
-    if (WJ) {
-        const double4_32a o = pinned ? make_double4_32a(1.0, 0.0, 0.0, 1.0)
-                                 : make_double4_32a(dPa, pq_i ? dPm : 0.0, pq_i ? dQa : 0.0, pq_i ? dQm : 1.0);
-        put_block(fac, ((size_t)P.dpos[row] << c.lg) + s, o);
+    const double Pc = fma(ei.x, Ir, ei.y * Ii);
+    const double Qc = fma(ei.y, Ir, -ei.x * Ii);
+    if (JM != 0) {
+        const size_t at = ((size_t)P.dpos[row] << c.lg) + s;
+        if (pinned) {
+            put_block(fac, at, 1.0, 0.0, 0.0, 1.0);
+        } else {
+            const double vi2 = fma(ei.x, ei.x, ei.y * ei.y);
+            const double Ps = vi2 * gii, Qs = -vi2 * bii;
+            const double ivi = JM == 1 ? c.Ei[si] : (double)vi32.z;
+            put_block(fac, at, Qs - Qc, pq_i ? (Pc + Ps) * ivi : 0.0, pq_i ? Pc - Ps : 0.0,
+                      pq_i ? (Qc + Qs) * ivi : 1.0);
+        }
     }
     const double rp = pinned ? 0.0 : Ssp.x - Pc;
     const double rq = (pinned || !pq_i) ? 0.0 : Ssp.y - Qc;
@@ -172,79 +210,13 @@ __device__ double eval_row_x(const EvalCtx& c, int i, int s, int row, bool pinne
     return (b > a || b != b) ? b : a;
 }
 
-// Mixed-precision row: mismatch in double from rectangular coordinates,
-//   I_i = sum_j Y_ij V_j,  P + jQ = V_i conj(I_i),
-// (four double FMAs per entry), and the Jacobian (if WJ) in float from the float copy of
-// the state (same formulas as eval_row_x).
-template <bool WJ>
-__device__ double eval_row_mixed(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp,
-                                 float4* fac, double2* R) {
-    const DevPlan& P = *c.P;
-    const double2 ei = c.Et[((size_t)i << c.lg) + s];
-    double Ir = 0.0, Ii = 0.0;
-    float dPa = 0.f, dQa = 0.f, dPm = 0.f, dQm = 0.f;
-    float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (WJ) vi32 = c.V32[((size_t)i << c.lg) + s];
-    const int k0 = P.Yp[i], k1 = P.Yp[i + 1];
-    const unsigned mask = row_stamp_mask(c, k0, k1);
-    for (int k = k0; k < k1; ++k) {
-        const int j = P.Yj[k];
-        const double2 y = ybus_val(c, k, mask);
-        const double2 ej = c.Et[((size_t)j << c.lg) + s];
-        Ir = fma(y.x, ej.x, fma(-y.y, ej.y, Ir));
-        Ii = fma(y.x, ej.y, fma(y.y, ej.x, Ii));
-        if (WJ) {
-            float gx, gy;
-            if (c.ymode == 0 && !mask) {
-                const float2 y32 = P.Y32[k];
-                gx = y32.x;
-                gy = y32.y;
-            } else {
-                gx = (float)y.x;
-                gy = (float)y.y;
-            }
-            if (j != i) {
-                const float4 vj = c.V32[((size_t)j << c.lg) + s];
-                const float wr = gx * vj.y - gy * vj.z, wi = gx * vj.z + gy * vj.y;
-                const float xr = vi32.y * wr + vi32.z * wi, xi = vi32.z * wr - vi32.y * wi;
-                const float vx = vi32.x * xr, vy = vi32.x * xi;
-                const float Wr = vx * vj.x, Wi = vy * vj.x;
-                dPa -= Wi;
-                dQa += Wr;
-                dPm += vj.x * xr;
-                dQm += vj.x * xi;
-                const int q = P.posmap[k];
-                if (q >= 0) {
-                    const bool pq_j = P.bus_pq[j] != 0;
-                    float4 o;
-                    if (pinned) {
-                        o = make_float4(0.f, 0.f, 0.f, 0.f);
-                    } else {
-                        o.x = Wi;
-                        o.y = pq_j ? vx : 0.f;
-                        o.z = pq_i ? -Wr : 0.f;
-                        o.w = (pq_i && pq_j) ? vy : 0.f;
-                    }
-                    fac[((size_t)q << c.lg) + s] = o;
-                }
-            } else {
-                dPm += 2.f * vi32.x * gx;
-                dQm -= 2.f * vi32.x * gy;
-            }
-        }
-    }
-    if (WJ) {
-        const float4 o = pinned ? make_float4(1.f, 0.f, 0.f, 1.f)
-                                : make_float4(dPa, pq_i ? dPm : 0.f, pq_i ? dQa : 0.f, pq_i ? dQm : 1.f);
-        fac[((size_t)P.dpos[row] << c.lg) + s] = o;
-    }
-    const double Pc = fma(ei.x, Ir, ei.y * Ii);
-    const double Qc = fma(ei.y, Ir, -ei.x * Ii);
-    const double rp = pinned ? 0.0 : Ssp.x - Pc;
-    const double rq = (pinned || !pq_i) ? 0.0 : Ssp.y - Qc;
-    R[((size_t)row << c.lg) + s] = make_double2(rp, rq);
-    const double a = fabs(rp), b = fabs(rq);
-    return (b > a || b != b) ? b : a;
+// Reciprocal of a positive double: float seed refined by two Newton-Raphson steps
+// r <- r (2 - x r) (quadratic convergence: ~2^-24 -> 2^-48 -> below double rounding).
+__device__ __forceinline__ double recip_nr(double x) {
+    double r = (double)__frcp_rn((float)x);
+    r = r * fma(-x, r, 2.0);
+    r = r * fma(-x, r, 2.0);
+    return r;
 }
 
 // ---------------------------------------------------------------------------- block LU
@@ -411,6 +383,7 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
     double4_32a* Vc = Sc.Vc + cta * Sc.bus_stride;
     double4_32a* Vt = Sc.Vt + cta * Sc.bus_stride;
     double2* Et = Sc.Et + cta * Sc.bus_stride;
+    double* Ei = Sc.Ei + cta * Sc.bus_stride;
     float4* V32 = Sc.V32 + cta * Sc.bus_stride;
     uint8_t* spin = Sc.pin + cta * Sc.bus_stride;
     const int n = P.n;
@@ -527,8 +500,10 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
             const double4_32a v = make_double4_32a(vm, va, cs, sn);
             Vc[idx] = v;
             Vt[idx] = v;
-            Et[idx] = make_double2(vm * cs, vm * sn);
-            V32[idx] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+            const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
+            Et[idx] = make_double2(e, f);
+            Ei[idx] = iv;
+            V32[idx] = make_float4((float)e, (float)f, (float)iv, 0.f);
             spin[idx] = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
         }
 
@@ -564,13 +539,18 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
         if (anyre) {  // this step's factorization is double but the Jacobian was built in float
             for (int idx = tid; idx < nG; idx += NT) {
                 const int s = idx & (G - 1);
+                if (s_reeval[s]) Ei[idx] = recip_nr(Vt[idx].x);
+            }
+            __syncthreads();
+            for (int idx = tid; idx < nG; idx += NT) {
+                const int s = idx & (G - 1);
                 if (!s_reeval[s]) continue;
                 const int bus = idx >> lg;
                 const int row = P.row_of_bus[bus];
                 if (row < 0) continue;
-                EvalCtx ec{&P, Vt, Et, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
-                eval_row_x<true>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0), fac64,
-                                 R, false);
+                EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
+                eval_row<1>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0), fac64, R,
+                            false);
             }
             __syncthreads();
             if (tid < G && s_reeval[tid]) s_jprec[tid] = 0;
@@ -620,20 +600,33 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
                 dvm = d.y;
             }
             const double va = vc.y + a * dth;  // nr_klu.cpp:665-669 (form_trial)
-            const double vm = P.bus_pq[bus] ? vc.x + a * dvm : vc.x;
+            const bool pq = P.bus_pq[bus] != 0;
+            const double vm = pq ? vc.x + a * dvm : vc.x;
             double cs, sn;
             const double d = a * dth;
-            if (fabs(d) <= 0.25) {
+            const double ad = fabs(d);
+            if (ad <= 0.25) {  // rotate the committed phasor by d
                 double sd, cd;
-                sincos_small(d, &sd, &cd);
+                sincos_small(d, ad, &sd, &cd);
                 cs = vc.z * cd - vc.w * sd;
                 sn = vc.w * cd + vc.z * sd;
             } else {
                 sincos(va, &sn, &cs);
             }
             Vt[idx] = make_double4_32a(vm, va, cs, sn);
-            Et[idx] = make_double2(vm * cs, vm * sn);
-            V32[idx] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+            const double e = vm * cs, f = vm * sn;
+            Et[idx] = make_double2(e, f);
+            float ivf;
+            if (!pq) {
+                ivf = V32[idx].z;  // magnitude fixed: 1/Vm unchanged since the case was loaded
+            } else if (!Bt.mixed || s_vote[s] != 1) {  // the next Jacobian is double
+                const double iv = recip_nr(vm);
+                Ei[idx] = iv;
+                ivf = (float)iv;
+            } else {
+                ivf = __frcp_rn((float)vm);
+            }
+            V32[idx] = make_float4((float)e, (float)f, ivf, 0.f);
         }
         if (tid < G) {
             const int st = s_st[tid];
@@ -654,20 +647,14 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
             const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
             const bool pinned = spin[idx] != 0;
             const bool pq = P.bus_pq[bus] != 0;
-            EvalCtx ec{&P, Vt, Et, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
+            EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             double worst;
-            if (!Bt.mixed) {
-                if (st == SL_BACKTRACK)
-                    worst = eval_row_x<false>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
-                else
-                    worst = eval_row_x<true>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
-            } else if (st == SL_BACKTRACK) {
-                worst = eval_row_mixed<false>(ec, bus, s, row, pinned, pq, Ssp, fac32, R);
-            } else if (s_jprec[s]) {
-                worst = eval_row_mixed<true>(ec, bus, s, row, pinned, pq, Ssp, fac32, R);
-            } else {
-                worst = eval_row_x<true>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
-            }
+            if (st == SL_BACKTRACK)
+                worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
+            else if (Bt.mixed && s_jprec[s])
+                worst = eval_row<2>(ec, bus, s, row, pinned, pq, Ssp, fac32, R, true);
+            else
+                worst = eval_row<1>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
             atomicMax(&s_res[s], dbits(worst));
         }
         __syncthreads();
@@ -679,18 +666,28 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
             double nw = bitsd(s_res[s]);
             if (!(nw < BIG)) nw = BIG;
             bool top = false;
+            // Precision votes (mixed only). Reference rule (vote_rule 0, nr_polar_kernels.cu:209-228):
+            // float while the mismatch is above mixed_switch, double below it, and double for
+            // good once a float step fails to halve the mismatch or the line search engages.
+            // GB300 rule (vote_rule 1): float throughout -- the double mismatch keeps the answer
+            // exact and a float step near the solution still contracts by ~cond(J)*2^-24 --
+            // and double for good only when contraction stalls near the solution (a float step
+            // from below mixed_switch that does not halve the mismatch, or needs damping).
             if (st == SL_FRESH) {
                 s_nrm[s] = nw;
-                s_vote[s] = (Bt.mixed && nw > Bt.mixed_switch) ? 1 : 0;
+                s_vote[s] = !Bt.mixed ? 0 : (Bt.vote_rule == 1 ? 1 : (nw > Bt.mixed_switch ? 1 : 0));
                 top = true;
             } else if (st == SL_ACTIVE) {
                 const double old = s_nrm[s];
                 if (!Bt.line_search || nw <= (1.0 - ARMIJO_C) * old) {
                     if (Bt.mixed && s_vote[s] >= 0) {
-                        if (s_vote[s] == 1 && !(nw <= 0.5 * old))
+                        if (Bt.vote_rule == 1) {
+                            if (s_vote[s] == 1 && !(nw <= 0.5 * old) && old < Bt.mixed_switch) s_vote[s] = -1;
+                        } else if (s_vote[s] == 1 && !(nw <= 0.5 * old)) {
                             s_vote[s] = -1;
-                        else
+                        } else {
                             s_vote[s] = nw > Bt.mixed_switch ? 1 : 0;
+                        }
                     }
                     s_nrm[s] = nw;
                     top = true;
@@ -700,7 +697,7 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
                     s_alpha[s] = 0.5;
                     s_trial[s] = 1;
                     s_st[s] = SL_BACKTRACK;
-                    if (Bt.mixed) s_vote[s] = -1;
+                    if (Bt.mixed && (Bt.vote_rule == 0 || old < Bt.mixed_switch)) s_vote[s] = -1;
                 }
             } else if (st == SL_BACKTRACK) {
                 const double a = s_alpha[s];
@@ -761,7 +758,8 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
 
 // Jacobian blocks and residual at one given voltage (G = 1): debug_J and tests.
 __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                                  double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R) {
+                                  double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                                  double2* R) {
     const int n = P.n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double vm = hypot(V[i].x, V[i].y), va = atan2(V[i].y, V[i].x);
@@ -769,14 +767,15 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
         sincos(va, &sn, &cs);
         Vt[i] = make_double4_32a(vm, va, cs, sn);
         Et[i] = make_double2(vm * cs, vm * sn);
-        V32[i] = make_float4((float)vm, (float)cs, (float)sn, 0.f);
+        Ei[i] = 1.0 / vm;
+        V32[i] = make_float4((float)(vm * cs), (float)(vm * sn), (float)(1.0 / vm), 0.f);
     }
     __syncthreads();  // single-CTA launch
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int row = P.row_of_bus[i];
         if (row < 0) continue;
-        EvalCtx ec{&P, Vt, Et, V32, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
-        eval_row_x<true>(ec, i, 0, row, pin && pin[i], P.bus_pq[i] != 0, Sbus[i], blocks, R, true);
+        EvalCtx ec{&P, Et, Ei, V32, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
+        eval_row<1>(ec, i, 0, row, pin && pin[i], P.bus_pq[i] != 0, Sbus[i], blocks, R, true);
     }
 }
 
@@ -787,9 +786,9 @@ cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, in
 }
 
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                              double4_32a* Vt, double2* Et, float4* V32, double4_32a* blocks, double2* R,
-                              cudaStream_t stream) {
-    eval_debug_kernel<<<1, 256, 0, stream>>>(P, V, Sbus, pin, Vt, Et, V32, blocks, R);
+                              double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                              double2* R, cudaStream_t stream) {
+    eval_debug_kernel<<<1, 256, 0, stream>>>(P, V, Sbus, pin, Vt, Et, Ei, V32, blocks, R);
     return cudaGetLastError();
 }
 

@@ -32,6 +32,7 @@ class Params(C.Structure):
         ("check_v0", C.c_int),
         ("pivot_ratio_double", C.c_double),
         ("pivot_ratio_single", C.c_double),
+        ("vote_rule", C.c_int),
     ]
 
 

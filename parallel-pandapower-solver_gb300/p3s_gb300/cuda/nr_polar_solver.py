@@ -35,6 +35,9 @@ class PolarNewtonSolverCUDA:
         self.mem_fraction = 0.6
         self.precision = "double"
         self.mixed_switch = 1e-3
+        # "gb300": float factors until contraction stalls below mixed_switch (default);
+        # "reference": the reference's votes (float above mixed_switch, double below it)
+        self.vote_rule = "gb300"
         self.line_search = True
         self.fallback = "none"
         self.cpu_handoff = 0
@@ -54,7 +57,8 @@ class PolarNewtonSolverCUDA:
     # ------------------------------------------------------------------ helpers
     def _params(self, max_iter, tol):
         return GpuSolver.params(max_iter, tol, self.line_search, self.precision, self.mixed_switch,
-                                pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single)
+                                pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single,
+                                vote_rule=self.vote_rule)
 
     def _record(self, B, r):
         st = self._s.stats
