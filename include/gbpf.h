@@ -35,6 +35,8 @@ typedef struct gbpf_params {
     double pivot_ratio_single; /* the same bound for a float factorization (1e-3) */
     int vote_rule;       /* mixed: 0 = the reference's precision votes (nr_polar_kernels.cu:209-228),
                             1 = float until contraction stalls below mixed_switch */
+    double polish;       /* vote_rule 1: a case on float factors iterates until mismatch < polish * tol,
+                            so its voltage is as accurate as a double solve's (1e-2) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */

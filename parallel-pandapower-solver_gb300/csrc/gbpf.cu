@@ -280,6 +280,7 @@ gbpf_params default_params() {
     p.pivot_ratio_double = 1e-3;
     p.pivot_ratio_single = 1e-3;
     p.vote_rule = 1;
+    p.polish = 1e-2;
     return p;
 }
 
@@ -346,6 +347,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.mixed = p.precision == 1;
     b.mixed_switch = p.mixed_switch;
     b.vote_rule = p.vote_rule;
+    b.polish = p.polish > 0.0 && p.polish <= 1.0 ? p.polish : 1.0;
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;

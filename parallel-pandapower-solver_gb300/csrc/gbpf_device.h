@@ -82,6 +82,7 @@ struct Batch {
     int mixed;               // 0: all factorizations double; 1: vote per case
     double mixed_switch;
     int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
+    double polish;           // GB300 rule: float-factor cases iterate to polish * tol
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch

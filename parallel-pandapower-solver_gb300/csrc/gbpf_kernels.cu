@@ -719,10 +719,16 @@ __global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, c
                 top = true;
             }
             if (top) {  // nr_klu.cpp:590-595 loop head
+                // A case on float factors (GB300 vote rule) keeps stepping until its mismatch
+                // is below polish x tol: a float step lands anywhere below tol, so without the
+                // polish its voltage would only be as close to the exact solution as tol
+                // allows, where the double path's quadratic last step lands far below tol.
+                const bool polish = Bt.mixed && Bt.vote_rule == 1 && s_vote[s] == 1;
+                const double tol_s = polish ? Bt.tol * Bt.polish : Bt.tol;
                 if (s_it[s] >= Bt.max_iter) {
                     s_st[s] = SL_FINISH;
-                    s_conv[s] = 0;
-                } else if (s_nrm[s] < Bt.tol) {
+                    s_conv[s] = polish && s_nrm[s] < Bt.tol;
+                } else if (s_nrm[s] < tol_s) {
                     s_st[s] = SL_FINISH;
                     s_conv[s] = 1;
                 } else if (s_nrm[s] >= BIG) {

@@ -33,6 +33,7 @@ class Params(C.Structure):
         ("pivot_ratio_double", C.c_double),
         ("pivot_ratio_single", C.c_double),
         ("vote_rule", C.c_int),
+        ("polish", C.c_double),
     ]
 
 

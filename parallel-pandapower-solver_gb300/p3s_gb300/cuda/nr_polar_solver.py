@@ -38,6 +38,8 @@ class PolarNewtonSolverCUDA:
         # "gb300": float factors until contraction stalls below mixed_switch (default);
         # "reference": the reference's votes (float above mixed_switch, double below it)
         self.vote_rule = "gb300"
+        # gb300 rule: a case on float factors iterates until its mismatch is below polish * tol
+        self.polish = 1e-2
         self.line_search = True
         self.fallback = "none"
         self.cpu_handoff = 0
@@ -58,7 +60,7 @@ class PolarNewtonSolverCUDA:
     def _params(self, max_iter, tol):
         return GpuSolver.params(max_iter, tol, self.line_search, self.precision, self.mixed_switch,
                                 pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single,
-                                vote_rule=self.vote_rule)
+                                vote_rule=self.vote_rule, polish=self.polish)
 
     def _record(self, B, r):
         st = self._s.stats

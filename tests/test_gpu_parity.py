@@ -149,7 +149,10 @@ def test_nan_admittance_is_never_reported_converged(grid118):
 
 def test_update_Y_equals_rebuilding_the_solver(grid118):
     S = timeseries_injections(grid118, 16)
-    Yx2 = grid118.Yx * (1.0 + 0.03 * np.random.default_rng(4).standard_normal(grid118.nnz))
+    # new branch parameters (every branch's stamp scaled by 1 +- 3%), same pattern
+    st = grid118.stamp * (1.0 + 0.03 * np.random.default_rng(4).standard_normal(grid118.n_branch))[:, None]
+    Yx2 = np.zeros(grid118.nnz, dtype=complex)
+    np.add.at(Yx2, grid118.stamp_pos.ravel(), st.ravel())
     gpu = PolarNewtonSolverCUDA(grid118.Yp, grid118.Yj, grid118.Yx, grid118.pv, grid118.pq)
     before = gpu.solve_batch(S, grid118.V0)["V"]
     gpu.update_Y(Yx2)
