@@ -67,6 +67,10 @@ int gbpf_device_count(void);
  * cases_per_cta: 0 = automatic, else a power of two in 1..32. Returns NULL on error. */
 gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
                          int npv, const int32_t* pq, int npq, int cases_per_cta);
+/* gbpf_create with the CTA shape chosen explicitly: threads_per_cta 512 or 1024 (0 = default). */
+gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz,
+                            const int32_t* pv, int npv, const int32_t* pq, int npq, int cases_per_cta,
+                            int threads_per_cta);
 void gbpf_destroy(gbpf_solver* s);
 
 /* Values-only Ybus refresh. Replaces Solver.update_Y (nr_klu.cpp:999-1011) and

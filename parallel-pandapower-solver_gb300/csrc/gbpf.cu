@@ -144,7 +144,7 @@ int compute_rcond0(gbpf_solver* s) {
     return 0;
 }
 
-int setup(gbpf_solver* s, int cases_per_cta) {
+int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     CK(cudaGetDevice(&s->device));
     CK(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -152,7 +152,8 @@ int setup(gbpf_solver* s, int cases_per_cta) {
     CK(cudaEventCreate(&s->e1));
     CK(cudaEventCreate(&s->c0));
     CK(cudaEventCreate(&s->c1));
-    s->NT = gbpf::newton_max_threads();
+    s->NT = threads_per_cta > 0 ? threads_per_cta : gbpf::newton_max_threads();
+    if (s->NT != 512 && s->NT != 1024) return fail("threads_per_cta must be 512 or 1024");
     int G = cases_per_cta;
     if (G <= 0) {
         // cases per CTA: enough slots to keep the CTA's workers busy on small grids,
@@ -164,7 +165,7 @@ int setup(gbpf_solver* s, int cases_per_cta) {
     s->G = G;
     s->lg = ilog2(G);
     int occ = 1;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(), s->NT, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(s->NT), s->NT, 0));
     s->occ = std::max(1, occ);
     return 0;
 }
@@ -373,6 +374,12 @@ int gbpf_device_count(void) {
 
 gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
                          int npv, const int32_t* pq, int npq, int cases_per_cta) {
+    return gbpf_create_ex(n, Yp, Yj, Yx, nnz, pv, npv, pq, npq, cases_per_cta, 0);
+}
+
+gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz,
+                            const int32_t* pv, int npv, const int32_t* pq, int npq, int cases_per_cta,
+                            int threads_per_cta) {
     if (n <= 0 || !Yp || (nnz > 0 && (!Yj || !Yx)) || npv < 0 || npq < 0) {
         fail("gbpf_create: invalid arguments");
         return nullptr;
@@ -393,7 +400,7 @@ gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const doub
         }
         s->plan.nv = probe.nv;
     }
-    if (setup(s.get(), cases_per_cta)) return nullptr;
+    if (setup(s.get(), cases_per_cta, threads_per_cta)) return nullptr;
     std::string e = gbpf::build_plan(s->plan, n, Yp, Yj, nnz, pv, npv, pq, npq, s->NT / s->G);
     if (!e.empty()) {
         fail("gbpf_create: " + e);

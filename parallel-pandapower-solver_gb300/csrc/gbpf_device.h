@@ -116,6 +116,6 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
                               double2* R, cudaStream_t stream);
 int newton_max_threads();
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
-const void* newton_kernel_ptr();
+const void* newton_kernel_ptr(int threads);
 
 }  // namespace gbpf

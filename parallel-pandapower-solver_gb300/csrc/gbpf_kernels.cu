@@ -27,7 +27,7 @@
 
 namespace gbpf {
 
-#define NT_NEWTON 512
+#define NT_NEWTON 512  // default threads per CTA (1024 also compiled)
 
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
@@ -115,7 +115,7 @@ __device__ __forceinline__ unsigned row_stamp_mask(const EvalCtx& c, int k0, int
 }
 
 __device__ __forceinline__ double2 ybus_val(const EvalCtx& c, int k, unsigned mask) {
-    double2 y = c.ymode == 2 ? c.Yd[(size_t)k * c.sYd + c.ncase] : c.P->Y[k];
+    double2 y = c.ymode == 2 ? c.Yd[(size_t)k * c.sYd + c.ncase] : __ldg(&c.P->Y[k]);
     if (mask) {
         for (int e = 0; e < c.nst; ++e)
             if (((mask >> e) & 1u) && c.stk[e] == k) {
@@ -142,10 +142,10 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
     float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
     if (JM == 2) vi32 = c.V32[si];
     double Ir = 0.0, Ii = 0.0, gii = 0.0, bii = 0.0;
-    const int k0 = P.Yp[i], k1 = P.Yp[i + 1];
+    const int k0 = __ldg(&P.Yp[i]), k1 = __ldg(&P.Yp[i + 1]);
     const unsigned mask = row_stamp_mask(c, k0, k1);
     for (int k = k0; k < k1; ++k) {
-        const int j = P.Yj[k];
+        const int j = __ldg(&P.Yj[k]);
         const double2 y = ybus_val(c, k, mask);
         const size_t sj = ((size_t)j << c.lg) + s;
         const double2 ej = c.Et[sj];
@@ -159,9 +159,9 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
             continue;
         }
         if (JM == 0) continue;
-        const int q = P.posmap[k];
+        const int q = __ldg(&P.posmap[k]);
         if (q < 0) continue;
-        const bool pq_j = P.bus_pq[j] != 0;
+        const bool pq_j = __ldg(&P.bus_pq[j]) != 0;
         const size_t at = ((size_t)q << c.lg) + s;
         if (pinned) {
             put_block(fac, at, 0.0, 0.0, 0.0, 0.0);
@@ -175,7 +175,7 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
         } else {
             float gx, gy;
             if (c.ymode == 0) {
-                const float2 y32 = P.Y32[k];
+                const float2 y32 = __ldg(&P.Y32[k]);
                 gx = y32.x;
                 gy = y32.y;
             } else {
@@ -267,19 +267,32 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     double pmin = DBL_MAX, pmax = 0.0;
     for (int h = 0; h < P.nlev; ++h) {
         if (act) {
-            const int t0 = P.ptrA[h * W + w], t1 = P.ptrA[h * W + w + 1];
+            const int t0 = __ldg(&P.ptrA[h * W + w]), t1 = __ldg(&P.ptrA[h * W + w + 1]);
+            // the next task's record is fetched while the current one runs
+            int4 next = t0 < t1 ? __ldg(&P.taskA[t0]) : make_int4(0, 0, 0, 0);
             for (int t = t0; t < t1; ++t) {
-                const int4 task = P.taskA[t];
+                const int4 task = next;
+                if (t + 1 < t1) next = __ldg(&P.taskA[t + 1]);
                 const int kind = task.y & 3;
                 if (kind == 3) {  // forward substitution of block row task.x
                     const double2 r = R[((size_t)task.x << lg) + s];
                     real y0 = (real)r.x, y1 = (real)r.y;
-                    for (int p = task.z; p < task.w; ++p) {
-                        const int2 pr = P.pairs[p];
-                        const B4 l = fac[((size_t)pr.x << lg) + s];
-                        const B2 ys = y[((size_t)pr.y << lg) + s];
-                        y0 -= l.x * ys.x + l.y * ys.y;
-                        y1 -= l.z * ys.x + l.w * ys.y;
+                    int p = task.z;
+                    for (; p + 1 < task.w; p += 2) {
+                        const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                        const B4 l0 = fac[((size_t)q0.x << lg) + s], l1 = fac[((size_t)q1.x << lg) + s];
+                        const B2 u0 = y[((size_t)q0.y << lg) + s], u1 = y[((size_t)q1.y << lg) + s];
+                        y0 -= l0.x * u0.x + l0.y * u0.y;
+                        y1 -= l0.z * u0.x + l0.w * u0.y;
+                        y0 -= l1.x * u1.x + l1.y * u1.y;
+                        y1 -= l1.z * u1.x + l1.w * u1.y;
+                    }
+                    if (p < task.w) {
+                        const int2 q0 = __ldg(&P.pairs[p]);
+                        const B4 l0 = fac[((size_t)q0.x << lg) + s];
+                        const B2 u0 = y[((size_t)q0.y << lg) + s];
+                        y0 -= l0.x * u0.x + l0.y * u0.y;
+                        y1 -= l0.z * u0.x + l0.w * u0.y;
                     }
                     B2 o;
                     o.x = y0;
@@ -288,11 +301,17 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     continue;
                 }
                 B4 acc = (task.y & 16) ? z4<B4>() : fac[((size_t)task.x << lg) + s];
-                for (int p = task.z; p < task.w; ++p) {
-                    const int2 pr = P.pairs[p];
-                    const B4 a = fac[((size_t)pr.x << lg) + s];
-                    const B4 b = fac[((size_t)pr.y << lg) + s];
-                    mm_sub(acc, a, b);
+                int p = task.z;
+                for (; p + 1 < task.w; p += 2) {
+                    const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                    const B4 a0 = fac[((size_t)q0.x << lg) + s], b0 = fac[((size_t)q0.y << lg) + s];
+                    const B4 a1 = fac[((size_t)q1.x << lg) + s], b1 = fac[((size_t)q1.y << lg) + s];
+                    mm_sub(acc, a0, b0);
+                    mm_sub(acc, a1, b1);
+                }
+                if (p < task.w) {
+                    const int2 q0 = __ldg(&P.pairs[p]);
+                    mm_sub(acc, fac[((size_t)q0.x << lg) + s], fac[((size_t)q0.y << lg) + s]);
                 }
                 if (kind == 0) {
                     const real det = acc.x * acc.w - acc.y * acc.z;
@@ -318,9 +337,9 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
         }
         __syncthreads();
         if (act) {
-            const int t0 = P.ptrB[h * W + w], t1 = P.ptrB[h * W + w + 1];
+            const int t0 = __ldg(&P.ptrB[h * W + w]), t1 = __ldg(&P.ptrB[h * W + w + 1]);
             for (int t = t0; t < t1; ++t) {
-                const int2 sc = P.scl[t];
+                const int2 sc = __ldg(&P.scl[t]);
                 const B4 l = fac[((size_t)sc.x << lg) + s];
                 const B4 d = fac[((size_t)sc.y << lg) + s];
                 B4 o;
@@ -335,17 +354,29 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     }
     for (int h = 0; h < P.nblev; ++h) {
         if (act) {
-            const int t0 = P.ptrC[h * W + w], t1 = P.ptrC[h * W + w + 1];
+            const int t0 = __ldg(&P.ptrC[h * W + w]), t1 = __ldg(&P.ptrC[h * W + w + 1]);
+            int4 next = t0 < t1 ? __ldg(&P.taskC[t0]) : make_int4(0, 0, 0, 0);
             for (int t = t0; t < t1; ++t) {
-                const int4 task = P.taskC[t];
+                const int4 task = next;
+                if (t + 1 < t1) next = __ldg(&P.taskC[t + 1]);
                 const B2 yr = y[((size_t)task.x << lg) + s];
                 real r0 = yr.x, r1 = yr.y;
-                for (int p = task.z; p < task.w; ++p) {
-                    const int2 pr = P.pairs[p];
-                    const B4 u = fac[((size_t)pr.x << lg) + s];
-                    const B2 yj = y[((size_t)pr.y << lg) + s];
-                    r0 -= u.x * yj.x + u.y * yj.y;
-                    r1 -= u.z * yj.x + u.w * yj.y;
+                int p = task.z;
+                for (; p + 1 < task.w; p += 2) {
+                    const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                    const B4 u0 = fac[((size_t)q0.x << lg) + s], u1 = fac[((size_t)q1.x << lg) + s];
+                    const B2 y0 = y[((size_t)q0.y << lg) + s], y1 = y[((size_t)q1.y << lg) + s];
+                    r0 -= u0.x * y0.x + u0.y * y0.y;
+                    r1 -= u0.z * y0.x + u0.w * y0.y;
+                    r0 -= u1.x * y1.x + u1.y * y1.y;
+                    r1 -= u1.z * y1.x + u1.w * y1.y;
+                }
+                if (p < task.w) {
+                    const int2 q0 = __ldg(&P.pairs[p]);
+                    const B4 u0 = fac[((size_t)q0.x << lg) + s];
+                    const B2 y0 = y[((size_t)q0.y << lg) + s];
+                    r0 -= u0.x * y0.x + u0.y * y0.y;
+                    r1 -= u0.z * y0.x + u0.w * y0.y;
                 }
                 const B4 d = fac[((size_t)task.y << lg) + s];
                 B2 o;
@@ -370,7 +401,8 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 }
 
 // ------------------------------------------------------------------------- the kernel
-__global__ void __launch_bounds__(NT_NEWTON, 1) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
+template <int NTB>
+__global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
     const int G = Sc.G, lg = Sc.log2G;
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
@@ -787,7 +819,12 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
 
 cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
                           cudaStream_t stream) {
-    newton_kernel<<<grid, threads, 0, stream>>>(P, B, S);
+    if (threads == 1024)
+        newton_kernel<1024><<<grid, 1024, 0, stream>>>(P, B, S);
+    else if (threads == 512)
+        newton_kernel<512><<<grid, 512, 0, stream>>>(P, B, S);
+    else
+        return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
@@ -800,6 +837,8 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
 
 int newton_max_threads() { return NT_NEWTON; }
 
-const void* newton_kernel_ptr() { return (const void*)newton_kernel; }
+const void* newton_kernel_ptr(int threads) {
+    return threads == 1024 ? (const void*)newton_kernel<1024> : (const void*)newton_kernel<512>;
+}
 
 }  // namespace gbpf

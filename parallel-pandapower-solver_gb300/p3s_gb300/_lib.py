@@ -75,6 +75,7 @@ SIGNATURES = {
     "gbpf_version": (C.c_int, []),
     "gbpf_device_count": (C.c_int, []),
     "gbpf_create": (_vp, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int]),
+    "gbpf_create_ex": (_vp, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int, C.c_int]),
     "gbpf_destroy": (None, [_vp]),
     "gbpf_update_Y": (C.c_int, [_vp, _dp, C.c_int]),
     "gbpf_get_info": (C.c_int, [_vp, C.POINTER(Info)]),

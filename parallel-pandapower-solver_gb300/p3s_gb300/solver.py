@@ -54,7 +54,7 @@ def pinned_empty(shape, dtype) -> np.ndarray:
 class GpuSolver:
     """One grid topology resident on the device."""
 
-    def __init__(self, Yp, Yj, Yx, pv, pq, cases_per_cta: int = 0):
+    def __init__(self, Yp, Yj, Yx, pv, pq, cases_per_cta: int = 0, threads_per_cta: int = 0):
         L = _lib.require_device()
         self.Yp = np.ascontiguousarray(Yp, dtype=np.int32)
         self.Yj = np.ascontiguousarray(Yj, dtype=np.int32)
@@ -65,8 +65,9 @@ class GpuSolver:
         self.nnz = len(self.Yj)
         if self.Yx.shape != (self.nnz,):
             raise ValueError("Yx must have one value per Ybus nonzero")
-        h = L.gbpf_create(self.n, _lib.i32(self.Yp), _lib.i32(self.Yj), _lib.cview(self.Yx), self.nnz,
-                          _lib.i32(self.pv), len(self.pv), _lib.i32(self.pq), len(self.pq), int(cases_per_cta))
+        h = L.gbpf_create_ex(self.n, _lib.i32(self.Yp), _lib.i32(self.Yj), _lib.cview(self.Yx), self.nnz,
+                             _lib.i32(self.pv), len(self.pv), _lib.i32(self.pq), len(self.pq), int(cases_per_cta),
+                             int(threads_per_cta))
         if not h:
             raise RuntimeError(_lib.last_error())
         self._h = h
