@@ -82,14 +82,25 @@ def reduce_max(x: float, world: int) -> float:
 
 # ----------------------------------------------------------------------------- workload
 def workload(rank: int = 0, hours: int = HOURS):
-    from p3s_gb300.synthetic import grid_2000, lanes, timeseries_injections
+    from p3s_gb300.synthetic import grid_2000, timeseries_injections
 
     g = grid_2000(0)
     S = timeseries_injections(g, hours, seed=1 + rank)
     return g, S
 
 
-def n_lanes(g, cases_per_cta=8):
+def shared_start(g):
+    """The lanes' shared start voltage: the converged base case (solved once by the CPU
+    oracle, outside any timed region) -- the role the reference's DC start plays for its
+    time series (p3s/timeseries.py:200-244)."""
+    from oracle import cpu
+
+    r = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(g.Sbus[:, None], g.V0)
+    assert r["converged"][0]
+    return np.ascontiguousarray(r["V"][:, 0])
+
+
+def n_lanes(g, cases_per_cta=32):
     import torch
 
     nsm = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
@@ -196,6 +207,7 @@ def run_gpu(args, rank, world, local):
     torch.cuda.set_device(local)
     _lib.require_device()
     g, S = workload(rank, args.hours)
+    V0 = shared_start(g)
     T = S.shape[1]
     solver = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     info = solver.info
@@ -203,7 +215,7 @@ def run_gpu(args, rank, world, local):
     off = lanes(T, K).astype(np.int64)
     dev = torch.device("cuda", local)
     dS = torch.from_numpy(S.view(np.float64).copy()).to(dev)
-    dV0 = torch.from_numpy(g.V0.view(np.float64).copy()).to(dev)
+    dV0 = torch.from_numpy(V0.view(np.float64).copy()).to(dev)
     doff = torch.from_numpy(off).to(dev)
     dV = torch.empty(2 * g.n * T, dtype=torch.float64, device=dev)
     dit = torch.empty(T, dtype=torch.int32, device=dev)
@@ -250,8 +262,8 @@ def run_gpu(args, rank, world, local):
     # end to end through the public API, pinned host buffers
     Sh = pinned_empty(S.shape, np.complex128)
     Sh[...] = S
-    V0h = pinned_empty(g.V0.shape, np.complex128)
-    V0h[...] = g.V0
+    V0h = pinned_empty(V0.shape, np.complex128)
+    V0h[...] = V0
     Vh = pinned_empty((g.n, T), np.complex128)
     ith = pinned_empty((T,), np.int32)
     cvh = pinned_empty((T,), np.uint8)
@@ -264,7 +276,7 @@ def run_gpu(args, rank, world, local):
         solver.solve_lanes(Sh, V0h, off, p, out=(Vh, ith, cvh))
         e2e_ms.append(solver.stats["call_ms"])
     barrier(world)
-    h2d = S.nbytes + g.V0.nbytes + off.nbytes
+    h2d = S.nbytes + V0.nbytes + off.nbytes
     d2h = Vh.nbytes + ith.nbytes + cvh.nbytes
 
     res = dict(out=out, e2e_ms=float(np.mean(e2e_ms)), h2d=h2d, d2h=d2h, info=info, K=len(off) - 1, T=T,
@@ -313,7 +325,7 @@ def gpu_line(args, res, rank, world):
                                / (dbl["ms"] * 1e-3) / 1e9, 1),
         "clocks": dbl["clocks"],
     }
-    cb = cpu_baseline(res["g"], args)
+    cb = cpu_baseline(res["g"], args, res["K"])
     line = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -329,7 +341,8 @@ def gpu_line(args, res, rank, world):
         "data": "synthetic (seeded 2,000-bus grid and 8,760-hour load/generation series)",
         "config": {
             "workload": f"2,000-bus grid x {T} hourly cases, warm-start lanes K={res['K']} "
-                        f"(hour h of a lane starts from hour h-1's converged voltage)",
+                        f"(hour h of a lane starts from hour h-1's converged voltage; a lane's first hour "
+                        f"from the converged base case)",
             "n_bus": g.n, "n_branch": g.n_branch, "n_pv": len(g.pv), "n_pq": len(g.pq), "hours": T,
             "lanes": res["K"], "tol_pu": 1e-8, "max_iter": 30, "precision": "mixed",
             "mixed_switch": args.mixed_switch,
@@ -354,14 +367,14 @@ def gpu_line(args, res, rank, world):
 
 
 # ----------------------------------------------------------------------------- CPU arms
-def cpu_solve(g, S, K):
+def cpu_solve(g, S, K, V0):
     from oracle import cpu
     from p3s_gb300.synthetic import lanes
 
     s = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     off = lanes(S.shape[1], K)
     t0 = time.perf_counter()
-    r = cpu.solve_lanes(s, S, g.V0, off)
+    r = cpu.solve_lanes(s, S, V0, off)
     return time.perf_counter() - t0, r
 
 
@@ -372,7 +385,7 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def cpu_baseline(g, args):
+def cpu_baseline(g, args, lanes_used):
     """The oracle (restated nr_klu, OpenMP over all usable cores) on a bounded sample of the
     same workload: the first `cpu_hours` hours in the same lane structure, best of 3."""
     from oracle.build import build_oracle
@@ -380,8 +393,9 @@ def cpu_baseline(g, args):
     build_oracle()
     hours = min(args.cpu_hours, HOURS)
     _, S = workload(0, hours)
-    K = max(1, round(hours * (args.lanes or 1216) / HOURS))
-    best = min(cpu_solve(g, S, K)[0] for _ in range(3))
+    K = max(1, round(hours * lanes_used / HOURS))
+    V0 = shared_start(g)
+    best = min(cpu_solve(g, S, K, V0)[0] for _ in range(3))
     return {"value": round(hours / best, 1), "unit": "solves/s", "cores": cpu_cores(), "kind": "port",
             "sample": f"first {hours} of the {HOURS} hours, {K} warm-start lanes, best of 3, oracle/liboracle.so "
                       f"(OpenMP, {cpu_cores()} threads)"}
@@ -397,10 +411,11 @@ def run_reference(args, rank, world):
     g = grid_2000(0)
     hours = min(args.cpu_hours, HOURS)
     _, S = workload(0, hours)
-    K = max(1, round(hours * (args.lanes or 1216) / HOURS))
+    K = max(1, round(hours * (args.lanes or 152 * 32) / HOURS))
+    V0 = shared_start(g)
     for _ in range(args.warmup):
-        cpu_solve(g, S, K)
-    times = [cpu_solve(g, S, K)[0] for _ in range(args.steps)]
+        cpu_solve(g, S, K, V0)
+    times = [cpu_solve(g, S, K, V0)[0] for _ in range(args.steps)]
     ms = float(np.mean(times)) * 1e3
     value = hours / (ms * 1e-3)
     line = {

@@ -152,14 +152,16 @@ int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     CK(cudaEventCreate(&s->e1));
     CK(cudaEventCreate(&s->c0));
     CK(cudaEventCreate(&s->c1));
-    s->NT = threads_per_cta > 0 ? threads_per_cta : gbpf::newton_max_threads();
+    s->NT = threads_per_cta > 0 ? threads_per_cta : 1024;
     if (s->NT != 512 && s->NT != 1024) return fail("threads_per_cta must be 512 or 1024");
     int G = cases_per_cta;
     if (G <= 0) {
         // cases per CTA: enough slots to keep the CTA's workers busy on small grids,
         // few enough that the per-CTA working set of large grids stays L2-friendly
+        // (measured on GB300, 2,000-bus grid: 32 slots x 1024 threads is fastest; larger
+        // grids get fewer slots so the per-CTA working set stays bounded)
         const int nv = std::max(1, (int)s->plan.nv);
-        G = nv <= 160 ? 32 : (nv <= 640 ? 16 : 8);
+        G = nv <= 4096 ? 32 : (nv <= 16384 ? 16 : 8);
     }
     if (G < 1 || G > gbpf::MAX_SLOTS || (G & (G - 1))) return fail("cases_per_cta must be a power of two in 1..32");
     s->G = G;
@@ -281,7 +283,7 @@ gbpf_params default_params() {
     p.pivot_ratio_double = 1e-3;
     p.pivot_ratio_single = 1e-3;
     p.vote_rule = 1;
-    p.polish = 1e-2;
+    p.polish = 1e-3;
     return p;
 }
 

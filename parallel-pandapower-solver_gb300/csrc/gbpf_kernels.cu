@@ -27,7 +27,7 @@
 
 namespace gbpf {
 
-#define NT_NEWTON 512  // default threads per CTA (1024 also compiled)
+#define NT_NEWTON 512  // threads per CTA of the smaller variant (1024 also compiled, the default)
 
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
