@@ -36,7 +36,7 @@ typedef struct gbpf_params {
     int vote_rule;       /* mixed: 0 = the reference's precision votes (nr_polar_kernels.cu:209-228),
                             1 = float until contraction stalls below mixed_switch */
     double polish;       /* vote_rule 1: a case on float factors iterates until mismatch < polish * tol,
-                            so its voltage is as accurate as a double solve's (1e-3) */
+                            so its voltage is as accurate as a double solve's (1e-4) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -123,6 +123,11 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
                        double* residual);
 /* Block row of each bus (-1 for slack), length n. */
 int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
+
+/* Device check of the kernels' integer-pipe float/double conversions: d2f[i] = in[i]
+ * converted to float (round toward zero), f2d[i] = d2f[i] converted back to double. No
+ * reference counterpart (a GB300-specific helper). */
+int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d);
 
 /* Page-locked host memory for fast transfers. */
 void* gbpf_host_alloc(size_t bytes);

@@ -94,13 +94,13 @@ struct gbpf_solver {
     size_t sc_ctas = 0;
     bool sc_mixed = false;
     // per-call buffers (grow-only)
-    DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin;
+    DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab;
     gbpf_stats last{};
     ~gbpf_solver() {
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dtaskA, &dptrA, &dscl, &dptrB,
                         &dtaskC, &dptrC, &dpairs, &drow_pq, &dbus_of_row, &ddpos, &fac64, &fac32, &R, &y64, &y32,
                         &Vc, &Vt, &Et, &Ei, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
-                        &bYd, &bpin})
+                        &bYd, &bpin, &btab})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -283,7 +283,7 @@ gbpf_params default_params() {
     p.pivot_ratio_double = 1e-3;
     p.pivot_ratio_single = 1e-3;
     p.vote_rule = 1;
-    p.polish = 1e-3;
+    p.polish = 1e-4;
     return p;
 }
 
@@ -308,6 +308,11 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     b.err = reinterpret_cast<int*>(ctl + 24);
     gbpf::Scratch sc = scratch_view(s);
     CK(cudaEventRecord(s->e0, s->stream));
+    if (b.v0_shared) {
+        CK(s->btab.ensure((size_t)s->n * 64));
+        b.v0tab = s->btab.as<double4_32a>();
+        CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, s->btab.as<double4_32a>(), b.err, s->stream));
+    }
     CK(gbpf::launch_newton(s->dp, b, sc, grid, s->NT, s->stream));
     CK(cudaEventRecord(s->e1, s->stream));
     unsigned long long host_ctl[32];
@@ -668,6 +673,23 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpy(blocks, dblk.p, nb * 32, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(residual, dR.p, (size_t)s->plan.nv * 16, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d) {
+    if (n <= 0) return 0;
+    DBuf a, b, c;
+    CK(a.ensure((size_t)n * 8));
+    CK(b.ensure((size_t)n * 4));
+    CK(c.ensure((size_t)n * 8));
+    CK(cudaMemcpy(a.p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
+    CK(gbpf::launch_conversions(a.as<double>(), n, b.as<float>(), c.as<double>()));
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpy(d2f, b.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f2d, c.p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    a.release();
+    b.release();
+    c.release();
     return 0;
 }
 

@@ -63,6 +63,7 @@ struct Batch {
     const double2* V0;       // start voltage: V0[bus * sV0 + case] or V0[bus] if shared
     int v0_shared;
     long long sV0;
+    const double4_32a* v0tab; // shared start: per bus (Vm, Va, cos, sin), (e, f, 1/Vm, 0)
     int check_v0;            // validate V0 like nr_klu's solve_batch
     int ymode;               // 0 base Ybus, 1 base minus per-case stamps, 2 dense per case
     const int* st_ptr;       // stamps of case c: [st_ptr[c], st_ptr[c+1])
@@ -114,6 +115,8 @@ cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, in
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
                               double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
                               double2* R, cudaStream_t stream);
+cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
+cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d);
 int newton_max_threads();
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
 const void* newton_kernel_ptr(int threads);

@@ -39,18 +39,63 @@ __device__ __forceinline__ bool finite_d(double x) {
     return (dbits(x) & 0x7ff0000000000000ULL) != 0x7ff0000000000000ULL;
 }
 
+// ---- float <-> double conversions on the integer pipes. GB300 runs double-precision
+// instructions, conversions included, at 1/64 of the float rate; the float Jacobian / LU
+// path converts a handful of values per bus and step, so these are done by IEEE-754 bit
+// manipulation instead. float -> double is exact (float subnormals flush to zero);
+// double -> float truncates the mantissa (round toward zero, within one float ulp),
+// flushes magnitudes below 2^-126 to zero and saturates above the float range to infinity.
+__device__ __forceinline__ float d2f_fast(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned de = (hi >> 20) & 0x7ffu;
+    const int ex = (int)de - 1023 + 127;
+    unsigned bits;
+    if (de == 0x7ffu)
+        bits = sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u);  // Inf / NaN
+    else if (ex <= 0)
+        bits = sign;
+    else if (ex >= 255)
+        bits = sign | 0x7f800000u;
+    else
+        bits = sign | ((unsigned)ex << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(bits);
+}
+
+__device__ __forceinline__ double f2d_fast(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u;
+    const unsigned ex = (b >> 23) & 0xffu;
+    const unsigned man = b & 0x7fffffu;
+    unsigned hi, lo = 0;
+    if (ex == 0)
+        hi = sign;
+    else if (ex == 0xffu)
+        hi = sign | 0x7ff00000u | (man ? 0x80000u : 0u);
+    else {
+        hi = sign | ((ex + 896u) << 20) | (man >> 3);
+        lo = man << 29;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// |x| as ordered bits (sign cleared): compares like the magnitudes, NaN above everything
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+
 // cos/sin of a small angle |d| <= 1/4 from their Maclaurin series (Horner in d^2), with as
 // many terms as |d| needs (the first dropped term stays below double rounding); the
 // truncation error is below 3e-18 on the whole range. Used to ROTATE a bus phasor by the
 // Newton angle increment instead of evaluating sincos of the full angle.
-__device__ __forceinline__ void sincos_small(double d, double ad, double* s, double* c) {
+__device__ __forceinline__ void sincos_small(double d, unsigned ahi, double* s, double* c) {
     const double z = d * d;
-    if (ad <= 0x1p-14) {  // next terms below 2^-100: d^5/120 and d^4/24
+    if (ahi < 0x3F100000u) {  // |d| < 2^-14  // next terms below 2^-100: d^5/120 and d^4/24
         *s = fma(z * (-1.0 / 6.0), d, d);
         *c = fma(z, -0.5, 1.0);
         return;
     }
-    if (ad <= 0x1p-6) {  // next terms below 2^-60 relative: d^9/9! and d^8/8!
+    if (ahi < 0x3F900000u) {  // |d| < 2^-6: next terms below 2^-60 relative: d^9/9! and d^8/8!
         double ps = -1.0 / 5040.0;
         ps = fma(ps, z, 1.0 / 120.0);
         ps = fma(ps, z, -1.0 / 6.0);
@@ -134,14 +179,15 @@ __device__ __forceinline__ void put_block(float4* fac, size_t at, double a, doub
 }
 
 template <int JM, typename FacT>
-__device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp, FacT* fac,
-                           double2* R, bool write_r) {
+__device__ unsigned long long eval_row(const EvalCtx& c, int i, int s, int row, bool pinned, bool pq_i, double2 Ssp,
+                                       FacT* fac, double2* R, bool write_r) {
     const DevPlan& P = *c.P;
     const size_t si = ((size_t)i << c.lg) + s;
     const double2 ei = c.Et[si];
     float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
     if (JM == 2) vi32 = c.V32[si];
     double Ir = 0.0, Ii = 0.0, gii = 0.0, bii = 0.0;
+    float gii32 = 0.f, bii32 = 0.f;
     const int k0 = __ldg(&P.Yp[i]), k1 = __ldg(&P.Yp[i + 1]);
     const unsigned mask = row_stamp_mask(c, k0, k1);
     for (int k = k0; k < k1; ++k) {
@@ -156,6 +202,16 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
         if (j == i) {
             gii = y.x;
             bii = y.y;
+            if (JM == 2) {
+                if (c.ymode == 0) {
+                    const float2 y32 = __ldg(&P.Y32[k]);
+                    gii32 = y32.x;
+                    bii32 = y32.y;
+                } else {
+                    gii32 = d2f_fast(y.x);
+                    bii32 = d2f_fast(y.y);
+                }
+            }
             continue;
         }
         if (JM == 0) continue;
@@ -179,8 +235,8 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
                 gx = y32.x;
                 gy = y32.y;
             } else {
-                gx = (float)y.x;
-                gy = (float)y.y;
+                gx = d2f_fast(y.x);
+                gy = d2f_fast(y.y);
             }
             const float4 vj = c.V32[sj];
             const float wr = fmaf(-gy, vj.y, gx * vj.x), wi = fmaf(gy, vj.x, gx * vj.y);
@@ -191,23 +247,36 @@ __device__ double eval_row(const EvalCtx& c, int i, int s, int row, bool pinned,
     }
     const double Pc = fma(ei.x, Ir, ei.y * Ii);
     const double Qc = fma(ei.y, Ir, -ei.x * Ii);
-    if (JM != 0) {
+    if (JM == 1) {
         const size_t at = ((size_t)P.dpos[row] << c.lg) + s;
         if (pinned) {
             put_block(fac, at, 1.0, 0.0, 0.0, 1.0);
         } else {
             const double vi2 = fma(ei.x, ei.x, ei.y * ei.y);
             const double Ps = vi2 * gii, Qs = -vi2 * bii;
-            const double ivi = JM == 1 ? c.Ei[si] : (double)vi32.z;
+            const double ivi = c.Ei[si];
             put_block(fac, at, Qs - Qc, pq_i ? (Pc + Ps) * ivi : 0.0, pq_i ? Pc - Ps : 0.0,
                       pq_i ? (Qc + Qs) * ivi : 1.0);
         }
+    } else if (JM == 2) {  // float diagonal block from float copies: no double arithmetic
+        const size_t at = ((size_t)P.dpos[row] << c.lg) + s;
+        float4 o;
+        if (pinned) {
+            o = make_float4(1.f, 0.f, 0.f, 1.f);
+        } else {
+            const float P32 = d2f_fast(Pc), Q32 = d2f_fast(Qc);
+            const float vi2 = fmaf(vi32.x, vi32.x, vi32.y * vi32.y);
+            const float Ps = vi2 * gii32, Qs = -vi2 * bii32;
+            o = make_float4(Qs - Q32, pq_i ? (P32 + Ps) * vi32.z : 0.f, pq_i ? P32 - Ps : 0.f,
+                            pq_i ? (Q32 + Qs) * vi32.z : 1.f);
+        }
+        reinterpret_cast<float4*>(fac)[at] = o;
     }
     const double rp = pinned ? 0.0 : Ssp.x - Pc;
     const double rq = (pinned || !pq_i) ? 0.0 : Ssp.y - Qc;
     if (write_r) R[((size_t)row << c.lg) + s] = make_double2(rp, rq);
-    const double a = fabs(rp), b = fabs(rq);
-    return (b > a || b != b) ? b : a;
+    const unsigned long long a = abs_bits(rp), b = abs_bits(rq);
+    return b > a ? b : a;
 }
 
 // Reciprocal of a positive double: float seed refined by two Newton-Raphson steps
@@ -264,7 +333,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     const int w = (tid >> 5) * (32 >> lg) + (lane >> lg);
     const int W = P.W;
     const bool act = on[s] != 0;
-    double pmin = DBL_MAX, pmax = 0.0;
+    real pmin = sizeof(real) == 4 ? (real)FLT_MAX : (real)DBL_MAX, pmax = 0;
     for (int h = 0; h < P.nlev; ++h) {
         if (act) {
             const int t0 = __ldg(&P.ptrA[h * W + w]), t1 = __ldg(&P.ptrA[h * W + w + 1]);
@@ -276,7 +345,14 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                 const int kind = task.y & 3;
                 if (kind == 3) {  // forward substitution of block row task.x
                     const double2 r = R[((size_t)task.x << lg) + s];
-                    real y0 = (real)r.x, y1 = (real)r.y;
+                    real y0, y1;
+                    if constexpr (sizeof(real) == 4) {
+                        y0 = d2f_fast(r.x);
+                        y1 = d2f_fast(r.y);
+                    } else {
+                        y0 = r.x;
+                        y1 = r.y;
+                    }
                     int p = task.z;
                     for (; p + 1 < task.w; p += 2) {
                         const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
@@ -313,13 +389,13 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     const int2 q0 = __ldg(&P.pairs[p]);
                     mm_sub(acc, fac[((size_t)q0.x << lg) + s], fac[((size_t)q0.y << lg) + s]);
                 }
-                if (kind == 0) {
+                if (kind == 0) {  // pivots of the 2x2 diagonal block: a00 and det / a00
                     const real det = acc.x * acc.w - acc.y * acc.z;
-                    const double u0 = fabs((double)acc.x);
+                    const real u0 = fabs(acc.x);
                     pmin = fmin(pmin, u0);
                     pmax = (u0 > pmax || u0 != u0) ? u0 : pmax;
                     if (task.y & 32) {
-                        const double u1 = fabs((double)det / (double)acc.x);
+                        const real u1 = fabs(det / acc.x);
                         pmin = fmin(pmin, u1);
                         pmax = (u1 > pmax || u1 != u1) ? u1 : pmax;
                     }
@@ -388,8 +464,16 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
         __syncthreads();
     }
     if (act) {
-        atomicMin(&smin[s], dbits(pmin));
-        atomicMax(&smax[s], dbits(pmax));
+        double dmin, dmax;
+        if constexpr (sizeof(real) == 4) {
+            dmin = f2d_fast((float)pmin);
+            dmax = f2d_fast((float)pmax);
+        } else {
+            dmin = pmin;
+            dmax = pmax;
+        }
+        atomicMin(&smin[s], dbits(dmin));
+        atomicMax(&smax[s], dbits(dmax));
     }
     __syncthreads();
 }
@@ -505,37 +589,43 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
             if (s_st[s] != SL_FRESH) continue;
             const int bus = idx >> lg;
             const int c = s_case[s];
-            double vm, va;
             if (s_warm[s]) {
-                const double4_32a v = Vt[idx];
-                vm = v.x;
-                va = v.y;
+                // previous hour of the lane converged here: its state is the start point
+                Vc[idx] = Vt[idx];
+            } else if (Bt.v0_shared) {
+                // shared start: the state table built once per launch (v0_table_kernel)
+                const double4_32a t0 = Bt.v0tab[2 * bus], t1 = Bt.v0tab[2 * bus + 1];
+                Vc[idx] = t0;
+                Vt[idx] = t0;
+                Et[idx] = make_double2(t1.x, t1.y);
+                Ei[idx] = t1.z;
+                V32[idx] = make_float4(d2f_fast(t1.x), d2f_fast(t1.y), d2f_fast(t1.z), 0.f);
             } else {
-                const double2 v0 = Bt.v0_shared ? Bt.V0[bus] : Bt.V0[(size_t)bus * Bt.sV0 + c];
+                const double2 v0 = Bt.V0[(size_t)bus * Bt.sV0 + c];
                 if (Bt.check_v0 && (!finite_d(v0.x) || !finite_d(v0.y))) {
                     if (atomicCAS(&Bt.err[0], 0, DE_V0_NONFINITE) == 0) {
                         Bt.err[1] = bus;
                         Bt.err[2] = c;
                     }
                 }
-                vm = hypot(v0.x, v0.y);
-                va = atan2(v0.y, v0.x);
+                const double vm = hypot(v0.x, v0.y);
+                const double va = atan2(v0.y, v0.x);
                 if (Bt.check_v0 && (vm <= 0.0 || vm > 10.0) && finite_d(vm)) {
                     if (atomicCAS(&Bt.err[0], 0, DE_V0_MAGNITUDE) == 0) {
                         Bt.err[1] = bus;
                         Bt.err[2] = c;
                     }
                 }
+                double sn, cs;
+                sincos(va, &sn, &cs);
+                const double4_32a v = make_double4_32a(vm, va, cs, sn);
+                Vc[idx] = v;
+                Vt[idx] = v;
+                const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
+                Et[idx] = make_double2(e, f);
+                Ei[idx] = iv;
+                V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), d2f_fast(iv), 0.f);
             }
-            double sn, cs;
-            sincos(va, &sn, &cs);
-            const double4_32a v = make_double4_32a(vm, va, cs, sn);
-            Vc[idx] = v;
-            Vt[idx] = v;
-            const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
-            Et[idx] = make_double2(e, f);
-            Ei[idx] = iv;
-            V32[idx] = make_float4((float)e, (float)f, (float)iv, 0.f);
             spin[idx] = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
         }
 
@@ -611,37 +701,36 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
             const int bus = idx >> lg;
             const int row = P.row_of_bus[bus];
             if (row < 0) continue;
+            const bool active = st == SL_ACTIVE;
             double4_32a vc;
-            double a;
-            if (st == SL_ACTIVE) {  // the point evaluated last was accepted: commit it
+            if (active) {  // the point evaluated last was accepted: commit it
                 vc = Vt[idx];
                 Vc[idx] = vc;
-                a = 1.0;
             } else {
                 vc = Vc[idx];
-                a = s_alpha[s];
             }
             double dth, dvm;
             if (s_yprec[s]) {
-                const float2 d = y32[((size_t)row << lg) + s];
-                dth = d.x;
-                dvm = d.y;
+                const float2 dd = y32[((size_t)row << lg) + s];
+                dth = f2d_fast(dd.x);
+                dvm = f2d_fast(dd.y);
             } else {
-                const double2 d = y64[((size_t)row << lg) + s];
-                dth = d.x;
-                dvm = d.y;
+                const double2 dd = y64[((size_t)row << lg) + s];
+                dth = dd.x;
+                dvm = dd.y;
             }
-            const double va = vc.y + a * dth;  // nr_klu.cpp:665-669 (form_trial)
-            const bool pq = P.bus_pq[bus] != 0;
-            const double vm = pq ? vc.x + a * dvm : vc.x;
+            // trial point (nr_klu.cpp:665-669 form_trial): committed + alpha * step
+            const double d = active ? dth : s_alpha[s] * dth;
+            const double va = vc.y + d;
+            const bool pq = __ldg(&P.bus_pq[bus]) != 0;
+            const double vm = !pq ? vc.x : (active ? vc.x + dvm : fma(s_alpha[s], dvm, vc.x));
             double cs, sn;
-            const double d = a * dth;
-            const double ad = fabs(d);
-            if (ad <= 0.25) {  // rotate the committed phasor by d
+            const unsigned ahi = (unsigned)__double2hiint(d) & 0x7fffffffu;
+            if (ahi < 0x3FD00000u) {  // |d| < 1/4: rotate the committed phasor by d
                 double sd, cd;
-                sincos_small(d, ad, &sd, &cd);
-                cs = vc.z * cd - vc.w * sd;
-                sn = vc.w * cd + vc.z * sd;
+                sincos_small(d, ahi, &sd, &cd);
+                cs = fma(vc.z, cd, -vc.w * sd);
+                sn = fma(vc.w, cd, vc.z * sd);
             } else {
                 sincos(va, &sn, &cs);
             }
@@ -654,11 +743,11 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
             } else if (!Bt.mixed || s_vote[s] != 1) {  // the next Jacobian is double
                 const double iv = recip_nr(vm);
                 Ei[idx] = iv;
-                ivf = (float)iv;
+                ivf = d2f_fast(iv);
             } else {
-                ivf = __frcp_rn((float)vm);
+                ivf = __frcp_rn(d2f_fast(vm));
             }
-            V32[idx] = make_float4((float)e, (float)f, ivf, 0.f);
+            V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), ivf, 0.f);
         }
         if (tid < G) {
             const int st = s_st[tid];
@@ -680,14 +769,14 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
             const bool pinned = spin[idx] != 0;
             const bool pq = P.bus_pq[bus] != 0;
             EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
-            double worst;
+            unsigned long long worst;
             if (st == SL_BACKTRACK)
                 worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
             else if (Bt.mixed && s_jprec[s])
                 worst = eval_row<2>(ec, bus, s, row, pinned, pq, Ssp, fac32, R, true);
             else
                 worst = eval_row<1>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
-            atomicMax(&s_res[s], dbits(worst));
+            atomicMax(&s_res[s], worst);
         }
         __syncthreads();
 
@@ -792,6 +881,50 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
         }
         __syncthreads();
     }
+}
+
+// Start-state table of a shared start voltage: per bus (Vm, Va, cos, sin) and (e, f, 1/Vm, 0),
+// so that loading a case costs no trigonometry. Validates the voltages like nr_klu's
+// solve_batch (nr_klu.cpp:1127-1139), reporting case 0.
+__global__ void v0_table_kernel(const double2* V0, int n, int check, double4_32a* tab, int* err) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double2 v0 = V0[i];
+        if (check && (!finite_d(v0.x) || !finite_d(v0.y))) {
+            if (atomicCAS(&err[0], 0, DE_V0_NONFINITE) == 0) {
+                err[1] = i;
+                err[2] = 0;
+            }
+        }
+        const double vm = hypot(v0.x, v0.y), va = atan2(v0.y, v0.x);
+        if (check && (vm <= 0.0 || vm > 10.0) && finite_d(vm)) {
+            if (atomicCAS(&err[0], 0, DE_V0_MAGNITUDE) == 0) {
+                err[1] = i;
+                err[2] = 0;
+            }
+        }
+        double sn, cs;
+        sincos(va, &sn, &cs);
+        tab[2 * i] = make_double4_32a(vm, va, cs, sn);
+        tab[2 * i + 1] = make_double4_32a(vm * cs, vm * sn, 1.0 / vm, 0.0);
+    }
+}
+
+// Conversion helpers applied elementwise (tests compare them with IEEE casts).
+__global__ void conversions_kernel(const double* in, int n, float* d2f, double* f2d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        d2f[i] = d2f_fast(in[i]);
+        f2d[i] = f2d_fast(d2f[i]);
+    }
+}
+
+cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d) {
+    conversions_kernel<<<(n + 255) / 256, 256>>>(in, n, d2f, f2d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream) {
+    v0_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(V0, n, check, tab, err);
+    return cudaGetLastError();
 }
 
 // Jacobian blocks and residual at one given voltage (G = 1): debug_J and tests.

@@ -271,3 +271,29 @@ def test_contingency_driver_matches_reference():
     mixed = contingency.solve_contingencies(g, reslack_islands=True, precision="mixed")
     assert np.array_equal(mixed.converged, ok) and np.array_equal(mixed.served, d["served"])
     assert np.nanmax(np.abs(mixed.V[:, ok] - Vs[:, ok])) < 1e-9
+
+
+def test_integer_pipe_conversions_match_ieee():
+    """The kernels' float <-> double helpers: float -> double exact; double -> float within
+    one float ulp of the IEEE cast (it truncates), zero / infinity / NaN preserved."""
+    import ctypes as C
+
+    from p3s_gb300 import _lib
+
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.standard_normal(4000) * 10.0 ** rng.integers(-30, 30, 4000),
+                        [0.0, -0.0, 1.0, -1.0, 3.4e38, 1e39, -1e39, 1e-39, np.inf, -np.inf, np.nan]])
+    x = np.ascontiguousarray(x)
+    d2f = np.empty(len(x), np.float32)
+    f2d = np.empty(len(x), np.float64)
+    rc = _lib.load().gbpf_selftest_conversions(_lib.d(x), len(x), d2f.ctypes.data_as(C.POINTER(C.c_float)),
+                                               _lib.d(f2d))
+    assert rc == 0, _lib.last_error()
+    ref = x.astype(np.float32)
+    normal = np.isfinite(ref) & (np.abs(ref) >= np.finfo(np.float32).tiny)
+    ulp = np.spacing(np.abs(ref[normal]).astype(np.float32))
+    assert (np.abs(d2f[normal].astype(np.float64) - ref[normal].astype(np.float64)) <= ulp).all()
+    assert (np.abs(d2f[normal]) <= np.abs(ref[normal])).all()  # toward zero
+    assert np.array_equal(f2d[normal], d2f[normal].astype(np.float64))  # exact widening
+    assert np.isnan(d2f[-1]) and np.isinf(d2f[-3]) and d2f[-3] > 0 and np.isinf(d2f[-2]) and d2f[-2] < 0
+    assert d2f[x == 0.0].tolist() == [0.0, 0.0]
