@@ -840,11 +840,12 @@ __global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const B
                 top = true;
             }
             if (top) {  // nr_klu.cpp:590-595 loop head
-                // A case on float factors (GB300 vote rule) keeps stepping until its mismatch
-                // is below polish x tol: a float step lands anywhere below tol, so without the
-                // polish its voltage would only be as close to the exact solution as tol
-                // allows, where the double path's quadratic last step lands far below tol.
-                const bool polish = Bt.mixed && Bt.vote_rule == 1 && s_vote[s] == 1;
+                // Under the GB300 vote rule a case keeps stepping until its mismatch is below
+                // polish x tol: a float step (or a double step taken after float ones) lands
+                // anywhere below tol, so without the polish its voltage would only be as close
+                // to the exact solution as tol allows, where the double path's quadratic last
+                // step lands far below tol. `converged` still means mismatch < tol.
+                const bool polish = Bt.mixed && Bt.vote_rule == 1;
                 const double tol_s = polish ? Bt.tol * Bt.polish : Bt.tol;
                 if (s_it[s] >= Bt.max_iter) {
                     s_st[s] = SL_FINISH;

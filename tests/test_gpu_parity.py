@@ -92,9 +92,13 @@ def test_mixed_precision_reaches_the_same_solution(grid2000, rule, switch):
     assert (_mismatch(g, mixed["V"][:, :16], S[:, :16]) <= 1e-8).all()
     assert (mixed["iterations"][ok] <= ref["iterations"][ok] + 2).all()
     # every float factorization rejected -> redone in double in the same step: the all-double run
+    # (under the GB300 rule, the all-double run to the polish target polish x tol)
     gpu._rcond_ratio_single = 1e30
     rejected = gpu.solve_batch(S, g.V0)
     assert gpu.last_stats["single_rejected"] == gpu.last_stats["single_factorizations"] > 0
+    if rule == "gb300":
+        gpu.precision = "double"
+        double = gpu.solve_batch(S, g.V0, tol=1e-8 * gpu.polish)
     assert np.array_equal(rejected["converged"], double["converged"])
     assert np.array_equal(rejected["iterations"], double["iterations"])
     assert np.array_equal(rejected["V"], double["V"])  # bit for bit: one mismatch for both paths
