@@ -88,8 +88,14 @@ def test_mixed_precision_reaches_the_same_solution(grid2000, rule, switch):
     assert gpu.last_stats["single_factorizations"] > 0
     ok = ref["converged"]
     assert np.array_equal(mixed["converged"], ok)
-    assert np.abs(mixed["V"][:, ok] - ref["V"][:, ok]).max() < 1e-9
     assert (_mismatch(g, mixed["V"][:, :16], S[:, :16]) <= 1e-8).all()
+    # voltages: the oracle's own answer is only as exact as its last step (it stops anywhere
+    # below tol), so the mixed result is held to 1e-9 against the oracle solved to the
+    # polish target, and to the reference-rule bar of 1e-9 against the tol-1e-8 oracle
+    ref_tight = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(S, g.V0, tol=1e-12)
+    tight = ref_tight["converged"] & ok
+    assert np.abs(mixed["V"][:, tight] - ref_tight["V"][:, tight]).max() < 1e-9
+    assert np.abs(mixed["V"][:, ok] - ref["V"][:, ok]).max() < 1e-8
     assert (mixed["iterations"][ok] <= ref["iterations"][ok] + 2).all()
     # every float factorization rejected -> redone in double in the same step: the all-double run
     # (under the GB300 rule, the all-double run to the polish target polish x tol)
@@ -274,7 +280,18 @@ def test_contingency_driver_matches_reference():
     assert np.nanmax(np.abs(res.V[:, ok] - Vs[:, ok])) < 1e-10
     mixed = contingency.solve_contingencies(g, reslack_islands=True, precision="mixed")
     assert np.array_equal(mixed.converged, ok) and np.array_equal(mixed.served, d["served"])
-    assert np.nanmax(np.abs(mixed.V[:, ok] - Vs[:, ok])) < 1e-9
+    assert np.nanmax(np.abs(mixed.V[:, ok] - Vs[:, ok])) < 1e-8
+    # against the oracle solved to the mixed path's polish target (1e-12)
+    L = d["pin"].shape[1]
+    Yx = np.repeat(d["Yx"][:, None], L, axis=1)
+    for c in range(1, L):
+        np.subtract.at(Yx[:, c], d["stamp_pos"][c - 1], d["stamp"][c - 1])
+    tight = cpu.Solver(d["Yp"], d["Yj"], d["Yx"], d["pv"], d["pq"]).solve_batch_contingency(
+        np.ascontiguousarray(np.abs(Yx)), np.ascontiguousarray(np.angle(Yx)), d["Sbus"], d["V0n1"], d["pin"],
+        tol=1e-12)
+    ok2 = ok & tight["converged"]
+    Vt = np.where(d["served"], tight["V"], np.nan)
+    assert np.nanmax(np.abs(mixed.V[:, ok2] - Vt[:, ok2])) < 1e-9
 
 
 def test_integer_pipe_conversions_match_ieee():
