@@ -146,6 +146,21 @@ int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t
                  const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
                  int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands);
 
+/* gbpf_islands on caller-owned DEVICE buffers (same layouts; out_idx holds n_out entries),
+ * allocating nothing: the kernel's scratch is a statically allocated 16 MiB device array,
+ * so n may not exceed GBPF_ISLANDS_STATIC_MAX_BUS (larger n is rejected with an error).
+ * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and returns after it
+ * has finished. The first call on each device looks up the scratch address (make it before
+ * any stream capture). The scratch is shared by every call on a device: calls that overlap
+ * in time there (other streams or host threads) race. No reference counterpart: for callers
+ * that must not allocate device memory (cudaMalloc / cudaFree synchronise the whole device,
+ * stalling the solves a serving loop overlaps, and can fail under a memory budget). */
+#define GBPF_ISLANDS_STATIC_MAX_BUS 65536
+int gbpf_islands_device_static(int n, int m, const int32_t* d_f, const int32_t* d_t, const uint8_t* d_live, int L,
+                               const int32_t* d_out_ptr, const int32_t* d_out_idx, int n_out,
+                               const uint8_t* d_is_slack, const double* d_gen_prio, int reslack, int32_t* d_labels,
+                               uint8_t* d_served, int32_t* d_ref_bus, int32_t* d_n_islands, void* stream);
+
 /* Host-only check of the planner and the device schedule (runs without a GPU): plan for
  * `workers` workers, Jacobian at (Vm, Va) with injections S (n complex), the schedule
  * executed serially with a structural race check per level. dx (n x 2): Newton step per

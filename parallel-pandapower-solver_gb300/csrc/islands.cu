@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 
 #include "gbpf.h"
@@ -205,5 +206,123 @@ extern "C" int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, co
         if (p) cudaFree(p);
     if (e) return ifail(std::string("gbpf_islands: ") + cudaGetErrorString(e));
     if (kerr) return ifail("gbpf_islands: label propagation did not settle");
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// gbpf_islands_device_static: the islanding kernel on caller-owned device buffers with its
+// scratch in statically allocated device memory, so a call allocates nothing (no
+// cudaMalloc / cudaFree, no library routine that allocates). The scratch below is shared
+// by every call on a device and keeps its last contents: the kernel initialises the label
+// and per-island words it reads, and the error word is cleared before each launch. Calls
+// that overlap in time on one device (other streams, other host threads) race on it.
+namespace {
+
+constexpr int STATIC_INTS = 1 << 21;  // 8 MiB: 4 n ints per CTA
+constexpr int STATIC_BEST = 1 << 20;  // 8 MiB: n u64 per CTA
+constexpr int STATIC_MAX_DEVICES = 64;
+static_assert(GBPF_ISLANDS_STATIC_MAX_BUS <= STATIC_BEST, "one CTA must fit the static scratch");
+
+static __device__ __align__(256) int g_static_ints[STATIC_INTS];
+static __device__ __align__(256) unsigned long long g_static_best[STATIC_BEST];
+static __device__ __align__(256) int g_static_err[64];
+
+struct StaticScratch {
+    int* ints = nullptr;
+    unsigned long long* best = nullptr;
+    int* err = nullptr;
+    int nsm = 0;
+    bool ready = false;
+};
+StaticScratch g_static[STATIC_MAX_DEVICES];
+std::mutex g_static_mu;
+
+// Validates the caller's device arrays before the islanding kernel indexes with them:
+// bit 1 branch end out of range, bit 2 outage pointers not a non-decreasing 0..n_out run,
+// bit 4 outage index out of range.
+__global__ void islands_check_kernel(int n, int m, const int* f, const int* t, int L, const int* out_ptr,
+                                     const int* out_idx, int n_out, int* err) {
+    const int stride = gridDim.x * blockDim.x;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int bad = 0;
+    for (int e = i0; e < m; e += stride)
+        if (f[e] < 0 || f[e] >= n || t[e] < 0 || t[e] >= n) bad |= 1;
+    for (int c = i0; c <= L; c += stride) {
+        const int p = out_ptr[c];
+        if (c == 0 ? p != 0 : (p < out_ptr[c - 1] || p > n_out)) bad |= 2;
+        if (c == L && p != n_out) bad |= 2;
+    }
+    for (int q = i0; q < n_out; q += stride)
+        if (out_idx[q] < 0 || out_idx[q] >= m) bad |= 4;
+    if (bad) atomicOr(err, bad);
+}
+
+int static_setup(StaticScratch** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return ifail(std::string("gbpf_islands_device_static: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES) return ifail("gbpf_islands_device_static: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    StaticScratch& s = g_static[dev];
+    if (!s.ready) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_ints);
+        if (e) return ifail(std::string("gbpf_islands_device_static: scratch address: ") + cudaGetErrorString(e));
+        s.ints = static_cast<int*>(p);
+        e = cudaGetSymbolAddress(&p, g_static_best);
+        if (e) return ifail(std::string("gbpf_islands_device_static: scratch address: ") + cudaGetErrorString(e));
+        s.best = static_cast<unsigned long long*>(p);
+        e = cudaGetSymbolAddress(&p, g_static_err);
+        if (e) return ifail(std::string("gbpf_islands_device_static: scratch address: ") + cudaGetErrorString(e));
+        s.err = static_cast<int*>(p);
+        e = cudaDeviceGetAttribute(&s.nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e) return ifail(std::string("gbpf_islands_device_static: ") + cudaGetErrorString(e));
+        s.ready = true;
+    }
+    *out = &s;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int gbpf_islands_device_static(int n, int m, const int32_t* d_f, const int32_t* d_t,
+                                          const uint8_t* d_live, int L, const int32_t* d_out_ptr,
+                                          const int32_t* d_out_idx, int n_out, const uint8_t* d_is_slack,
+                                          const double* d_gen_prio, int reslack, int32_t* d_labels,
+                                          uint8_t* d_served, int32_t* d_ref_bus, int32_t* d_n_islands, void* stream) {
+    if (n <= 0 || m < 0 || L <= 0 || n_out < 0) return ifail("gbpf_islands_device_static: invalid sizes");
+    if (n > GBPF_ISLANDS_STATIC_MAX_BUS)
+        return ifail("gbpf_islands_device_static: n = " + std::to_string(n) +
+                     " buses exceeds the static scratch maximum of " + std::to_string(GBPF_ISLANDS_STATIC_MAX_BUS));
+    if (!d_live || !d_out_ptr || !d_is_slack || !d_labels || !d_served || !d_ref_bus || !d_n_islands ||
+        (m > 0 && (!d_f || !d_t)) || (n_out > 0 && !d_out_idx))
+        return ifail("gbpf_islands_device_static: null device pointer");
+    if (reslack && !d_gen_prio) return ifail("gbpf_islands_device_static: gen_prio is required with reslack");
+    StaticScratch* s = nullptr;
+    if (static_setup(&s)) return -1;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int per_cta = std::min(STATIC_INTS / (4 * n), STATIC_BEST / n);
+    const int grid = std::max(1, std::min(std::min(L, 4 * s->nsm), per_cta));
+    int herr = 0;
+    cudaError_t e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
+    if (!e) {
+        const int span = std::max(std::max(m, n_out), L + 1);
+        const int cg = std::max(1, std::min((span + 255) / 256, 4 * s->nsm));
+        islands_check_kernel<<<cg, 256, 0, st>>>(n, m, d_f, d_t, L, d_out_ptr, d_out_idx, n_out, s->err);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) return ifail(std::string("gbpf_islands_device_static: ") + cudaGetErrorString(e));
+    if (herr & 1) return ifail("gbpf_islands_device_static: branch end out of range");
+    if (herr & 2) return ifail("gbpf_islands_device_static: outage pointers must rise from 0 to n_out");
+    if (herr & 4) return ifail("gbpf_islands_device_static: outage index out of range");
+    islands_kernel<<<grid, NT, 0, st>>>(n, m, d_f, d_t, d_live, L, d_out_ptr, d_out_idx, d_is_slack, d_gen_prio,
+                                        reslack, s->ints, s->best, d_labels, d_served, d_ref_bus, d_n_islands, s->err);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) return ifail(std::string("gbpf_islands_device_static: ") + cudaGetErrorString(e));
+    if (herr) return ifail("gbpf_islands_device_static: label propagation did not settle");
     return 0;
 }

@@ -97,6 +97,8 @@ SIGNATURES = {
                                      _dp, _dp, _ip, C.c_char_p, C.c_int]),
     "gbpf_islands": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                _ip, _ip]),
+    "gbpf_islands_device_static": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, _vp,
+                                             _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 }
 
 
