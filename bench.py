@@ -100,11 +100,14 @@ def shared_start(g):
     return np.ascontiguousarray(r["V"][:, 0])
 
 
-def n_lanes(g, cases_per_cta=32):
-    import torch
+def n_lanes(T, cases_per_cta=32, threads_per_cta=512, nsm=None):
+    """Warm-start lanes: one per case slot of the launch (SMs x resident CTAs x slots), at most
+    one per hour. K = T starts every hour from the shared start (the reference's semantics)."""
+    if nsm is None:
+        import torch
 
-    nsm = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
-    return nsm * cases_per_cta
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
+    return min(T, nsm * (1024 // threads_per_cta) * cases_per_cta)
 
 
 def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
@@ -211,7 +214,7 @@ def run_gpu(args, rank, world, local):
     T = S.shape[1]
     solver = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     info = solver.info
-    K = args.lanes or n_lanes(g, info["cases_per_cta"])
+    K = args.lanes or n_lanes(T, info["cases_per_cta"], info["threads_per_cta"])
     off = lanes(T, K).astype(np.int64)
     dev = torch.device("cuda", local)
     dS = torch.from_numpy(S.view(np.float64).copy()).to(dev)
@@ -258,6 +261,19 @@ def run_gpu(args, rank, world, local):
     osv = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     hrs = np.linspace(0, T - 1, 8).astype(int)
     worst_mis = max(float(np.abs(osv.debug_J_at(S[:, h], V[:, h])["F"]).max()) for h in hrs)
+    # voltages of the mixed path against the double path at the same tolerance (the oracle's
+    # iterations; it stops anywhere below tol) and against a converged double solve (tol 1e-12)
+    Vd = {}
+    for tol in (1e-8, 1e-12):
+        dev_step(GpuSolver.params(precision="double", tol=tol))
+        Vd[tol] = dV.cpu().numpy().view(np.complex128).reshape(g.n, T)
+
+    def dv(a, b):
+        return {"max_dVm": float(np.abs(np.abs(a) - np.abs(b)).max()),
+                "max_dVa_rad": float(np.abs(np.angle(a * np.conj(b))).max())}
+
+    accuracy = {"mixed_vs_fp64_path": dv(V, Vd[1e-8]), "mixed_vs_converged_fp64": dv(V, Vd[1e-12]),
+                "fp64_path_vs_converged_fp64": dv(Vd[1e-8], Vd[1e-12])}
 
     # end to end through the public API, pinned host buffers
     Sh = pinned_empty(S.shape, np.complex128)
@@ -280,7 +296,7 @@ def run_gpu(args, rank, world, local):
     d2h = Vh.nbytes + ith.nbytes + cvh.nbytes
 
     res = dict(out=out, e2e_ms=float(np.mean(e2e_ms)), h2d=h2d, d2h=d2h, info=info, K=len(off) - 1, T=T,
-               worst_mis=worst_mis, g=g)
+               worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish)
     return res
 
 
@@ -343,8 +359,8 @@ def gpu_line(args, res, rank, world):
         "data": "synthetic (seeded 2,000-bus grid and 8,760-hour load/generation series)",
         "config": {
             "workload": f"2,000-bus grid x {T} hourly cases, warm-start lanes K={res['K']} "
-                        f"(hour h of a lane starts from hour h-1's converged voltage; a lane's first hour "
-                        f"from the converged base case)",
+                        f"(hour h of a lane starts from hour h-1's converged voltage, a lane's first hour "
+                        f"from the converged base case; K = {T} starts every hour from it)",
             "n_bus": g.n, "n_branch": g.n_branch, "n_pv": len(g.pv), "n_pq": len(g.pq), "hours": T,
             "lanes": res["K"], "tol_pu": 1e-8, "max_iter": 30, "precision": "mixed",
             "mixed_switch": args.mixed_switch,
@@ -352,17 +368,19 @@ def gpu_line(args, res, rank, world):
             "l2": "inputs larger than L2 (S is 280 MB per step; L2 is 129 MB)",
             "iterations_mean": float(mixed["it"].mean()), "converged": bool(mixed["cv"].all()),
             "max_mismatch_pu_sampled": res["worst_mis"],
+            "polish": res["polish"], "threads_per_cta": info["threads_per_cta"],
             "single_factorizations": int(mixed["stats"]["single_factorizations"]),
             "double_factorizations": int(mixed["stats"]["double_factorizations"]),
         },
         "fp64": fp64,
+        "accuracy": res["accuracy"],
         "roofline": roof,
         "cpu_baseline": cb,
         "e2e": {"value": round(world * T / (e2e_ms * 1e-3), 1), "unit": "solves/s",
                 "h2d_bytes_per_step": int(res["h2d"]), "d2h_bytes_per_step": int(res["d2h"]),
                 "ms_per_step": round(e2e_ms, 3)},
         "clocks": mixed["clocks"],
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,  # per step: the start-state table kernel + the Newton kernel
         "wall_ms_per_step": round(mixed["wall_ms"], 3),
     }
     return line
@@ -413,7 +431,7 @@ def run_reference(args, rank, world):
     g = grid_2000(0)
     hours = min(args.cpu_hours, HOURS)
     _, S = workload(0, hours)
-    K = max(1, round(hours * (args.lanes or 152 * 32) / HOURS))
+    K = max(1, round(hours * (args.lanes or n_lanes(HOURS, nsm=152)) / HOURS))
     V0 = shared_start(g)
     for _ in range(args.warmup):
         cpu_solve(g, S, K, V0)
@@ -452,7 +470,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--hours", type=int, default=HOURS)
-    ap.add_argument("--lanes", type=int, default=0, help="warm-start lanes (0: SMs x cases per CTA)")
+    ap.add_argument("--lanes", type=int, default=0, help="warm-start lanes (0: one per case slot, at most T)")
     ap.add_argument("--mixed-switch", type=float, default=1e-3)
     ap.add_argument("--cpu-hours", type=int, default=HOURS)
     args = ap.parse_args()

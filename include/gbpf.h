@@ -36,7 +36,7 @@ typedef struct gbpf_params {
     int vote_rule;       /* mixed: 0 = the reference's precision votes (nr_polar_kernels.cu:209-228),
                             1 = float until contraction stalls below mixed_switch */
     double polish;       /* vote_rule 1: a case on float factors iterates until mismatch < polish * tol,
-                            so its voltage is as accurate as a double solve's (1e-4) */
+                            so its voltage is as accurate as a double solve's (1e-3) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -67,7 +67,8 @@ int gbpf_device_count(void);
  * cases_per_cta: 0 = automatic, else a power of two in 1..32. Returns NULL on error. */
 gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
                          int npv, const int32_t* pq, int npq, int cases_per_cta);
-/* gbpf_create with the CTA shape chosen explicitly: threads_per_cta 512 or 1024 (0 = 1024). */
+/* gbpf_create with the CTA shape chosen explicitly: threads_per_cta 256, 512 or 1024 (0 = 512);
+ * CTAs of 1024 / threads_per_cta threads share an SM. */
 gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz,
                             const int32_t* pv, int npv, const int32_t* pq, int npq, int cases_per_cta,
                             int threads_per_cta);

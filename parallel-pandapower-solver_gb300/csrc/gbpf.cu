@@ -144,7 +144,7 @@ int compute_rcond0(gbpf_solver* s) {
     return 0;
 }
 
-int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
+int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta, int n_var_bus) {
     CK(cudaGetDevice(&s->device));
     CK(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -152,15 +152,15 @@ int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     CK(cudaEventCreate(&s->e1));
     CK(cudaEventCreate(&s->c0));
     CK(cudaEventCreate(&s->c1));
-    s->NT = threads_per_cta > 0 ? threads_per_cta : 1024;
-    if (s->NT != 512 && s->NT != 1024) return fail("threads_per_cta must be 512 or 1024");
+    s->NT = threads_per_cta > 0 ? threads_per_cta : 512;
+    if (s->NT != 256 && s->NT != 512 && s->NT != 1024) return fail("threads_per_cta must be 256, 512 or 1024");
     int G = cases_per_cta;
     if (G <= 0) {
-        // cases per CTA: enough slots to keep the CTA's workers busy on small grids,
-        // few enough that the per-CTA working set of large grids stays L2-friendly
-        // (measured on GB300, 2,000-bus grid: 32 slots x 1024 threads is fastest; larger
-        // grids get fewer slots so the per-CTA working set stays bounded)
-        const int nv = std::max(1, (int)s->plan.nv);
+        // cases per CTA: as many slots as a warp has lanes while the per-CTA working set
+        // stays bounded (measured on GB300, 2,000-bus grid x 8,760 cases: two 512-thread
+        // CTAs of 32 slots per SM are fastest; fewer slots per SM starve the memory
+        // pipeline, 1,024-thread CTAs of 32 slots overlap less), fewer on large grids
+        const int nv = std::max(1, n_var_bus);
         G = nv <= 4096 ? 32 : (nv <= 16384 ? 16 : 8);
     }
     if (G < 1 || G > gbpf::MAX_SLOTS || (G & (G - 1))) return fail("cases_per_cta must be a power of two in 1..32");
@@ -283,7 +283,7 @@ gbpf_params default_params() {
     p.pivot_ratio_double = 1e-3;
     p.pivot_ratio_single = 1e-3;
     p.vote_rule = 1;
-    p.polish = 1e-4;
+    p.polish = 1e-3;
     return p;
 }
 
@@ -397,17 +397,8 @@ gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const d
     s->Yp.assign(Yp, Yp + n + 1);
     s->Yj.assign(Yj, Yj + nnz);
     s->Yx.assign(Yx, Yx + 2 * (size_t)nnz);
-    // workers depend on the slot count; choose the slot count first from the bus count
-    {
-        gbpf::Plan probe;
-        std::string e = gbpf::build_plan(probe, n, Yp, Yj, nnz, pv, npv, pq, npq, 1);
-        if (!e.empty()) {
-            fail("gbpf_create: " + e);
-            return nullptr;
-        }
-        s->plan.nv = probe.nv;
-    }
-    if (setup(s.get(), cases_per_cta, threads_per_cta)) return nullptr;
+    // workers depend on the slot count, chosen first from the number of non-slack buses
+    if (setup(s.get(), cases_per_cta, threads_per_cta, npv + npq)) return nullptr;
     std::string e = gbpf::build_plan(s->plan, n, Yp, Yj, nnz, pv, npv, pq, npq, s->NT / s->G);
     if (!e.empty()) {
         fail("gbpf_create: " + e);

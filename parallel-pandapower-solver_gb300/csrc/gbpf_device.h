@@ -117,7 +117,6 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
                               double2* R, cudaStream_t stream);
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d);
-int newton_max_threads();
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
 const void* newton_kernel_ptr(int threads);
 

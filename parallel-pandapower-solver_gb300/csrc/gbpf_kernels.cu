@@ -27,7 +27,6 @@
 
 namespace gbpf {
 
-#define NT_NEWTON 512  // threads per CTA of the smaller variant (1024 also compiled, the default)
 
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
@@ -485,8 +484,11 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 }
 
 // ------------------------------------------------------------------------- the kernel
+// NTB threads per CTA and 1024 / NTB resident CTAs per SM (64 registers per thread in
+// every variant): smaller CTAs let one CTA's latency-bound factorization overlap another's
+// double-precision evaluation on the same SM.
 template <int NTB>
-__global__ void __launch_bounds__(NTB, 1) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
+__global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
     const int G = Sc.G, lg = Sc.log2G;
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
@@ -957,6 +959,8 @@ cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, in
         newton_kernel<1024><<<grid, 1024, 0, stream>>>(P, B, S);
     else if (threads == 512)
         newton_kernel<512><<<grid, 512, 0, stream>>>(P, B, S);
+    else if (threads == 256)
+        newton_kernel<256><<<grid, 256, 0, stream>>>(P, B, S);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -969,10 +973,10 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
     return cudaGetLastError();
 }
 
-int newton_max_threads() { return NT_NEWTON; }
-
 const void* newton_kernel_ptr(int threads) {
-    return threads == 1024 ? (const void*)newton_kernel<1024> : (const void*)newton_kernel<512>;
+    if (threads == 1024) return (const void*)newton_kernel<1024>;
+    if (threads == 512) return (const void*)newton_kernel<512>;
+    return (const void*)newton_kernel<256>;
 }
 
 }  // namespace gbpf

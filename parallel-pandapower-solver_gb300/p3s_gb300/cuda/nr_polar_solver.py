@@ -39,7 +39,7 @@ class PolarNewtonSolverCUDA:
         # "reference": the reference's votes (float above mixed_switch, double below it)
         self.vote_rule = "gb300"
         # gb300 rule: a case on float factors iterates until its mismatch is below polish * tol
-        self.polish = 1e-4
+        self.polish = 1e-3
         self.line_search = True
         self.fallback = "none"
         self.cpu_handoff = 0

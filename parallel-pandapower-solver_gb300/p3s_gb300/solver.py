@@ -107,7 +107,7 @@ class GpuSolver:
 
     @staticmethod
     def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False,
-               pivot_ratio_double=1e-3, pivot_ratio_single=1e-3, vote_rule="gb300", polish=1e-4):
+               pivot_ratio_double=1e-3, pivot_ratio_single=1e-3, vote_rule="gb300", polish=1e-3):
         if precision not in ("double", "mixed"):
             raise ValueError(f"precision must be 'double' or 'mixed', got {precision!r}")
         return _lib.Params(int(max_iter), float(tol), int(bool(line_search)), 1 if precision == "mixed" else 0,

@@ -281,7 +281,7 @@ def test_contingency_driver_matches_reference():
     mixed = contingency.solve_contingencies(g, reslack_islands=True, precision="mixed")
     assert np.array_equal(mixed.converged, ok) and np.array_equal(mixed.served, d["served"])
     assert np.nanmax(np.abs(mixed.V[:, ok] - Vs[:, ok])) < 1e-8
-    # against the oracle solved to the mixed path's polish target (1e-12)
+    # against the oracle solved to convergence (tol 1e-12)
     L = d["pin"].shape[1]
     Yx = np.repeat(d["Yx"][:, None], L, axis=1)
     for c in range(1, L):
