@@ -300,6 +300,37 @@ def run_gpu(args, rank, world, local):
     return res
 
 
+def run_n1(args):
+    """The full N-1 sweep of the same grid (base case + every single-branch outage, 3,001
+    cases): device islanding with re-slack, then one stamp-patched solve, through the public
+    driver (host arrays in and out). Reported beside the time series, not as the headline."""
+    from p3s_gb300 import contingency
+    from p3s_gb300.cuda.nr_polar_solver import PolarNewtonSolverCUDA
+    from p3s_gb300.synthetic import grid_2000
+
+    g = grid_2000(0)
+    batch = contingency.build_batch(g)
+    solver = PolarNewtonSolverCUDA(batch.Yp, batch.Yj, batch.Yx_base, batch.pv, batch.pq)
+    out = {"cases": len(batch.groups)}
+    for prec in ("mixed", "double"):
+        for _ in range(args.warmup):
+            r = contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver)
+        wall, kern = [], []
+        for _ in range(max(1, args.steps // 2)):
+            t0 = time.perf_counter()
+            r = contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver)
+            wall.append(time.perf_counter() - t0)
+            kern.append(solver.last_stats["kernel_ms"])
+        L = len(batch.groups)
+        out["fp64" if prec == "double" else prec] = {
+            "value": round(L / (np.mean(kern) * 1e-3), 1), "unit": "solves/s", "kernel_ms": round(float(np.mean(kern)), 3),
+            "e2e_solves_per_s": round(L / np.mean(wall), 1), "e2e_ms": round(float(np.mean(wall)) * 1e3, 1),
+            "iterations_mean": float(r.iterations.mean()), "converged": int(r.converged.sum()),
+            "islanded_cases": int((r.served.sum(axis=0) < g.n).sum()),
+        }
+    return out
+
+
 def gpu_line(args, res, rank, world):
     out = res["out"]
     T = res["T"]
@@ -374,6 +405,7 @@ def gpu_line(args, res, rank, world):
         },
         "fp64": fp64,
         "accuracy": res["accuracy"],
+        "n1_sweep": res.get("n1"),
         "roofline": roof,
         "cpu_baseline": cb,
         "e2e": {"value": round(world * T / (e2e_ms * 1e-3), 1), "unit": "solves/s",
@@ -473,6 +505,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=0, help="warm-start lanes (0: one per case slot, at most T)")
     ap.add_argument("--mixed-switch", type=float, default=1e-3)
     ap.add_argument("--cpu-hours", type=int, default=HOURS)
+    ap.add_argument("--no-n1", action="store_true", help="skip the N-1 sweep block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":  # rank 0 alone times the CPU reference; other ranks exit at once
@@ -481,6 +514,8 @@ def main():
         return
     rank, world, local = dist_init()
     res = run_gpu(args, rank, world, local)
+    if rank == 0 and not args.no_n1:
+        res["n1"] = run_n1(args)
     line = gpu_line(args, res, rank, world)
     if line is not None:
         print(json.dumps(line), flush=True)

@@ -318,3 +318,43 @@ def test_integer_pipe_conversions_match_ieee():
     assert np.array_equal(f2d[normal], d2f[normal].astype(np.float64))  # exact widening
     assert np.isnan(d2f[-1]) and np.isinf(d2f[-3]) and d2f[-3] > 0 and np.isinf(d2f[-2]) and d2f[-2] < 0
     assert d2f[x == 0.0].tolist() == [0.0, 0.0]
+
+
+def test_n1_sweep_of_the_2000_bus_grid(grid2000):
+    """The full N-1 sweep (base case + every single-branch outage): islands, served masks and
+    references bit-exact against the restated reference islanding for all 3,001 cases; the
+    solves of a sample (every islanded case plus random ones) against the oracle."""
+    from oracle import islands as oisl
+    from p3s_gb300 import contingency
+
+    g = grid2000
+    batch = contingency.build_batch(g)
+    assert len(batch.groups) == g.n_branch + 1
+    prio = np.zeros(g.n)
+    prio[g.pv] = g.p_gen[g.pv]
+    lab, sv, rb, ni = contingency.islands(batch, True, prio)
+    olab, osv, orb, oni = oisl.islands(g.n, g.f, g.t, batch.live, batch.groups, g.ref, True, prio)
+    assert np.array_equal(lab, olab) and np.array_equal(sv, osv)
+    assert np.array_equal(rb, orb) and np.array_equal(ni, oni)
+    split = np.nonzero(ni > 1)[0]
+    assert len(split) > 0
+    rng = np.random.default_rng(3)
+    pick = np.union1d(split[:48], rng.choice(len(batch.groups), 48, replace=False))
+    groups = [batch.groups[c] for c in pick]
+    sub = contingency.build_batch(g, groups=groups)
+    s_lab, s_sv, s_rb, _ = contingency.islands(sub, True, prio)
+    V0, pin = contingency.start_and_pins(sub, g.V0, s_sv, s_rb)
+    Yx = sub.Yx_matrix
+    osolver = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    ref = osolver.solve_batch_contingency(np.abs(Yx), np.angle(Yx), g.Sbus, V0, pin)
+    ok = ref["converged"]
+    assert ok.all()
+    res = contingency.solve_contingencies(g, reslack_islands=True, groups=groups)
+    assert np.array_equal(res.served, s_sv) and np.array_equal(res.converged, ok)
+    assert np.array_equal(res.iterations, ref["iterations"])
+    Vs = np.where(s_sv, ref["V"], np.nan)
+    assert np.nanmax(np.abs(res.V - Vs)) < 1e-10  # the oracle rebuilds each Ybus from |Y| and angle
+    mixed = contingency.solve_contingencies(g, reslack_islands=True, groups=groups, precision="mixed")
+    tight = osolver.solve_batch_contingency(np.abs(Yx), np.angle(Yx), g.Sbus, V0, pin, tol=1e-12)
+    assert np.array_equal(mixed.converged, ok) and tight["converged"].all()
+    assert np.nanmax(np.abs(mixed.V - np.where(s_sv, tight["V"], np.nan))) < 1e-9
