@@ -54,6 +54,7 @@ typedef struct gbpf_stats {
     int grid, cases_per_cta;
     double kernel_ms; /* device time of the Newton kernel, CUDA events on the solver's stream */
     double call_ms;   /* device time of the last host-pointer call: first copy in to last copy out */
+    int threads_per_cta; /* CTA shape of the last launch (with cases_per_cta) */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);
@@ -64,11 +65,12 @@ int gbpf_device_count(void);
  * factorization and schedule, device upload.
  * Replaces nr_klu.Solver(Yp, Yj, Yx, pv, pq) (nr_klu.cpp:964-994, build_topology :732-759)
  * and PolarNewtonSolverCUDA(Yp, Yj, Yx, pv, pq) (nr_polar_solver.py:285-378).
- * cases_per_cta: 0 = automatic, else a power of two in 1..32. Returns NULL on error. */
+ * cases_per_cta: 0 = chosen per batch size, else a power of two in 1..32. Returns NULL on error. */
 gbpf_solver* gbpf_create(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
                          int npv, const int32_t* pq, int npq, int cases_per_cta);
-/* gbpf_create with the CTA shape chosen explicitly: threads_per_cta 256, 512 or 1024 (0 = 512);
- * CTAs of 1024 / threads_per_cta threads share an SM. */
+/* gbpf_create with the CTA shape fixed: threads_per_cta 256, 512 or 1024 and cases_per_cta a
+ * power of two in 1..32; 0 leaves that part to the batch-size rule (gbpf_get_shape). CTAs of
+ * 1024 / threads_per_cta threads share an SM. */
 gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz,
                             const int32_t* pv, int npv, const int32_t* pq, int npq, int cases_per_cta,
                             int threads_per_cta);
@@ -80,6 +82,16 @@ int gbpf_update_Y(gbpf_solver* s, const double* Yx, int nnz);
 
 int gbpf_get_info(gbpf_solver* s, gbpf_info* out);
 int gbpf_get_stats(gbpf_solver* s, gbpf_stats* out);
+/* CTA shape (threads per CTA, case slots per CTA) the solver launches for a batch of
+ * `units` work items (cases, or lanes), and an override per batch-size class
+ * (ceil(log2(units))) -- what an autotuner sets after timing candidate shapes. Results do not
+ * depend on the shape (every case runs the same arithmetic); only the speed does.
+ * threads_per_cta = cases_per_cta = 0 removes the override. No reference counterpart (the
+ * reference's lean LU kernel takes a fixed warps-per-block `slots` argument,
+ * nr_polar_solver.py:285-300). */
+int gbpf_get_shape(gbpf_solver* s, long long units, int* threads_per_cta, int* cases_per_cta);
+int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cases_per_cta);
+
 /* Ybus nnz -> Jacobian block position (-1 for slack rows/columns), length nnz. */
 int gbpf_get_posmap(gbpf_solver* s, int32_t* out);
 

@@ -76,31 +76,45 @@ int ilog2(int g) {
 
 void gbpf::set_error(const std::string& msg) { g_err = msg; }
 
+// One CTA shape of the Newton kernel for a topology: threads per CTA, case slots per CTA,
+// and the factorization schedule dealt to its NT / G workers (built on first use).
+struct Shape {
+    int NT = 0, G = 0, lg = 0, occ = 1;
+    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC;
+    gbpf::DevPlan dp{};
+    ~Shape() {
+        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC}) b->release();
+    }
+};
+
+constexpr int N_SIZE_CLASSES = 48;  // batch sizes by ceil(log2(work items))
+
 struct gbpf_solver {
     gbpf::Plan plan;
     int n = 0, nnz = 0;
     std::vector<int> Yp, Yj;
     std::vector<double> Yx;  // interleaved complex
-    int device = 0, nsm = 0, occ = 1;
+    int device = 0, nsm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
-    int G = 8, lg = 3, NT = 512;
+    int fixed_NT = 0, fixed_G = 0;               // CTA shape requested at creation (0: by batch size)
+    int table_NT[N_SIZE_CLASSES] = {}, table_G[N_SIZE_CLASSES] = {};  // shapes set per size class
+    std::vector<std::unique_ptr<Shape>> shapes;
     // topology on the device
-    DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dpairs,
-        drow_pq, dbus_of_row, ddpos;
-    gbpf::DevPlan dp{};
-    // scratch (per CTA, grow-only)
+    DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos;
+    gbpf::DevPlan dp{};  // topology part (schedule fields filled per shape)
+    // scratch (case slots, grow-only)
     DBuf fac64, fac32, R, y64, y32, Vc, Vt, Et, Ei, V32, spin;
-    size_t sc_ctas = 0;
+    size_t sc_slots = 0;
     bool sc_mixed = false;
     // per-call buffers (grow-only)
     DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab;
     gbpf_stats last{};
     ~gbpf_solver() {
-        for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dtaskA, &dptrA, &dscl, &dptrB,
-                        &dtaskC, &dptrC, &dpairs, &drow_pq, &dbus_of_row, &ddpos, &fac64, &fac32, &R, &y64, &y32,
-                        &Vc, &Vt, &Et, &Ei, &V32, &spin, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv,
-                        &bYd, &bpin, &btab})
+        shapes.clear();
+        for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
+                        &ddpos, &fac64, &fac32, &R, &y64, &y32, &Vc, &Vt, &Et, &Ei, &V32, &spin, &bS, &bV0, &bV, &bit,
+                        &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin, &btab})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -144,7 +158,7 @@ int compute_rcond0(gbpf_solver* s) {
     return 0;
 }
 
-int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta, int n_var_bus) {
+int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     CK(cudaGetDevice(&s->device));
     CK(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -152,23 +166,92 @@ int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta, int n_var_bus)
     CK(cudaEventCreate(&s->e1));
     CK(cudaEventCreate(&s->c0));
     CK(cudaEventCreate(&s->c1));
-    s->NT = threads_per_cta > 0 ? threads_per_cta : 512;
-    if (s->NT != 256 && s->NT != 512 && s->NT != 1024) return fail("threads_per_cta must be 256, 512 or 1024");
-    int G = cases_per_cta;
-    if (G <= 0) {
-        // cases per CTA: as many slots as a warp has lanes while the per-CTA working set
-        // stays bounded (measured on GB300, 2,000-bus grid x 8,760 cases: two 512-thread
-        // CTAs of 32 slots per SM are fastest; fewer slots per SM starve the memory
-        // pipeline, 1,024-thread CTAs of 32 slots overlap less), fewer on large grids
-        const int nv = std::max(1, n_var_bus);
-        G = nv <= 4096 ? 32 : (nv <= 16384 ? 16 : 8);
+    if (threads_per_cta != 0 && threads_per_cta != 256 && threads_per_cta != 512 && threads_per_cta != 1024)
+        return fail("threads_per_cta must be 256, 512 or 1024");
+    if (cases_per_cta != 0 && (cases_per_cta < 1 || cases_per_cta > gbpf::MAX_SLOTS || (cases_per_cta & (cases_per_cta - 1))))
+        return fail("cases_per_cta must be a power of two in 1..32");
+    s->fixed_NT = threads_per_cta;
+    s->fixed_G = cases_per_cta;
+    return 0;
+}
+
+int size_class(long long units) {
+    int c = 0;
+    while (c + 1 < N_SIZE_CLASSES && (1LL << c) < units) ++c;
+    return c;
+}
+
+// CTA shape for a batch of `units` work items. Case slots per SM: the batch's share of an
+// SM rounded up to a power of two (measured on GB300, 2,000-bus grid: every batch from 1 to
+// 8,760 cases is within a few percent of its best shape this way), at most 64 per SM
+// (32 per SM above 4,096 variable buses, 16 above 16,384: the per-slot working set grows
+// with the grid). Up to 4 slots per SM run as one 1,024-thread CTA (many workers per
+// case); more run as two 512-thread CTAs per SM, whose phases overlap.
+void choose_shape(const gbpf_solver* s, long long units, int* NT, int* G) {
+    const int c = size_class(units);
+    if (s->table_NT[c]) {
+        *NT = s->table_NT[c];
+        *G = s->table_G[c];
+        return;
     }
-    if (G < 1 || G > gbpf::MAX_SLOTS || (G & (G - 1))) return fail("cases_per_cta must be a power of two in 1..32");
-    s->G = G;
-    s->lg = ilog2(G);
+    const int nv = std::max(1, s->plan.nv);
+    const int cap = nv <= 4096 ? 64 : (nv <= 16384 ? 32 : 16);
+    const long long share = (units + s->nsm - 1) / s->nsm;
+    int per_sm = 1;
+    while (per_sm < share && per_sm < cap) per_sm *= 2;
+    int nt = s->fixed_NT, g = s->fixed_G;
+    if (!nt && !g) {
+        nt = per_sm <= 4 ? 1024 : 512;
+    } else if (!nt) {
+        nt = 512;
+    }
+    if (!g) g = std::min(gbpf::MAX_SLOTS, std::max(1, per_sm / (1024 / nt)));
+    *NT = nt;
+    *G = g;
+}
+
+// The schedule of one CTA shape: tasks dealt to NT / G workers, uploaded next to the
+// shared topology arrays.
+int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
+    for (auto& sh : s->shapes)
+        if (sh->NT == NT && sh->G == G) {
+            *out = sh.get();
+            return 0;
+        }
+    std::unique_ptr<Shape> sh(new Shape);
+    sh->NT = NT;
+    sh->G = G;
+    sh->lg = ilog2(G);
     int occ = 1;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(s->NT), s->NT, 0));
-    s->occ = std::max(1, occ);
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(NT), NT, 0));
+    sh->occ = std::max(1, occ);
+    const gbpf::Plan& p = s->plan;
+    gbpf::Schedule sc;
+    gbpf::make_schedule(p, NT / G, sc);
+    // DIAG tasks carry the "two real pivots" flag (PQ row) in bit 5 of their code
+    for (size_t t = 0; t < sc.taskA.size() / 4; ++t) {
+        if ((sc.taskA[4 * t + 1] & 3) == gbpf::TK_DIAG) {
+            const int dst = sc.taskA[4 * t];
+            const int row = (int)(std::upper_bound(p.base.begin(), p.base.end(), dst) - p.base.begin()) - 1;
+            if (p.row_pq[row]) sc.taskA[4 * t + 1] |= 32;
+        }
+    }
+    CK(upload(sh->dtaskA, sc.taskA));
+    CK(upload(sh->dptrA, sc.ptrA));
+    CK(upload(sh->dscl, sc.scl));
+    CK(upload(sh->dptrB, sc.ptrB));
+    CK(upload(sh->dtaskC, sc.taskC));
+    CK(upload(sh->dptrC, sc.ptrC));
+    sh->dp = s->dp;
+    sh->dp.W = sc.W;
+    sh->dp.taskA = sh->dtaskA.as<int4>();
+    sh->dp.ptrA = sh->dptrA.as<int>();
+    sh->dp.scl = sh->dscl.as<int2>();
+    sh->dp.ptrB = sh->dptrB.as<int>();
+    sh->dp.taskC = sh->dtaskC.as<int4>();
+    sh->dp.ptrC = sh->dptrC.as<int>();
+    *out = sh.get();
+    s->shapes.push_back(std::move(sh));
     return 0;
 }
 
@@ -179,21 +262,6 @@ int upload_plan(gbpf_solver* s) {
     CK(upload(s->dposmap, p.posmap));
     CK(upload(s->drow_of_bus, p.row_of_bus));
     CK(upload(s->dbus_pq, p.bus_pq));
-    // DIAG tasks carry the "two real pivots" flag (PQ row) in bit 5 of their code
-    std::vector<int> tA = p.taskA;
-    for (size_t t = 0; t < tA.size() / 4; ++t) {
-        if ((tA[4 * t + 1] & 3) == gbpf::TK_DIAG) {
-            const int dst = tA[4 * t];
-            const int row = (int)(std::upper_bound(p.base.begin(), p.base.end(), dst) - p.base.begin()) - 1;
-            if (p.row_pq[row]) tA[4 * t + 1] |= 32;
-        }
-    }
-    CK(upload(s->dtaskA, tA));
-    CK(upload(s->dptrA, p.ptrA));
-    CK(upload(s->dscl, p.scl));
-    CK(upload(s->dptrB, p.ptrB));
-    CK(upload(s->dtaskC, p.taskC));
-    CK(upload(s->dptrC, p.ptrC));
     CK(upload(s->dpairs, p.pairs));
     CK(upload(s->drow_pq, p.row_pq));
     CK(upload(s->dbus_of_row, p.bus_of_row));
@@ -204,7 +272,7 @@ int upload_plan(gbpf_solver* s) {
     d.n = p.n;
     d.nv = p.nv;
     d.nblk = p.nblk;
-    d.W = p.W;
+    d.W = 0;
     d.nlev = p.nlev;
     d.nblev = p.nblev;
     d.nnzY = p.nnzY;
@@ -215,12 +283,12 @@ int upload_plan(gbpf_solver* s) {
     d.posmap = s->dposmap.as<int>();
     d.row_of_bus = s->drow_of_bus.as<int>();
     d.bus_pq = s->dbus_pq.as<uint8_t>();
-    d.taskA = s->dtaskA.as<int4>();
-    d.ptrA = s->dptrA.as<int>();
-    d.scl = s->dscl.as<int2>();
-    d.ptrB = s->dptrB.as<int>();
-    d.taskC = s->dtaskC.as<int4>();
-    d.ptrC = s->dptrC.as<int>();
+    d.taskA = nullptr;
+    d.ptrA = nullptr;
+    d.scl = nullptr;
+    d.ptrB = nullptr;
+    d.taskC = nullptr;
+    d.ptrC = nullptr;
     d.pairs = s->dpairs.as<int2>();
     d.row_pq = s->drow_pq.as<uint8_t>();
     d.bus_of_row = s->dbus_of_row.as<int>();
@@ -228,36 +296,37 @@ int upload_plan(gbpf_solver* s) {
     return 0;
 }
 
-int ensure_scratch(gbpf_solver* s, size_t ctas, bool mixed) {
-    if (ctas <= s->sc_ctas && (!mixed || s->sc_mixed)) return 0;
-    ctas = std::max(ctas, s->sc_ctas);
+// Scratch for `slots` case slots (CTAs x slots per CTA; laid out per CTA, [item][slot]).
+int ensure_scratch(gbpf_solver* s, size_t slots, bool mixed) {
+    if (slots <= s->sc_slots && (!mixed || s->sc_mixed)) return 0;
+    slots = std::max(slots, s->sc_slots);
     mixed = mixed || s->sc_mixed;
-    const size_t G = s->G, nb = s->plan.nblk, nv = std::max(1, s->plan.nv), n = s->n;
-    CK(s->fac64.ensure(ctas * nb * G * 32));
-    CK(s->R.ensure(ctas * nv * G * 16));
-    CK(s->y64.ensure(ctas * nv * G * 16));
-    CK(s->Vc.ensure(ctas * n * G * 32));
-    CK(s->Vt.ensure(ctas * n * G * 32));
-    CK(s->Et.ensure(ctas * n * G * 16));
-    CK(s->Ei.ensure(ctas * n * G * 8));
-    CK(s->V32.ensure(ctas * n * G * 16));
-    CK(s->spin.ensure(ctas * n * G));
+    const size_t nb = s->plan.nblk, nv = std::max(1, s->plan.nv), n = s->n;
+    CK(s->fac64.ensure(slots * nb * 32));
+    CK(s->R.ensure(slots * nv * 16));
+    CK(s->y64.ensure(slots * nv * 16));
+    CK(s->Vc.ensure(slots * n * 32));
+    CK(s->Vt.ensure(slots * n * 32));
+    CK(s->Et.ensure(slots * n * 16));
+    CK(s->Ei.ensure(slots * n * 8));
+    CK(s->V32.ensure(slots * n * 16));
+    CK(s->spin.ensure(slots * n));
     if (mixed) {
-        CK(s->fac32.ensure(ctas * nb * G * 16));
-        CK(s->y32.ensure(ctas * nv * G * 8));
+        CK(s->fac32.ensure(slots * nb * 16));
+        CK(s->y32.ensure(slots * nv * 8));
     }
-    s->sc_ctas = ctas;
+    s->sc_slots = slots;
     s->sc_mixed = mixed;
     return 0;
 }
 
-gbpf::Scratch scratch_view(gbpf_solver* s) {
+gbpf::Scratch scratch_view(gbpf_solver* s, const Shape& sh) {
     gbpf::Scratch sc{};
-    sc.G = s->G;
-    sc.log2G = s->lg;
-    sc.blk_stride = (size_t)s->plan.nblk * s->G;
-    sc.row_stride = (size_t)std::max(1, s->plan.nv) * s->G;
-    sc.bus_stride = (size_t)s->n * s->G;
+    sc.G = sh.G;
+    sc.log2G = sh.lg;
+    sc.blk_stride = (size_t)s->plan.nblk * sh.G;
+    sc.row_stride = (size_t)std::max(1, s->plan.nv) * sh.G;
+    sc.bus_stride = (size_t)s->n * sh.G;
     sc.fac64 = s->fac64.as<double4_32a>();
     sc.fac32 = s->sc_mixed ? s->fac32.as<float4>() : nullptr;
     sc.R = s->R.as<double2>();
@@ -297,23 +366,27 @@ int check_params(const gbpf_params& p, const char* who) {
 // Run the persistent kernel over `units` work items (cases, or lanes) and wait for it.
 int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     if (units <= 0) return fail(std::string(who) + ": empty batch");
-    const long long want = (units + s->G - 1) / s->G;
-    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)s->nsm * s->occ));
-    if (int rc = ensure_scratch(s, grid, b.mixed != 0)) return rc;
+    int NT = 0, G = 0;
+    choose_shape(s, units, &NT, &G);
+    Shape* sh = nullptr;
+    if (int rc = get_shape(s, NT, G, &sh)) return rc;
+    const long long want = (units + G - 1) / G;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)s->nsm * sh->occ));
+    if (int rc = ensure_scratch(s, (size_t)grid * G, b.mixed != 0)) return rc;
     CK(s->bctl.ensure(64 * sizeof(unsigned long long)));
     auto* ctl = s->bctl.as<unsigned long long>();
     CK(cudaMemsetAsync(ctl, 0, 64 * sizeof(unsigned long long), s->stream));
     b.counter = reinterpret_cast<int*>(ctl + 16);
     b.stats = ctl;
     b.err = reinterpret_cast<int*>(ctl + 24);
-    gbpf::Scratch sc = scratch_view(s);
+    gbpf::Scratch sc = scratch_view(s, *sh);
     CK(cudaEventRecord(s->e0, s->stream));
     if (b.v0_shared) {
         CK(s->btab.ensure((size_t)s->n * 64));
         b.v0tab = s->btab.as<double4_32a>();
         CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, s->btab.as<double4_32a>(), b.err, s->stream));
     }
-    CK(gbpf::launch_newton(s->dp, b, sc, grid, s->NT, s->stream));
+    CK(gbpf::launch_newton(sh->dp, b, sc, grid, NT, s->stream));
     CK(cudaEventRecord(s->e1, s->stream));
     unsigned long long host_ctl[32];
     CK(cudaMemcpyAsync(host_ctl, ctl, sizeof host_ctl, cudaMemcpyDeviceToHost, s->stream));
@@ -326,7 +399,8 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     s->last.double_rejected = host_ctl[3];
     s->last.macro_steps = host_ctl[4];
     s->last.grid = grid;
-    s->last.cases_per_cta = s->G;
+    s->last.cases_per_cta = G;
+    s->last.threads_per_cta = NT;
     s->last.kernel_ms = ms;
     const int* err = reinterpret_cast<const int*>(host_ctl + 24);
     if (err[0] == gbpf::DE_V0_NONFINITE)
@@ -397,9 +471,8 @@ gbpf_solver* gbpf_create_ex(int n, const int32_t* Yp, const int32_t* Yj, const d
     s->Yp.assign(Yp, Yp + n + 1);
     s->Yj.assign(Yj, Yj + nnz);
     s->Yx.assign(Yx, Yx + 2 * (size_t)nnz);
-    // workers depend on the slot count, chosen first from the number of non-slack buses
-    if (setup(s.get(), cases_per_cta, threads_per_cta, npv + npq)) return nullptr;
-    std::string e = gbpf::build_plan(s->plan, n, Yp, Yj, nnz, pv, npv, pq, npq, s->NT / s->G);
+    if (setup(s.get(), cases_per_cta, threads_per_cta)) return nullptr;
+    std::string e = gbpf::build_plan(s->plan, n, Yp, Yj, nnz, pv, npv, pq, npq, 1);
     if (!e.empty()) {
         fail("gbpf_create: " + e);
         return nullptr;
@@ -428,13 +501,39 @@ int gbpf_get_info(gbpf_solver* s, gbpf_info* o) {
     o->n_blocks = p.nblk;
     o->n_levels = p.nlev;
     o->n_back_levels = p.nblev;
-    o->cases_per_cta = s->G;
-    o->threads_per_cta = s->NT;
-    o->workers = p.W;
+    int NT = 0, G = 0;  // the shape of a batch that fills the device
+    choose_shape(s, 1LL << 40, &NT, &G);
+    o->cases_per_cta = G;
+    o->threads_per_cta = NT;
+    o->workers = NT / G;
     o->factor_pairs = p.n_factor_pairs;
     o->forward_pairs = p.n_fwd_pairs;
     o->backward_pairs = p.n_bwd_pairs;
     o->rcond0 = p.rcond0;
+    return 0;
+}
+
+int gbpf_get_shape(gbpf_solver* s, long long units, int* threads_per_cta, int* cases_per_cta) {
+    if (!s || !threads_per_cta || !cases_per_cta) return fail("null argument");
+    if (units <= 0) return fail("get_shape: units must be > 0");
+    choose_shape(s, units, threads_per_cta, cases_per_cta);
+    return 0;
+}
+
+int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cases_per_cta) {
+    if (!s) return fail("null solver");
+    if (units <= 0) return fail("set_shape: units must be > 0");
+    const int c = size_class(units);
+    if (threads_per_cta == 0 && cases_per_cta == 0) {
+        s->table_NT[c] = s->table_G[c] = 0;
+        return 0;
+    }
+    if (threads_per_cta != 256 && threads_per_cta != 512 && threads_per_cta != 1024)
+        return fail("set_shape: threads_per_cta must be 256, 512 or 1024");
+    if (cases_per_cta < 1 || cases_per_cta > gbpf::MAX_SLOTS || (cases_per_cta & (cases_per_cta - 1)))
+        return fail("set_shape: cases_per_cta must be a power of two in 1..32");
+    s->table_NT[c] = threads_per_cta;
+    s->table_G[c] = cases_per_cta;
     return 0;
 }
 

@@ -74,10 +74,7 @@ int deal(const std::vector<long long>& weight, int W, std::vector<int>& who) {
     return (int)std::min<long long>(mx, 1LL << 30);
 }
 
-struct Task {
-    int level, dst, code, p0, p1;
-    long long w;
-};
+using Task = PlanTask;
 
 // Lay tasks out grouped by (level, worker); `rec` ints per record.
 void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& out, std::vector<int>& ptr,
@@ -326,11 +323,27 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
         C.push_back({p.depth[t], t, p.base[t], p0, p1, 4LL * (p1 - p0) + 8});
     }
     if (p.pairs.size() / 2 >= (size_t)1 << 31) return "too many pairs";
-    p.level_work.assign(std::max(p.nlev, p.nblev), 0);
-    layout(A, p.nlev, W, p.taskA, p.ptrA, &p.level_work, true);
-    layout(B, p.nlev, W, p.scl, p.ptrB, nullptr, false);
-    layout(C, p.nblev, W, p.taskC, p.ptrC, nullptr, true);
+    p.tasksA = std::move(A);
+    p.tasksB = std::move(B);
+    p.tasksC = std::move(C);
+    Schedule sc;
+    make_schedule(p, W, sc);
+    p.taskA = std::move(sc.taskA);
+    p.ptrA = std::move(sc.ptrA);
+    p.scl = std::move(sc.scl);
+    p.ptrB = std::move(sc.ptrB);
+    p.taskC = std::move(sc.taskC);
+    p.ptrC = std::move(sc.ptrC);
+    p.level_work = std::move(sc.level_work);
     return std::string();
+}
+
+void make_schedule(const Plan& p, int workers, Schedule& out) {
+    const int W = out.W = std::max(1, workers);
+    out.level_work.assign(std::max(p.nlev, p.nblev), 0);
+    layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true);
+    layout(p.tasksB, p.nlev, W, out.scl, out.ptrB, nullptr, false);
+    layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true);
 }
 
 // ----------------------------------------------------------------------------- host replica

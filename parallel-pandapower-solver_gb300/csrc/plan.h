@@ -26,6 +26,22 @@ namespace gbpf {
 enum TaskKind { TK_DIAG = 0, TK_U = 1, TK_L = 2, TK_FWD = 3 };
 constexpr int TASK_FILL = 1 << 4;  // block not in the Jacobian: accumulate from zero
 
+// One unit of factorization work before it is dealt to a worker: its level, destination
+// block (or row), code, pair range and weight (the dealing key).
+struct PlanTask {
+    int level, dst, code, p0, p1;
+    long long w;
+};
+
+// The worker-dependent part of a plan: the level tasks dealt to W workers.
+struct Schedule {
+    int W = 0;
+    std::vector<int> taskA, ptrA;   // entry tasks (4 ints) and per-(level, worker) ranges
+    std::vector<int> scl, ptrB;     // L scalings (2 ints)
+    std::vector<int> taskC, ptrC;   // backward substitution tasks (4 ints)
+    std::vector<int> level_work;    // per level: max worker load
+};
+
 struct Plan {
     int n = 0;    // buses
     int nnzY = 0;
@@ -54,6 +70,8 @@ struct Plan {
     std::vector<int> taskC;         // backward: 4 ints: row, diag block, p0, p1
     std::vector<int> ptrC;          // nblev*W + 1
     std::vector<int> pairs;         // 2 ints per pair
+    // undealt tasks (entry, scale, backward), kept so other worker counts can be scheduled
+    std::vector<PlanTask> tasksA, tasksB, tasksC;
     // statistics
     long long n_factor_pairs = 0, n_fwd_pairs = 0, n_bwd_pairs = 0;
     double rcond0 = 0.0;            // pivot ratio of the flat-start factorization
@@ -63,6 +81,9 @@ struct Plan {
 // Build everything topology-only. Returns an empty string on success, else the error.
 std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, const int* pv, int npv,
                        const int* pq, int npq, int workers);
+
+// Deal the plan's tasks to `workers` workers (longest first onto the least-loaded one).
+void make_schedule(const Plan& p, int workers, Schedule& out);
 
 // Host replica of the device algorithm (double precision): Jacobian blocks at (Vm, Va)
 // written to `blocks` (nblk*4, zero where not in the Jacobian) and residual R (nv*2).

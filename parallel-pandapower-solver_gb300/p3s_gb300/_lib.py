@@ -66,6 +66,7 @@ class Stats(C.Structure):
         ("cases_per_cta", C.c_int),
         ("kernel_ms", C.c_double),
         ("call_ms", C.c_double),
+        ("threads_per_cta", C.c_int),
     ]
 
 
@@ -81,6 +82,8 @@ SIGNATURES = {
     "gbpf_get_info": (C.c_int, [_vp, C.POINTER(Info)]),
     "gbpf_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_get_posmap": (C.c_int, [_vp, _ip]),
+    "gbpf_get_shape": (C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "gbpf_set_shape": (C.c_int, [_vp, C.c_longlong, C.c_int, C.c_int]),
     "gbpf_get_row_of_bus": (C.c_int, [_vp, _ip]),
     "gbpf_solve_batch": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.POINTER(Params), _dp, _ip, _bp]),
     "gbpf_solve_batch_device": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.POINTER(Params), _vp, _vp,

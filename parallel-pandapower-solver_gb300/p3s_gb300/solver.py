@@ -95,6 +95,17 @@ class GpuSolver:
         _lib.check(_lib.load().gbpf_get_stats(self._h, C.byref(o)), "gbpf_get_stats")
         return {f: getattr(o, f) for f, _ in o._fields_}
 
+    def shape(self, units: int):
+        """(threads per CTA, case slots per CTA) launched for a batch of `units` work items."""
+        nt, g = C.c_int(), C.c_int()
+        _lib.check(_lib.load().gbpf_get_shape(self._h, int(units), C.byref(nt), C.byref(g)), "gbpf_get_shape")
+        return nt.value, g.value
+
+    def set_shape(self, units: int, threads_per_cta: int, cases_per_cta: int):
+        """Pin the CTA shape for batches of `units`' size class (0, 0 restores the rule)."""
+        _lib.check(_lib.load().gbpf_set_shape(self._h, int(units), int(threads_per_cta), int(cases_per_cta)),
+                   "gbpf_set_shape")
+
     def posmap(self) -> np.ndarray:
         out = np.empty(self.nnz, dtype=np.int32)
         _lib.check(_lib.load().gbpf_get_posmap(self._h, _lib.i32(out)))

@@ -358,3 +358,29 @@ def test_n1_sweep_of_the_2000_bus_grid(grid2000):
     tight = osolver.solve_batch_contingency(np.abs(Yx), np.angle(Yx), g.Sbus, V0, pin, tol=1e-12)
     assert np.array_equal(mixed.converged, ok) and tight["converged"].all()
     assert np.nanmax(np.abs(mixed.V - np.where(s_sv, tight["V"], np.nan))) < 1e-9
+
+
+def test_results_do_not_depend_on_the_cta_shape(grid2000):
+    """Every CTA shape runs the same arithmetic per case: the batch-size rule, a pinned
+    shape and the autotuner change only the speed, never a bit of the result."""
+    from p3s_gb300.autotune import tune_lanes
+    from p3s_gb300.solver import GpuSolver
+
+    g = grid2000
+    S = timeseries_injections(g, 96)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    off = lanes(96, 96)
+    assert s.shape(1) == (1024, 1) and s.shape(8760) == (512, 32)
+    for prec in ("double", "mixed"):
+        p = GpuSolver.params(precision=prec)
+        base = s.solve_lanes(S, g.V0, off, p)
+        for nt, slots in ((1024, 4), (512, 8), (256, 16), (512, 32)):
+            s.set_shape(96, nt, slots)
+            assert s.shape(96) == (nt, slots)
+            r = s.solve_lanes(S, g.V0, off, p)
+            assert s.stats["threads_per_cta"] == nt and s.stats["cases_per_cta"] == slots
+            assert np.array_equal(r["V"], base["V"]) and np.array_equal(r["iterations"], base["iterations"])
+        s.set_shape(96, 0, 0)
+    choice, timings = tune_lanes(s, S, g.V0, off, GpuSolver.params(precision="mixed"),
+                                 candidates=((1024, 2), (512, 4)), reps=1)
+    assert s.shape(96) == choice and set(timings) == {(1024, 2), (512, 4)}
