@@ -146,6 +146,40 @@ int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d);
 void* gbpf_host_alloc(size_t bytes);
 void gbpf_host_free(void* p);
 
+/* ------------------------------------------------------------------ several topologies
+ * One launch of the persistent kernel over jobs of different topologies (grids of uneven
+ * size, requests of a serving loop): CTAs serve the jobs largest first, each job until its
+ * cases run out, so short jobs fill the tail of long ones. A group owns the launch's
+ * stream, scratch and staging buffers; the solvers lend their plans (no call on a solver
+ * may overlap a group launch that uses it). No reference counterpart: the reference solves
+ * one topology per call (nr_polar_solver.py:466-596). */
+typedef struct gbpf_group gbpf_group;
+
+typedef struct gbpf_job {
+    gbpf_solver* solver;     /* the topology */
+    int n_cases;
+    const double* S;         /* (n, n_cases) complex (s_per_col = 1) or (n,) */
+    int s_per_col;
+    const double* V0;        /* (n, n_cases) (v0_per_col = 1) or (n,) */
+    int v0_per_col;
+    const uint8_t* pin;      /* (n, n_cases) or NULL */
+    const int32_t* st_ptr;   /* outage stamps (gbpf_solve_contingency) or NULL */
+    const int32_t* st_k;
+    const double* st_val;
+    double* V;               /* out: (n, n_cases) complex */
+    int32_t* iterations;     /* out: (n_cases,) */
+    uint8_t* converged;      /* out: (n_cases,) */
+} gbpf_job;
+
+gbpf_group* gbpf_group_create(void);
+void gbpf_group_destroy(gbpf_group* g);
+/* Host arrays: staged to the device, one launch, results copied back. */
+int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* p);
+/* Device arrays (every pointer of every job on the device). */
+int gbpf_group_solve_device(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* p);
+/* Counters of the last group launch (summed over its jobs). */
+int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
+
 /* Islanding of N-1 cases on the device (case_generator.py:355-430 semantics).
  * Graph: n buses, m branches (f[e], t[e]); live[e] != 0 if the branch couples its ends.
  * Case c removes branches out_idx[out_ptr[c] .. out_ptr[c+1]). Labels are the connected

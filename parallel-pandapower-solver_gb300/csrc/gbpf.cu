@@ -23,6 +23,7 @@
 namespace {
 
 thread_local std::string g_err;
+thread_local cudaError_t g_copy_error = cudaSuccess;
 
 int fail(const std::string& m) {
     g_err = m;
@@ -76,6 +77,30 @@ int ilog2(int g) {
 
 void gbpf::set_error(const std::string& msg) { g_err = msg; }
 
+gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool mixed) {
+    ScratchOffsets o{};
+    unsigned long long at = 0;
+    auto take = [&](unsigned long long bytes) {
+        const unsigned long long p = at;
+        at += (bytes + 255) & ~255ULL;
+        return p;
+    };
+    const unsigned long long g = (unsigned long long)G;
+    o.fac64 = take((unsigned long long)nblk * g * 32);
+    o.fac32 = mixed ? take((unsigned long long)nblk * g * 16) : ~0ULL;
+    o.R = take((unsigned long long)nv * g * 16);
+    o.y64 = take((unsigned long long)nv * g * 16);
+    o.y32 = mixed ? take((unsigned long long)nv * g * 8) : ~0ULL;
+    o.Vc = take((unsigned long long)n * g * 32);
+    o.Vt = take((unsigned long long)n * g * 32);
+    o.Et = take((unsigned long long)n * g * 16);
+    o.Ei = take((unsigned long long)n * g * 8);
+    o.V32 = take((unsigned long long)n * g * 16);
+    o.pin = take((unsigned long long)n * g);
+    o.total = at;
+    return o;
+}
+
 // One CTA shape of the Newton kernel for a topology: threads per CTA, case slots per CTA,
 // and the factorization schedule dealt to its NT / G workers (built on first use).
 struct Shape {
@@ -103,18 +128,16 @@ struct gbpf_solver {
     // topology on the device
     DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos;
     gbpf::DevPlan dp{};  // topology part (schedule fields filled per shape)
-    // scratch (case slots, grow-only)
-    DBuf fac64, fac32, R, y64, y32, Vc, Vt, Et, Ei, V32, spin;
-    size_t sc_slots = 0;
-    bool sc_mixed = false;
+    // scratch: one region per CTA (grow-only)
+    DBuf scr;
     // per-call buffers (grow-only)
-    DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab;
+    DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab, bjobs;
     gbpf_stats last{};
     ~gbpf_solver() {
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
-                        &ddpos, &fac64, &fac32, &R, &y64, &y32, &Vc, &Vt, &Et, &Ei, &V32, &spin, &bS, &bV0, &bV, &bit,
-                        &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin, &btab})
+                        &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
+                        &btab, &bjobs})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -296,49 +319,8 @@ int upload_plan(gbpf_solver* s) {
     return 0;
 }
 
-// Scratch for `slots` case slots (CTAs x slots per CTA; laid out per CTA, [item][slot]).
-int ensure_scratch(gbpf_solver* s, size_t slots, bool mixed) {
-    if (slots <= s->sc_slots && (!mixed || s->sc_mixed)) return 0;
-    slots = std::max(slots, s->sc_slots);
-    mixed = mixed || s->sc_mixed;
-    const size_t nb = s->plan.nblk, nv = std::max(1, s->plan.nv), n = s->n;
-    CK(s->fac64.ensure(slots * nb * 32));
-    CK(s->R.ensure(slots * nv * 16));
-    CK(s->y64.ensure(slots * nv * 16));
-    CK(s->Vc.ensure(slots * n * 32));
-    CK(s->Vt.ensure(slots * n * 32));
-    CK(s->Et.ensure(slots * n * 16));
-    CK(s->Ei.ensure(slots * n * 8));
-    CK(s->V32.ensure(slots * n * 16));
-    CK(s->spin.ensure(slots * n));
-    if (mixed) {
-        CK(s->fac32.ensure(slots * nb * 16));
-        CK(s->y32.ensure(slots * nv * 8));
-    }
-    s->sc_slots = slots;
-    s->sc_mixed = mixed;
-    return 0;
-}
-
-gbpf::Scratch scratch_view(gbpf_solver* s, const Shape& sh) {
-    gbpf::Scratch sc{};
-    sc.G = sh.G;
-    sc.log2G = sh.lg;
-    sc.blk_stride = (size_t)s->plan.nblk * sh.G;
-    sc.row_stride = (size_t)std::max(1, s->plan.nv) * sh.G;
-    sc.bus_stride = (size_t)s->n * sh.G;
-    sc.fac64 = s->fac64.as<double4_32a>();
-    sc.fac32 = s->sc_mixed ? s->fac32.as<float4>() : nullptr;
-    sc.R = s->R.as<double2>();
-    sc.y64 = s->y64.as<double2>();
-    sc.y32 = s->sc_mixed ? s->y32.as<float2>() : nullptr;
-    sc.Vc = s->Vc.as<double4_32a>();
-    sc.Vt = s->Vt.as<double4_32a>();
-    sc.Et = s->Et.as<double2>();
-    sc.Ei = s->Ei.as<double>();
-    sc.V32 = s->V32.as<float4>();
-    sc.pin = s->spin.as<uint8_t>();
-    return sc;
+gbpf::ScratchOffsets solver_offsets(const gbpf_solver* s, int G, bool mixed) {
+    return gbpf::scratch_offsets(s->n, std::max(1, s->plan.nv), s->plan.nblk, G, mixed);
 }
 
 gbpf_params default_params() {
@@ -372,21 +354,34 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     if (int rc = get_shape(s, NT, G, &sh)) return rc;
     const long long want = (units + G - 1) / G;
     const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)s->nsm * sh->occ));
-    if (int rc = ensure_scratch(s, (size_t)grid * G, b.mixed != 0)) return rc;
+    gbpf::Job job{};
+    job.P = sh->dp;
+    job.off = solver_offsets(s, G, b.mixed != 0);
+    CK(s->scr.ensure((size_t)grid * job.off.total));
     CK(s->bctl.ensure(64 * sizeof(unsigned long long)));
     auto* ctl = s->bctl.as<unsigned long long>();
     CK(cudaMemsetAsync(ctl, 0, 64 * sizeof(unsigned long long), s->stream));
     b.counter = reinterpret_cast<int*>(ctl + 16);
     b.stats = ctl;
     b.err = reinterpret_cast<int*>(ctl + 24);
-    gbpf::Scratch sc = scratch_view(s, *sh);
-    CK(cudaEventRecord(s->e0, s->stream));
     if (b.v0_shared) {
         CK(s->btab.ensure((size_t)s->n * 64));
         b.v0tab = s->btab.as<double4_32a>();
-        CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, s->btab.as<double4_32a>(), b.err, s->stream));
     }
-    CK(gbpf::launch_newton(sh->dp, b, sc, grid, NT, s->stream));
+    job.B = b;
+    CK(s->bjobs.ensure(sizeof(gbpf::Job)));
+    CK(cudaMemcpyAsync(s->bjobs.p, &job, sizeof job, cudaMemcpyHostToDevice, s->stream));
+    gbpf::Launch L{};
+    L.jobs = s->bjobs.as<gbpf::Job>();
+    L.njobs = 1;
+    L.G = G;
+    L.log2G = ilog2(G);
+    L.scratch = s->scr.as<char>();
+    L.cta_bytes = job.off.total;
+    CK(cudaEventRecord(s->e0, s->stream));
+    if (b.v0_shared)
+        CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, s->btab.as<double4_32a>(), b.err, s->stream));
+    CK(gbpf::launch_newton(L, grid, NT, s->stream));
     CK(cudaEventRecord(s->e1, s->stream));
     unsigned long long host_ctl[32];
     CK(cudaMemcpyAsync(host_ctl, ctl, sizeof host_ctl, cudaMemcpyDeviceToHost, s->stream));
@@ -433,6 +428,173 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
+}
+
+// Shape rule for a launch over several topologies: the batch-size rule of choose_shape on
+// the total work, capped by the largest topology.
+void group_shape(int nsm, long long units, int max_nv, int* NT, int* G) {
+    const int cap = max_nv <= 4096 ? 64 : (max_nv <= 16384 ? 32 : 16);
+    const long long share = (units + nsm - 1) / nsm;
+    int per_sm = 1;
+    while (per_sm < share && per_sm < cap) per_sm *= 2;
+    *NT = per_sm <= 4 ? 1024 : 512;
+    *G = std::min(gbpf::MAX_SLOTS, std::max(1, per_sm / (1024 / *NT)));
+}
+
+}  // namespace
+
+// A launch context for several topologies at once: its own stream, scratch, control blocks
+// and staging buffers. The topologies (gbpf_solver) keep their plans; a group launch borrows
+// them and must not overlap a call on the same solver.
+struct gbpf_group {
+    int device = 0, nsm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
+    DBuf scr, bjobs, bctl, btab, bin, bout;
+    gbpf_stats last{};
+    ~gbpf_group() {
+        for (DBuf* b : {&scr, &bjobs, &bctl, &btab, &bin, &bout}) b->release();
+        for (cudaEvent_t e : {e0, e1, c0, c1})
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// One launch over `nj` jobs whose inputs and outputs are device pointers.
+int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p, const char* who) {
+    long long units = 0;
+    int max_nv = 1;
+    for (int j = 0; j < nj; ++j) {
+        const gbpf_job& J = jobs[j];
+        if (!J.solver) return fail(std::string(who) + ": job without a solver");
+        if (J.n_cases <= 0) return fail(std::string(who) + ": job " + std::to_string(j) + " has no cases");
+        if (!J.S || !J.V0 || !J.V || !J.iterations || !J.converged)
+            return fail(std::string(who) + ": job " + std::to_string(j) + " lacks an input or output array");
+        units += J.n_cases;
+        max_nv = std::max(max_nv, J.solver->plan.nv);
+    }
+    int NT = 0, G = 0;
+    group_shape(g->nsm, units, max_nv, &NT, &G);
+    const bool mixed = p.precision == 1;
+    // largest work first, so the long jobs start early and the short ones fill the tail
+    std::vector<int> order(nj);
+    for (int j = 0; j < nj; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const double wa = (double)jobs[a].n_cases * jobs[a].solver->plan.nblk;
+        const double wb = (double)jobs[b].n_cases * jobs[b].solver->plan.nblk;
+        return wa > wb;
+    });
+    std::vector<gbpf::Job> hj(nj);
+    unsigned long long cta_bytes = 0;
+    long long want = 0;
+    int occ = 1 << 20;
+    size_t tab_bytes = 0;
+    for (int j = 0; j < nj; ++j) tab_bytes += jobs[j].v0_per_col ? 0 : (size_t)jobs[j].solver->n * 64;
+    CK(g->bctl.ensure((size_t)nj * 32 * sizeof(unsigned long long)));
+    CK(g->btab.ensure(std::max<size_t>(tab_bytes, 64)));
+    auto* ctl = g->bctl.as<unsigned long long>();
+    CK(cudaMemsetAsync(ctl, 0, (size_t)nj * 32 * sizeof(unsigned long long), g->stream));
+    size_t tab_at = 0;
+    for (int q = 0; q < nj; ++q) {
+        const int j = order[q];
+        const gbpf_job& J = jobs[j];
+        gbpf_solver* s = J.solver;
+        Shape* sh = nullptr;
+        if (int rc = get_shape(s, NT, G, &sh)) return rc;
+        occ = std::min(occ, sh->occ);
+        gbpf::Job& o = hj[q];
+        o.P = sh->dp;
+        o.off = solver_offsets(s, G, mixed);
+        cta_bytes = std::max(cta_bytes, o.off.total);
+        want += (J.n_cases + G - 1) / G;
+        gbpf::Batch b{};
+        b.B = J.n_cases;
+        b.S = reinterpret_cast<const double2*>(J.S);
+        b.s_shared = !J.s_per_col;
+        b.sS = J.n_cases;
+        b.V0 = reinterpret_cast<const double2*>(J.V0);
+        b.v0_shared = !J.v0_per_col;
+        b.sV0 = J.n_cases;
+        if (b.v0_shared) {
+            b.v0tab = reinterpret_cast<double4_32a*>(g->btab.as<char>() + tab_at);
+            tab_at += (size_t)s->n * 64;
+        }
+        if (J.pin) {
+            b.pin = J.pin;
+            b.spin = J.n_cases;
+        }
+        if (J.st_ptr) {
+            b.ymode = 1;
+            b.st_ptr = J.st_ptr;
+            b.st_k = J.st_k;
+            b.st_v = reinterpret_cast<const double2*>(J.st_val);
+        }
+        b.Vout = reinterpret_cast<double2*>(J.V);
+        b.sV = J.n_cases;
+        b.iters = J.iterations;
+        b.conv = J.converged;
+        fill_common(b, s, p);
+        unsigned long long* c = ctl + (size_t)q * 32;
+        b.counter = reinterpret_cast<int*>(c + 16);
+        b.stats = c;
+        b.err = reinterpret_cast<int*>(c + 24);
+        o.B = b;
+    }
+    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)g->nsm * occ));
+    CK(g->scr.ensure((size_t)grid * cta_bytes));
+    CK(g->bjobs.ensure((size_t)nj * sizeof(gbpf::Job)));
+    CK(cudaMemcpyAsync(g->bjobs.p, hj.data(), (size_t)nj * sizeof(gbpf::Job), cudaMemcpyHostToDevice, g->stream));
+    gbpf::Launch L{};
+    L.jobs = g->bjobs.as<gbpf::Job>();
+    L.njobs = nj;
+    L.G = G;
+    L.log2G = ilog2(G);
+    L.scratch = g->scr.as<char>();
+    L.cta_bytes = cta_bytes;
+    CK(cudaEventRecord(g->e0, g->stream));
+    for (int q = 0; q < nj; ++q) {
+        const gbpf::Batch& b = hj[q].B;
+        if (b.v0_shared)
+            CK(gbpf::launch_v0_table(b.V0, hj[q].P.n, b.check_v0, const_cast<double4_32a*>(b.v0tab), b.err,
+                                     g->stream));
+    }
+    CK(gbpf::launch_newton(L, grid, NT, g->stream));
+    CK(cudaEventRecord(g->e1, g->stream));
+    std::vector<unsigned long long> hc((size_t)nj * 32);
+    CK(cudaMemcpyAsync(hc.data(), ctl, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, g->e0, g->e1));
+    gbpf_stats st{};
+    for (int q = 0; q < nj; ++q) {
+        const unsigned long long* c = hc.data() + (size_t)q * 32;
+        st.single_factorizations += c[0];
+        st.double_factorizations += c[1];
+        st.single_rejected += c[2];
+        st.double_rejected += c[3];
+        st.macro_steps += c[4];
+    }
+    st.grid = grid;
+    st.cases_per_cta = G;
+    st.threads_per_cta = NT;
+    st.kernel_ms = ms;
+    g->last = st;
+    for (int q = 0; q < nj; ++q) {
+        const int* err = reinterpret_cast<const int*>(hc.data() + (size_t)q * 32 + 24);
+        const std::string job = std::string(who) + ": job " + std::to_string(order[q]) + ": ";
+        if (err[0] == gbpf::DE_V0_NONFINITE)
+            return fail(job + "invalid initial voltage at bus " + std::to_string(err[1]) + ", step " +
+                        std::to_string(err[2]));
+        if (err[0] == gbpf::DE_V0_MAGNITUDE)
+            return fail(job + "invalid voltage magnitude at bus " + std::to_string(err[1]) + ", step " +
+                        std::to_string(err[2]));
+        if (err[0] == gbpf::DE_STAMPS)
+            return fail(job + "case " + std::to_string(err[2]) + " has " + std::to_string(err[1]) +
+                        " outage stamp entries, more than the " + std::to_string(gbpf::MAX_STAMPS) + " supported");
+    }
+    return 0;
 }
 
 }  // namespace
@@ -794,6 +956,116 @@ void* gbpf_host_alloc(size_t bytes) {
 
 void gbpf_host_free(void* p) {
     if (p) cudaFreeHost(p);
+}
+
+gbpf_group* gbpf_group_create(void) {
+    std::unique_ptr<gbpf_group> g(new gbpf_group);
+    auto ok = [&](cudaError_t e) {
+        if (e != cudaSuccess) fail(std::string("gbpf_group_create: ") + cudaGetErrorString(e));
+        return e == cudaSuccess;
+    };
+    if (!ok(cudaGetDevice(&g->device)) ||
+        !ok(cudaDeviceGetAttribute(&g->nsm, cudaDevAttrMultiProcessorCount, g->device)) ||
+        !ok(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || !ok(cudaEventCreate(&g->e0)) ||
+        !ok(cudaEventCreate(&g->e1)) || !ok(cudaEventCreate(&g->c0)) || !ok(cudaEventCreate(&g->c1)))
+        return nullptr;
+    return g.release();
+}
+
+void gbpf_group_destroy(gbpf_group* g) { delete g; }
+
+int gbpf_group_solve_device(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* pp) {
+    if (!g || !jobs || njobs <= 0) return fail("group_solve: no jobs");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (int rc = check_params(p, "group_solve")) return rc;
+    return group_run(g, njobs, jobs, p, "group_solve");
+}
+
+int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* pp) {
+    if (!g || !jobs || njobs <= 0) return fail("group_solve: no jobs");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (int rc = check_params(p, "group_solve")) return rc;
+    // stage every job's inputs in one device buffer and its outputs in another
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    std::vector<size_t> in_at(njobs), out_at(njobs);
+    size_t in_bytes = 0, out_bytes = 0;
+    for (int j = 0; j < njobs; ++j) {
+        const gbpf_job& J = jobs[j];
+        if (!J.solver || J.n_cases <= 0) return fail("group_solve: job " + std::to_string(j) + " is empty");
+        if (J.st_ptr) {
+            const int ne = J.st_ptr[J.n_cases];
+            for (int c = 0; c < J.n_cases; ++c)
+                if (J.st_ptr[c + 1] - J.st_ptr[c] > gbpf::MAX_STAMPS)
+                    return fail("group_solve: job " + std::to_string(j) + " case " + std::to_string(c) +
+                                " has more than " + std::to_string(gbpf::MAX_STAMPS) + " stamp entries");
+            for (int e = 0; e < ne; ++e)
+                if (J.st_k[e] < 0 || J.st_k[e] >= J.solver->nnz)
+                    return fail("group_solve: job " + std::to_string(j) + " stamp row out of range");
+        }
+        const size_t n = J.solver->n, T = J.n_cases;
+        in_at[j] = in_bytes;
+        in_bytes += up(n * (J.s_per_col ? T : 1) * 16) + up(n * (J.v0_per_col ? T : 1) * 16) + (J.pin ? up(n * T) : 0);
+        if (J.st_ptr) in_bytes += up((T + 1) * 4) + up((size_t)std::max(J.st_ptr[T], 1) * 4) +
+                                  up((size_t)std::max(J.st_ptr[T], 1) * 16);
+        out_at[j] = out_bytes;
+        out_bytes += up(n * T * 16) + up(T * 4) + up(T);
+    }
+    CK(g->bin.ensure(in_bytes));
+    CK(g->bout.ensure(out_bytes));
+    CK(cudaEventRecord(g->c0, g->stream));
+    std::vector<gbpf_job> dj(jobs, jobs + njobs);
+    for (int j = 0; j < njobs; ++j) {
+        const gbpf_job& J = jobs[j];
+        gbpf_job& D = dj[j];
+        const size_t n = J.solver->n, T = J.n_cases;
+        char* at = g->bin.as<char>() + in_at[j];
+        auto put = [&](const void* src, size_t bytes) -> void* {
+            void* dst = at;
+            at += up(bytes);
+            if (bytes) g_copy_error = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g->stream);
+            return dst;
+        };
+        g_copy_error = cudaSuccess;
+        D.S = static_cast<const double*>(put(J.S, n * (J.s_per_col ? T : 1) * 16));
+        CK(g_copy_error);
+        D.V0 = static_cast<const double*>(put(J.V0, n * (J.v0_per_col ? T : 1) * 16));
+        CK(g_copy_error);
+        if (J.pin) {
+            D.pin = static_cast<const uint8_t*>(put(J.pin, n * T));
+            CK(g_copy_error);
+        }
+        if (J.st_ptr) {
+            const size_t ne = (size_t)J.st_ptr[T];
+            D.st_ptr = static_cast<const int32_t*>(put(J.st_ptr, (T + 1) * 4));
+            D.st_k = static_cast<const int32_t*>(put(J.st_k, ne * 4));
+            D.st_val = static_cast<const double*>(put(J.st_val, ne * 16));
+            CK(g_copy_error);
+        }
+        char* o = g->bout.as<char>() + out_at[j];
+        D.V = reinterpret_cast<double*>(o);
+        D.iterations = reinterpret_cast<int32_t*>(o + up(n * T * 16));
+        D.converged = reinterpret_cast<uint8_t*>(o + up(n * T * 16) + up(T * 4));
+    }
+    if (int rc = group_run(g, njobs, dj.data(), p, "group_solve")) return rc;
+    for (int j = 0; j < njobs; ++j) {
+        const gbpf_job& J = jobs[j];
+        const size_t n = J.solver->n, T = J.n_cases;
+        CK(cudaMemcpyAsync(J.V, dj[j].V, n * T * 16, cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaMemcpyAsync(J.iterations, dj[j].iterations, T * 4, cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaMemcpyAsync(J.converged, dj[j].converged, T, cudaMemcpyDeviceToHost, g->stream));
+    }
+    CK(cudaEventRecord(g->c1, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, g->c0, g->c1));
+    g->last.call_ms = ms;
+    return 0;
+}
+
+int gbpf_group_stats(gbpf_group* g, gbpf_stats* out) {
+    if (!g || !out) return fail("null argument");
+    *out = g->last;
+    return 0;
 }
 
 }  // extern "C"

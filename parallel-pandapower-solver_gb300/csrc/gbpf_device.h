@@ -91,27 +91,46 @@ struct Batch {
     int* err;                // [0] code [1] bus [2] case
 };
 
-struct Scratch {
-    int G, log2G;
-    size_t blk_stride;       // per-CTA elements (blocks) of the factor arrays = nblk*G
-    size_t row_stride;       // nv*G
-    size_t bus_stride;       // n*G
-    double4_32a* fac64;          // [cta][blk][slot] (a00 a01 a10 a11)
-    float4* fac32;
-    double2* R;              // [cta][row][slot] residual (P, Q) = S - S(V)
-    double2* y64;            // [cta][row][slot] step
-    float2* y32;
-    double4_32a* Vc;             // committed point (Vm, Va, cos, sin)
-    double4_32a* Vt;             // evaluation point (Vm, Va, cos, sin)
-    double2* Et;             // evaluation point rectangular (e, f)
-    double* Ei;              // evaluation point 1 / Vm
-    float4* V32;             // evaluation point (e, f, 1 / Vm, 0) in float
-    uint8_t* pin;            // [cta][bus][slot]
+// Byte offsets of one job's scratch arrays inside a CTA's scratch region (G case slots;
+// every array is [item][slot]); ~0 for an array the job does not use.
+struct ScratchOffsets {
+    unsigned long long fac64;  // [blk][slot] double 2x2 blocks (a00 a01 a10 a11)
+    unsigned long long fac32;  // [blk][slot] float blocks (mixed precision)
+    unsigned long long R;      // [row][slot] residual (P, Q) = S - S(V)
+    unsigned long long y64;    // [row][slot] step
+    unsigned long long y32;
+    unsigned long long Vc;     // [bus][slot] committed point (Vm, Va, cos, sin)
+    unsigned long long Vt;     // [bus][slot] evaluation point (Vm, Va, cos, sin)
+    unsigned long long Et;     // [bus][slot] evaluation point rectangular (e, f)
+    unsigned long long Ei;     // [bus][slot] evaluation point 1 / Vm
+    unsigned long long V32;    // [bus][slot] evaluation point (e, f, 1 / Vm, 0) in float
+    unsigned long long pin;    // [bus][slot]
+    unsigned long long total;  // bytes of the job's region
 };
 
+// One job of a launch: a topology's plan (with the schedule of the launch's CTA shape), a
+// batch of its cases, and where its scratch sits in a CTA's region.
+struct Job {
+    DevPlan P;
+    Batch B;
+    ScratchOffsets off;
+};
+
+// A launch of the persistent Newton kernel: CTAs serve the jobs in order, each job until its
+// cases run out; every CTA owns `cta_bytes` of scratch, reused job after job.
+struct Launch {
+    const Job* jobs;         // device array
+    int njobs;
+    int G, log2G;            // case slots per CTA
+    char* scratch;
+    unsigned long long cta_bytes;
+};
+
+// Scratch layout of a job with n buses, nv block rows, nblk blocks and G slots.
+ScratchOffsets scratch_offsets(int n, int nv, int nblk, int G, bool mixed);
+
 // host-side launchers (gbpf_kernels.cu)
-cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
-                          cudaStream_t stream);
+cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream);
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
                               double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
                               double2* R, cudaStream_t stream);

@@ -488,22 +488,56 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 // every variant): smaller CTAs let one CTA's latency-bound factorization overlap another's
 // double-precision evaluation on the same SM.
 template <int NTB>
-__global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const DevPlan P, const Batch Bt, const Scratch Sc) {
-    const int G = Sc.G, lg = Sc.log2G;
+__global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L) {
+    const int G = L.G, lg = L.log2G;
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
-    const size_t cta = blockIdx.x;
-    double4_32a* fac64 = Sc.fac64 ? Sc.fac64 + cta * Sc.blk_stride : nullptr;
-    float4* fac32 = Sc.fac32 ? Sc.fac32 + cta * Sc.blk_stride : nullptr;
-    double2* R = Sc.R + cta * Sc.row_stride;
-    double2* y64 = Sc.y64 + cta * Sc.row_stride;
-    float2* y32 = Sc.y32 ? Sc.y32 + cta * Sc.row_stride : nullptr;
-    double4_32a* Vc = Sc.Vc + cta * Sc.bus_stride;
-    double4_32a* Vt = Sc.Vt + cta * Sc.bus_stride;
-    double2* Et = Sc.Et + cta * Sc.bus_stride;
-    double* Ei = Sc.Ei + cta * Sc.bus_stride;
-    float4* V32 = Sc.V32 + cta * Sc.bus_stride;
-    uint8_t* spin = Sc.pin + cta * Sc.bus_stride;
+    char* const region = L.scratch + (size_t)blockIdx.x * L.cta_bytes;
+    __shared__ DevPlan s_plan;
+    __shared__ Batch s_batch;
+    __shared__ int s_job;
+    int next_job = 0;  // thread 0: first job this CTA has not finished yet
+    for (;;) {
+    // ------------------------------------------------------------------ bind the next job
+    // Jobs are taken in order; a job is open while its work counter is below its units.
+    // Every CTA that finds a job open serves it until the job runs out of cases.
+    if (tid == 0) {
+        int sel = -1;
+        for (; next_job < L.njobs; ++next_job) {
+            const Batch& b = L.jobs[next_job].B;
+            if (*(volatile const int*)b.counter < (b.lanes ? b.K : b.B)) {
+                sel = next_job++;
+                break;
+            }
+        }
+        s_job = sel;
+    }
+    __syncthreads();
+    const int job = s_job;
+    if (job < 0) break;
+    {
+        const int* src = reinterpret_cast<const int*>(&L.jobs[job].P);
+        int* dst = reinterpret_cast<int*>(&s_plan);
+        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = src[w];
+        src = reinterpret_cast<const int*>(&L.jobs[job].B);
+        dst = reinterpret_cast<int*>(&s_batch);
+        for (int w = tid; w < (int)(sizeof(Batch) / 4); w += NT) dst[w] = src[w];
+    }
+    const ScratchOffsets& off = L.jobs[job].off;
+    double4_32a* fac64 = reinterpret_cast<double4_32a*>(region + off.fac64);
+    float4* fac32 = off.fac32 != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32) : nullptr;
+    double2* R = reinterpret_cast<double2*>(region + off.R);
+    double2* y64 = reinterpret_cast<double2*>(region + off.y64);
+    float2* y32 = off.y32 != ~0ULL ? reinterpret_cast<float2*>(region + off.y32) : nullptr;
+    double4_32a* Vc = reinterpret_cast<double4_32a*>(region + off.Vc);
+    double4_32a* Vt = reinterpret_cast<double4_32a*>(region + off.Vt);
+    double2* Et = reinterpret_cast<double2*>(region + off.Et);
+    double* Ei = reinterpret_cast<double*>(region + off.Ei);
+    float4* V32 = reinterpret_cast<float4*>(region + off.V32);
+    uint8_t* spin = reinterpret_cast<uint8_t*>(region + off.pin);
+    __syncthreads();
+    const DevPlan& P = s_plan;
+    const Batch& Bt = s_batch;
     const int n = P.n;
     const int nG = n << lg;
 
@@ -884,6 +918,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const DevPlan P
         }
         __syncthreads();
     }
+    }  // jobs
 }
 
 // Start-state table of a shared start voltage: per bus (Vm, Va, cos, sin) and (e, f, 1/Vm, 0),
@@ -953,14 +988,13 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
     }
 }
 
-cudaError_t launch_newton(const DevPlan& P, const Batch& B, const Scratch& S, int grid, int threads,
-                          cudaStream_t stream) {
+cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream) {
     if (threads == 1024)
-        newton_kernel<1024><<<grid, 1024, 0, stream>>>(P, B, S);
+        newton_kernel<1024><<<grid, 1024, 0, stream>>>(L);
     else if (threads == 512)
-        newton_kernel<512><<<grid, 512, 0, stream>>>(P, B, S);
+        newton_kernel<512><<<grid, 512, 0, stream>>>(L);
     else if (threads == 256)
-        newton_kernel<256><<<grid, 256, 0, stream>>>(P, B, S);
+        newton_kernel<256><<<grid, 256, 0, stream>>>(L);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();

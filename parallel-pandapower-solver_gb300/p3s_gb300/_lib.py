@@ -70,6 +70,26 @@ class Stats(C.Structure):
     ]
 
 
+class Job(C.Structure):
+    """struct gbpf_job (one topology's cases in a group launch)."""
+
+    _fields_ = [
+        ("solver", _vp),
+        ("n_cases", C.c_int),
+        ("S", _vp),
+        ("s_per_col", C.c_int),
+        ("V0", _vp),
+        ("v0_per_col", C.c_int),
+        ("pin", _vp),
+        ("st_ptr", _vp),
+        ("st_k", _vp),
+        ("st_val", _vp),
+        ("V", _vp),
+        ("iterations", _vp),
+        ("converged", _vp),
+    ]
+
+
 # exported symbols and their signatures (restype, argtypes)
 SIGNATURES = {
     "gbpf_last_error": (C.c_char_p, []),
@@ -100,6 +120,11 @@ SIGNATURES = {
                                      _dp, _dp, _ip, C.c_char_p, C.c_int]),
     "gbpf_islands": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                _ip, _ip]),
+    "gbpf_group_create": (_vp, []),
+    "gbpf_group_destroy": (None, [_vp]),
+    "gbpf_group_solve": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
+    "gbpf_group_solve_device": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
+    "gbpf_group_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_islands_device_static": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, _vp,
                                              _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -1,0 +1,99 @@
+"""Several topologies in one launch of the persistent Newton kernel (include/gbpf.h group API).
+
+A ``GpuGroup`` owns a stream, scratch and staging buffers; ``solve`` takes one job per
+topology (a ``GpuSolver`` and its cases) and runs them all in ONE launch, largest job first,
+so grids of uneven size and the requests of a serving loop share the device instead of
+queueing behind each other. Per case the arithmetic is the single-topology solve's, so
+every result equals the one ``GpuSolver`` returns for the same case (bit for bit).
+No reference counterpart: the reference solves one topology per call.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .solver import GpuSolver, c128
+
+
+@dataclass
+class GroupJob:
+    """One topology's cases. S: (n, T) or (n,) with T from V0; V0: (n,) or (n, T); pin: (n, T)
+    or None; stamps: (ptr (T+1,), k, val) outage stamps subtracted from the base Ybus, or None."""
+
+    solver: GpuSolver
+    S: np.ndarray
+    V0: np.ndarray
+    n_cases: int = 0
+    pin: np.ndarray | None = None
+    stamps: tuple | None = None
+
+
+class GpuGroup:
+    def __init__(self):
+        L = _lib.require_device()
+        h = L.gbpf_group_create()
+        if not h:
+            raise RuntimeError(_lib.last_error())
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().gbpf_group_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def stats(self) -> dict:
+        o = _lib.Stats()
+        _lib.check(_lib.load().gbpf_group_stats(self._h, C.byref(o)), "gbpf_group_stats")
+        return {f: getattr(o, f) for f, _ in o._fields_}
+
+    def solve(self, jobs: list[GroupJob], params: _lib.Params) -> list[dict]:
+        arr = (_lib.Job * len(jobs))()
+        keep = []
+        outs = []
+        for i, jb in enumerate(jobs):
+            n = jb.solver.n
+            S = c128(jb.S)
+            V0 = c128(jb.V0)
+            T = jb.n_cases or (S.shape[1] if S.ndim == 2 else (V0.shape[1] if V0.ndim == 2 else 1))
+            if S.shape not in ((n, T), (n,)) or V0.shape not in ((n, T), (n,)):
+                raise ValueError(f"job {i}: S / V0 must be (n_bus, T) or (n_bus,)")
+            V = np.empty((n, T), dtype=np.complex128)
+            it = np.empty(T, dtype=np.int32)
+            cv = np.empty(T, dtype=np.uint8)
+            J = arr[i]
+            J.solver = jb.solver._h
+            J.n_cases = T
+            J.S = S.ctypes.data
+            J.s_per_col = int(S.ndim == 2)
+            J.V0 = V0.ctypes.data
+            J.v0_per_col = int(V0.ndim == 2)
+            keep += [S, V0]
+            if jb.pin is not None:
+                pin = np.ascontiguousarray(jb.pin, dtype=np.uint8)
+                if pin.shape != (n, T):
+                    raise ValueError(f"job {i}: pin must be (n_bus, T)")
+                J.pin = pin.ctypes.data
+                keep.append(pin)
+            if jb.stamps is not None:
+                ptr, k, val = jb.stamps
+                ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+                k = np.ascontiguousarray(k, dtype=np.int32)
+                val = c128(val)
+                if ptr.shape != (T + 1,):
+                    raise ValueError(f"job {i}: stamp pointers must be (T + 1,)")
+                J.st_ptr, J.st_k, J.st_val = ptr.ctypes.data, k.ctypes.data, val.ctypes.data
+                keep += [ptr, k, val]
+            J.V, J.iterations, J.converged = V.ctypes.data, it.ctypes.data, cv.ctypes.data
+            outs.append((V, it, cv))
+        rc = _lib.load().gbpf_group_solve(self._h, len(jobs), arr, C.byref(params))
+        _lib.check(rc, "group_solve")
+        return [{"V": V, "iterations": it, "converged": cv.astype(bool)} for V, it, cv in outs]

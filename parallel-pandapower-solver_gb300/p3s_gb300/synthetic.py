@@ -178,6 +178,7 @@ def make_grid(
     seed: int = 0,
     gen_scale: float = 1.03,
     max_angle_deg: float = 20.0,
+    charging_scale: float | None = None,
 ) -> Grid:
     """A synthetic meshed grid (see the module docstring for the recipe)."""
     rng = np.random.default_rng(seed)
@@ -194,9 +195,25 @@ def make_grid(
     x = 0.02 + 0.3 * length
     r = x * rng.uniform(0.1, 0.4, nbr)
     b = rng.uniform(0.0, 0.05, nbr)
+    if charging_scale is None:
+        # charging is drawn per branch whatever its length; on grids of more than 2,000
+        # buses (branches ever shorter, injections scaled down with the DC angle spread)
+        # it is scaled so the total stays that of a 2,000-bus grid -- otherwise the lines'
+        # reactive generation swamps the loads and the grid has no AC solution
+        charging_scale = min(1.0, 2000.0 / n)
+    if charging_scale != 1.0:
+        b = b * charging_scale
     tap = np.ones(nbr)
     tr = rng.choice(nbr, size=n_trafo, replace=False) if n_trafo else np.zeros(0, dtype=int)
     tap[tr] = rng.uniform(0.95, 1.05, len(tr))
+    if n > 2000:
+        # lines get shorter as the unit square fills up, but a transformer's leakage
+        # reactance does not: on grids of more than 2,000 buses transformers get at least
+        # 0.1 pu, else off-nominal taps on near-zero impedances drive circulating reactive
+        # flows of several pu around every mesh and the grid has no AC solution; their
+        # off-nominal ratios spread less for the same reason
+        x[tr] = np.maximum(x[tr], 0.1)
+        tap[tr] = 1.0 + (tap[tr] - 1.0) * (2000.0 / n)
     y = 1.0 / (r + 1j * x)
     ysh = 0.5j * b
     stamp = np.empty((nbr, 4), dtype=np.complex128)
@@ -217,6 +234,11 @@ def make_grid(
     vm_set = np.ones(n)
     vm_set[slack] = 1.04
     vm_set[pv] = rng.uniform(0.98, 1.05, n_pv)
+    if n > 2000:
+        # generator set points spread less on denser grids: two PV buses a short line apart
+        # holding set points 0.07 pu apart exchange reactive power ~ 0.07 / x, which grows
+        # without bound as the lines shorten
+        vm_set[pv] = 1.015 + (vm_set[pv] - 1.015) * (2000.0 / n)
     p_load = np.zeros(n)
     q_load = np.zeros(n)
     p_load[pq] = rng.uniform(0.0, 0.6, len(pq))

@@ -384,3 +384,32 @@ def test_results_do_not_depend_on_the_cta_shape(grid2000):
     choice, timings = tune_lanes(s, S, g.V0, off, GpuSolver.params(precision="mixed"),
                                  candidates=((1024, 2), (512, 4)), reps=1)
     assert s.shape(96) == choice and set(timings) == {(1024, 2), (512, 4)}
+
+
+def test_uneven_grids_in_one_launch_match_their_own_solves():
+    """Grids of uneven size in ONE persistent launch (a group): every result equals the grid's
+    own single-topology solve bit for bit, and the double path matches the oracle."""
+    from p3s_gb300.group import GpuGroup, GroupJob
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.synthetic import make_grid, scenario_injections
+
+    rng = np.random.default_rng(11)
+    sizes = np.exp(rng.uniform(np.log(30), np.log(3000), 12)).astype(int)
+    grids = [make_grid(int(n), seed=100 + i) for i, n in enumerate(sizes)]
+    scen = [scenario_injections(g, 16, seed=200 + i) for i, g in enumerate(grids)]
+    solvers = [GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq) for g in grids]
+    grp = GpuGroup()
+    for prec in ("double", "mixed"):
+        p = GpuSolver.params(precision=prec)
+        res = grp.solve([GroupJob(s, S, g.V0) for s, S, g in zip(solvers, scen, grids)], p)
+        assert grp.stats["single_factorizations" if prec == "mixed" else "double_factorizations"] > 0
+        for s, S, g, r in zip(solvers, scen, grids, res):
+            alone = s.solve_batch(S, g.V0, p)
+            assert np.array_equal(r["V"], alone["V"]) and np.array_equal(r["iterations"], alone["iterations"])
+            assert np.array_equal(r["converged"], alone["converged"]) and r["converged"].all()
+        if prec == "double":
+            for i in (0, len(grids) // 2, len(grids) - 1):
+                g = grids[i]
+                ref = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(scen[i], g.V0)
+                assert np.array_equal(res[i]["iterations"], ref["iterations"])
+                assert np.abs(res[i]["V"] - ref["V"]).max() < TOL_V
