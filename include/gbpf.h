@@ -169,6 +169,7 @@ typedef struct gbpf_job {
     double* V;               /* out: (n, n_cases) complex */
     int32_t* iterations;     /* out: (n_cases,) */
     uint8_t* converged;      /* out: (n_cases,) */
+    int cases_per_cta;       /* 0: by the group rule (fewer for large grids), else a power of two <= 32 */
 } gbpf_job;
 
 gbpf_group* gbpf_group_create(void);
@@ -177,6 +178,9 @@ void gbpf_group_destroy(gbpf_group* g);
 int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* p);
 /* Device arrays (every pointer of every job on the device). */
 int gbpf_group_solve_device(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* p);
+/* Launch shape of later group launches: threads per CTA (0: by the batch-size rule) and the
+ * budget of variable buses x case slots a CTA holds per job (0: 8,192). */
+int gbpf_group_set_shape(gbpf_group* g, int threads_per_cta, int slot_budget);
 /* Counters of the last group launch (summed over its jobs). */
 int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
 

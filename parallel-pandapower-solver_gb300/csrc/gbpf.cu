@@ -357,6 +357,8 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     gbpf::Job job{};
     job.P = sh->dp;
     job.off = solver_offsets(s, G, b.mixed != 0);
+    job.G = G;
+    job.log2G = ilog2(G);
     CK(s->scr.ensure((size_t)grid * job.off.total));
     CK(s->bctl.ensure(64 * sizeof(unsigned long long)));
     auto* ctl = s->bctl.as<unsigned long long>();
@@ -374,8 +376,6 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     gbpf::Launch L{};
     L.jobs = s->bjobs.as<gbpf::Job>();
     L.njobs = 1;
-    L.G = G;
-    L.log2G = ilog2(G);
     L.scratch = s->scr.as<char>();
     L.cta_bytes = job.off.total;
     CK(cudaEventRecord(s->e0, s->stream));
@@ -430,15 +430,24 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
 }
 
-// Shape rule for a launch over several topologies: the batch-size rule of choose_shape on
-// the total work, capped by the largest topology.
-void group_shape(int nsm, long long units, int max_nv, int* NT, int* G) {
-    const int cap = max_nv <= 4096 ? 64 : (max_nv <= 16384 ? 32 : 16);
+// Shape rule for a launch over several topologies: threads per CTA by the batch-size rule of
+// choose_shape on the total work; case slots per CTA per job: the batch-size rule's count,
+// reduced for large topologies so that a job's CTA holds at most `slot_budget` (8,192)
+// variable buses' worth of cases -- a large grid's cases then get many workers each, and
+// they set the launch's critical path (measured on GB300, 256 grids of 30..19,423 buses x 16
+// scenarios: one slot per CTA for the largest grids halves the launch).
+void group_shape(int nsm, long long units, int* NT, int* Gmax) {
     const long long share = (units + nsm - 1) / nsm;
     int per_sm = 1;
-    while (per_sm < share && per_sm < cap) per_sm *= 2;
+    while (per_sm < share && per_sm < 64) per_sm *= 2;
     *NT = per_sm <= 4 ? 1024 : 512;
-    *G = std::min(gbpf::MAX_SLOTS, std::max(1, per_sm / (1024 / *NT)));
+    *Gmax = std::min(gbpf::MAX_SLOTS, std::max(1, per_sm / (1024 / *NT)));
+}
+
+int job_slots(int Gmax, int nv, int budget) {
+    int g = 1;
+    while (g * 2 <= Gmax && (long long)(g * 2) * std::max(1, nv) <= budget) g *= 2;
+    return g;
 }
 
 }  // namespace
@@ -452,6 +461,8 @@ struct gbpf_group {
     cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
     DBuf scr, bjobs, bctl, btab, bin, bout;
     gbpf_stats last{};
+    int fixed_NT = 0;              // threads per CTA (0: by the group rule)
+    int slot_budget = 8192;        // variable buses x case slots a CTA may hold per job
     ~gbpf_group() {
         for (DBuf* b : {&scr, &bjobs, &bctl, &btab, &bin, &bout}) b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
@@ -465,18 +476,19 @@ namespace {
 // One launch over `nj` jobs whose inputs and outputs are device pointers.
 int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p, const char* who) {
     long long units = 0;
-    int max_nv = 1;
     for (int j = 0; j < nj; ++j) {
         const gbpf_job& J = jobs[j];
         if (!J.solver) return fail(std::string(who) + ": job without a solver");
         if (J.n_cases <= 0) return fail(std::string(who) + ": job " + std::to_string(j) + " has no cases");
         if (!J.S || !J.V0 || !J.V || !J.iterations || !J.converged)
             return fail(std::string(who) + ": job " + std::to_string(j) + " lacks an input or output array");
+        if (J.cases_per_cta < 0 || J.cases_per_cta > gbpf::MAX_SLOTS || (J.cases_per_cta & (J.cases_per_cta - 1)))
+            return fail(std::string(who) + ": job " + std::to_string(j) + ": cases_per_cta must be 0 or a power of two in 1..32");
         units += J.n_cases;
-        max_nv = std::max(max_nv, J.solver->plan.nv);
     }
-    int NT = 0, G = 0;
-    group_shape(g->nsm, units, max_nv, &NT, &G);
+    int NT = 0, Gmax = 0;
+    group_shape(g->nsm, units, &NT, &Gmax);
+    if (g->fixed_NT) NT = g->fixed_NT;
     const bool mixed = p.precision == 1;
     // largest work first, so the long jobs start early and the short ones fill the tail
     std::vector<int> order(nj);
@@ -501,12 +513,15 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         const int j = order[q];
         const gbpf_job& J = jobs[j];
         gbpf_solver* s = J.solver;
+        const int G = J.cases_per_cta ? J.cases_per_cta : job_slots(Gmax, s->plan.nv, g->slot_budget);
         Shape* sh = nullptr;
         if (int rc = get_shape(s, NT, G, &sh)) return rc;
         occ = std::min(occ, sh->occ);
         gbpf::Job& o = hj[q];
         o.P = sh->dp;
         o.off = solver_offsets(s, G, mixed);
+        o.G = G;
+        o.log2G = ilog2(G);
         cta_bytes = std::max(cta_bytes, o.off.total);
         want += (J.n_cases + G - 1) / G;
         gbpf::Batch b{};
@@ -549,8 +564,6 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
     gbpf::Launch L{};
     L.jobs = g->bjobs.as<gbpf::Job>();
     L.njobs = nj;
-    L.G = G;
-    L.log2G = ilog2(G);
     L.scratch = g->scr.as<char>();
     L.cta_bytes = cta_bytes;
     CK(cudaEventRecord(g->e0, g->stream));
@@ -577,7 +590,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         st.macro_steps += c[4];
     }
     st.grid = grid;
-    st.cases_per_cta = G;
+    st.cases_per_cta = Gmax;
     st.threads_per_cta = NT;
     st.kernel_ms = ms;
     g->last = st;
@@ -1059,6 +1072,16 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, g->c0, g->c1));
     g->last.call_ms = ms;
+    return 0;
+}
+
+int gbpf_group_set_shape(gbpf_group* g, int threads_per_cta, int slot_budget) {
+    if (!g) return fail("null group");
+    if (threads_per_cta != 0 && threads_per_cta != 256 && threads_per_cta != 512 && threads_per_cta != 1024)
+        return fail("group_set_shape: threads_per_cta must be 0, 256, 512 or 1024");
+    if (slot_budget < 0) return fail("group_set_shape: slot_budget must be >= 0");
+    g->fixed_NT = threads_per_cta;
+    g->slot_budget = slot_budget ? slot_budget : 8192;
     return 0;
 }
 

@@ -114,6 +114,7 @@ struct Job {
     DevPlan P;
     Batch B;
     ScratchOffsets off;
+    int G, log2G;            // case slots per CTA for this job (the schedule has NT / G workers)
 };
 
 // A launch of the persistent Newton kernel: CTAs serve the jobs in order, each job until its
@@ -121,7 +122,6 @@ struct Job {
 struct Launch {
     const Job* jobs;         // device array
     int njobs;
-    int G, log2G;            // case slots per CTA
     char* scratch;
     unsigned long long cta_bytes;
 };

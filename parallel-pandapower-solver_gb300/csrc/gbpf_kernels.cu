@@ -489,7 +489,6 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 // double-precision evaluation on the same SM.
 template <int NTB>
 __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L) {
-    const int G = L.G, lg = L.log2G;
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
     char* const region = L.scratch + (size_t)blockIdx.x * L.cta_bytes;
@@ -524,6 +523,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         for (int w = tid; w < (int)(sizeof(Batch) / 4); w += NT) dst[w] = src[w];
     }
     const ScratchOffsets& off = L.jobs[job].off;
+    const int G = L.jobs[job].G, lg = L.jobs[job].log2G;  // case slots of this job's CTAs
     double4_32a* fac64 = reinterpret_cast<double4_32a*>(region + off.fac64);
     float4* fac32 = off.fac32 != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32) : nullptr;
     double2* R = reinterpret_cast<double2*>(region + off.R);

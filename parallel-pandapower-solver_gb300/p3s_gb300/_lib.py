@@ -87,6 +87,7 @@ class Job(C.Structure):
         ("V", _vp),
         ("iterations", _vp),
         ("converged", _vp),
+        ("cases_per_cta", C.c_int),
     ]
 
 
@@ -125,6 +126,7 @@ SIGNATURES = {
     "gbpf_group_solve": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
     "gbpf_group_solve_device": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
     "gbpf_group_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
+    "gbpf_group_set_shape": (C.c_int, [_vp, C.c_int, C.c_int]),
     "gbpf_islands_device_static": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, _vp,
                                              _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -30,6 +30,7 @@ class GroupJob:
     n_cases: int = 0
     pin: np.ndarray | None = None
     stamps: tuple | None = None
+    cases_per_cta: int = 0
 
 
 class GpuGroup:
@@ -48,6 +49,12 @@ class GpuGroup:
             except Exception:
                 pass
             self._h = None
+
+    def set_shape(self, threads_per_cta: int = 0, slot_budget: int = 0):
+        """Threads per CTA of later launches (0: by batch size) and the variable buses x case
+        slots a CTA may hold per job (0: 8,192)."""
+        _lib.check(_lib.load().gbpf_group_set_shape(self._h, int(threads_per_cta), int(slot_budget)),
+                   "gbpf_group_set_shape")
 
     @property
     def stats(self) -> dict:
@@ -93,6 +100,7 @@ class GpuGroup:
                 J.st_ptr, J.st_k, J.st_val = ptr.ctypes.data, k.ctypes.data, val.ctypes.data
                 keep += [ptr, k, val]
             J.V, J.iterations, J.converged = V.ctypes.data, it.ctypes.data, cv.ctypes.data
+            J.cases_per_cta = int(jb.cases_per_cta)
             outs.append((V, it, cv))
         rc = _lib.load().gbpf_group_solve(self._h, len(jobs), arr, C.byref(params))
         _lib.check(rc, "group_solve")

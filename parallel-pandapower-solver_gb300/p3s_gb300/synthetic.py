@@ -170,6 +170,26 @@ def _loading_scale(n, Yp, Yj, Yx, slack, P, max_angle_deg) -> float:
     return max_angle_deg / worst
 
 
+def _voltage_scale(n, Yp, Yj, Yx, fixed, Q, max_drop_pu) -> float:
+    """Largest factor <= 1 keeping the decoupled (Q-V) estimate of the voltage drops of
+    reactive loads ``Q`` within ``max_drop_pu``: dV = B_pq^-1 Q with the branch susceptance
+    Laplacian and the voltage-controlled buses (``fixed``) held."""
+    import scipy.sparse.linalg as spl
+
+    Y = sp.csr_matrix((Yx, Yj, Yp), shape=(n, n)).tocoo()
+    off = Y.row != Y.col
+    B = sp.coo_matrix((-Y.data.imag[off], (Y.row[off], Y.col[off])), shape=(n, n)).tocsr()
+    B = B - sp.diags(np.asarray(B.sum(axis=1)).ravel())
+    keep = np.setdiff1d(np.arange(n), fixed)
+    if len(keep) == 0:
+        return 1.0
+    dv = spl.spsolve(B[keep][:, keep].tocsc(), Q[keep])
+    worst = float(np.abs(dv).max()) if len(dv) else 0.0
+    if not np.isfinite(worst) or worst <= max_drop_pu:
+        return 1.0
+    return max_drop_pu / worst
+
+
 def make_grid(
     n: int,
     n_branches: int | None = None,
@@ -179,6 +199,7 @@ def make_grid(
     gen_scale: float = 1.03,
     max_angle_deg: float = 20.0,
     charging_scale: float | None = None,
+    max_drop_pu: float | None = None,
 ) -> Grid:
     """A synthetic meshed grid (see the module docstring for the recipe)."""
     rng = np.random.default_rng(seed)
@@ -235,10 +256,11 @@ def make_grid(
     vm_set[slack] = 1.04
     vm_set[pv] = rng.uniform(0.98, 1.05, n_pv)
     if n > 2000:
-        # generator set points spread less on denser grids: two PV buses a short line apart
-        # holding set points 0.07 pu apart exchange reactive power ~ 0.07 / x, which grows
-        # without bound as the lines shorten
-        vm_set[pv] = 1.015 + (vm_set[pv] - 1.015) * (2000.0 / n)
+        # generator and slack set points lie closer to 1 pu on denser grids: two PV buses a
+        # short line apart holding set points 0.07 pu apart exchange reactive power
+        # ~ 0.07 / x, which grows without bound as the lines shorten
+        vm_set[pv] = 1.0 + (vm_set[pv] - 1.015) * (2000.0 / n)
+        vm_set[slack] = 1.0 + (vm_set[slack] - 1.0) * (2000.0 / n)
     p_load = np.zeros(n)
     q_load = np.zeros(n)
     p_load[pq] = rng.uniform(0.0, 0.6, len(pq))
@@ -254,6 +276,10 @@ def make_grid(
     # All injections are therefore scaled by the largest factor <= 1 whose DC power flow
     # keeps every bus angle within `max_angle_deg` of the slack.
     lam = _loading_scale(n, Yp, Yj, Yx, slack, p_gen - p_load, max_angle_deg)
+    if max_drop_pu is not None:
+        # optionally also bound the decoupled estimate of the reactive voltage drops (small
+        # grids have long lines: the angle bound alone leaves some near voltage collapse)
+        lam = min(lam, _voltage_scale(n, Yp, Yj, Yx, np.r_[slack, pv], q_load, max_drop_pu))
     p_load *= lam
     q_load *= lam
     p_gen *= lam
@@ -345,6 +371,6 @@ def multigrid_batch(n_grids: int = 256, n_scen: int = 16, lo: int = 30, hi: int 
     """Uneven multi-grid batch: bus counts log-uniform in [lo, hi], 1.5 n branches, 10% PV."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_grids)).astype(int)
-    grids = [make_grid(int(s), seed=int(seed * 1000 + i)) for i, s in enumerate(sizes)]
+    grids = [make_grid(int(s), seed=int(seed * 1000 + i), max_drop_pu=0.05) for i, s in enumerate(sizes)]
     scen = [scenario_injections(g, n_scen, seed=int(seed * 1000 + i + 17)) for i, g in enumerate(grids)]
     return grids, scen
