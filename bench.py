@@ -296,7 +296,7 @@ def run_gpu(args, rank, world, local):
     d2h = Vh.nbytes + ith.nbytes + cvh.nbytes
 
     res = dict(out=out, e2e_ms=float(np.mean(e2e_ms)), h2d=h2d, d2h=d2h, info=info, K=len(off) - 1, T=T,
-               worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish)
+               worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish, vtol=p.vtol)
     return res
 
 
@@ -399,7 +399,8 @@ def gpu_line(args, res, rank, world):
             "l2": "inputs larger than L2 (S is 280 MB per step; L2 is 129 MB)",
             "iterations_mean": float(mixed["it"].mean()), "converged": bool(mixed["cv"].all()),
             "max_mismatch_pu_sampled": res["worst_mis"],
-            "polish": res["polish"], "threads_per_cta": info["threads_per_cta"],
+            "polish": res["polish"], "vtol": res["vtol"], "jinv_norm_est": info["jinv_norm"],
+            "threads_per_cta": info["threads_per_cta"],
             "single_factorizations": int(mixed["stats"]["single_factorizations"]),
             "double_factorizations": int(mixed["stats"]["double_factorizations"]),
         },

@@ -35,8 +35,12 @@ typedef struct gbpf_params {
     double pivot_ratio_single; /* the same bound for a float factorization (1e-3) */
     int vote_rule;       /* mixed: 0 = the reference's precision votes (nr_polar_kernels.cu:209-228),
                             1 = float until contraction stalls below mixed_switch */
-    double polish;       /* vote_rule 1: a case on float factors iterates until mismatch < polish * tol,
-                            so its voltage is as accurate as a double solve's (1e-3) */
+    double polish;       /* vote_rule 1: a case on float factors iterates until its mismatch is
+                            below polish * tol (1e-3) ... */
+    double vtol;         /* ... and below vtol / |J^-1| (jinv_norm of gbpf_info), a bound on the
+                            voltage error left (1e-8 p.u.; 0: no bound) -- though not below twice
+                            the double mismatch's rounding floor -- so its voltage is as accurate
+                            as a double solve's on ill-conditioned grids too */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -45,6 +49,7 @@ typedef struct gbpf_info {
     int cases_per_cta, threads_per_cta, workers;
     long long factor_pairs, forward_pairs, backward_pairs;
     double rcond0;
+    double jinv_norm;    /* estimate of |J^-1| (infinity norm) at the flat start */
 } gbpf_info;
 
 /* Counters of the last solve (the reference's last_stats, nr_polar_solver.py:671-681). */
@@ -196,6 +201,14 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
 int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
                  const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
                  int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands);
+
+/* gbpf_islands for the topology of `s` (n = its bus count) on the solver's stream, with
+ * device buffers the solver keeps and grows (no allocation once they are large enough):
+ * for a caller that islands many batches of outages of one grid, e.g. a serving loop.
+ * Replaces the same reference calls as gbpf_islands. */
+int gbpf_solver_islands(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
+                        const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
+                        int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands);
 
 /* gbpf_islands on caller-owned DEVICE buffers (same layouts; out_idx holds n_out entries),
  * allocating nothing: the kernel's scratch is a statically allocated 16 MiB device array,

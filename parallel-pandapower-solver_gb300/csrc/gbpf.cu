@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -132,12 +133,14 @@ struct gbpf_solver {
     DBuf scr;
     // per-call buffers (grow-only)
     DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab, bjobs;
+    // islanding buffers (grow-only)
+    DBuf iin, iscr, ibest, iout;
     gbpf_stats last{};
     ~gbpf_solver() {
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
-                        &btab, &bjobs})
+                        &btab, &bjobs, &iin, &iscr, &ibest, &iout})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -161,6 +164,13 @@ int upload_values(gbpf_solver* s) {
 // nr_polar_solver.py:409-427).
 int compute_rcond0(gbpf_solver* s) {
     gbpf::Plan& p = s->plan;
+    // largest row sum of |Y|: scales the rounding floor of a mismatch evaluated in double
+    p.y_rowsum = 0.0;
+    for (int r = 0; r < s->n; ++r) {
+        double a = 0.0;
+        for (int k = s->Yp[r]; k < s->Yp[r + 1]; ++k) a += std::hypot(s->Yx[2 * (size_t)k], s->Yx[2 * (size_t)k + 1]);
+        p.y_rowsum = std::max(p.y_rowsum, a);
+    }
     std::vector<double> Vm(s->n, 1.0), Va(s->n, 0.0), S(2 * (size_t)s->n, 0.0), blk(4 * (size_t)p.nblk),
         R(2 * (size_t)std::max(p.nv, 1));
     gbpf::host_eval(p, s->Yp.data(), s->Yj.data(), s->Yx.data(), Vm.data(), Va.data(), S.data(), nullptr, blk.data(),
@@ -168,6 +178,7 @@ int compute_rcond0(gbpf_solver* s) {
     double mn = 0, mx = 0;
     if (p.nv == 0) {
         p.rcond0 = 1.0;
+        p.jinv_est = 0.0;
         return 0;
     }
     if (!gbpf::host_factor(p, blk.data(), &mn, &mx) || !(mx > 0.0) || !(mn > 0.0) || !std::isfinite(mx)) {
@@ -175,9 +186,27 @@ int compute_rcond0(gbpf_solver* s) {
         // pivot check and the cases end not converged (nr_klu.cpp's behaviour when its plan
         // cannot be built); gbpf_info reports rcond0 = NaN so callers can refuse the grid
         p.rcond0 = std::nan("");
+        p.jinv_est = std::nan("");
         return 0;
     }
     p.rcond0 = mn / mx;
+    // |J^-1| (infinity norm) estimate: the largest |J^-1 b| over a few sign vectors b
+    // (all ones, P rows only, a fixed pseudo-random pattern); a lower bound that is usually
+    // within a small factor
+    std::vector<double> y(2 * (size_t)p.nv);
+    double est = 0.0;
+    unsigned rng = 12345u;
+    for (int probe = 0; probe < 3; ++probe) {
+        for (int r = 0; r < p.nv; ++r) {
+            rng = rng * 1664525u + 1013904223u;
+            const double sgn = probe == 2 ? ((rng >> 16) & 1 ? 1.0 : -1.0) : 1.0;
+            y[2 * r] = sgn;
+            y[2 * r + 1] = probe == 1 ? 0.0 : sgn * (p.row_pq[r] ? 1.0 : 0.0);
+        }
+        gbpf::host_solve(p, blk.data(), y.data());
+        for (double v : y) est = std::max(est, std::fabs(v));
+    }
+    p.jinv_est = std::isfinite(est) ? est : std::nan("");
     return 0;
 }
 
@@ -335,6 +364,7 @@ gbpf_params default_params() {
     p.pivot_ratio_single = 1e-3;
     p.vote_rule = 1;
     p.polish = 1e-3;
+    p.vtol = 1e-8;
     return p;
 }
 
@@ -424,7 +454,17 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     b.mixed = p.precision == 1;
     b.mixed_switch = p.mixed_switch;
     b.vote_rule = p.vote_rule;
-    b.polish = p.polish > 0.0 && p.polish <= 1.0 ? p.polish : 1.0;
+    // mixed (GB300 rule) cases polish to polish x tol, and further on ill-conditioned grids:
+    // until |J^-1| x mismatch, a bound on the voltage error left, is below vtol -- but not
+    // below twice the rounding floor of the double mismatch (eps x the largest row sum of
+    // |Y|), which no step in double precision gets under reliably
+    const double polish = p.polish > 0.0 && p.polish <= 1.0 ? p.polish : 1.0;
+    b.tol_polish = p.tol * polish;
+    const double k = s->plan.jinv_est;
+    if (p.vtol > 0.0 && k > 0.0 && std::isfinite(k)) {
+        const double floor_ = 2.0 * DBL_EPSILON * s->plan.y_rowsum;
+        b.tol_polish = std::min(b.tol_polish, std::max(p.vtol / k, floor_));
+    }
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
@@ -685,6 +725,7 @@ int gbpf_get_info(gbpf_solver* s, gbpf_info* o) {
     o->forward_pairs = p.n_fwd_pairs;
     o->backward_pairs = p.n_bwd_pairs;
     o->rcond0 = p.rcond0;
+    o->jinv_norm = p.jinv_est;
     return 0;
 }
 
@@ -969,6 +1010,73 @@ void* gbpf_host_alloc(size_t bytes) {
 
 void gbpf_host_free(void* p) {
     if (p) cudaFreeHost(p);
+}
+
+int gbpf_solver_islands(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
+                        const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
+                        int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands) {
+    if (!s) return fail("null solver");
+    const int n = s->n;
+    if (m < 0 || L <= 0 || !out_ptr || !is_slack || !labels || !served || !ref_bus || !n_islands ||
+        (m > 0 && (!f || !t || !live)))
+        return fail("solver_islands: invalid arguments");
+    for (int e = 0; e < m; ++e)
+        if (f[e] < 0 || f[e] >= n || t[e] < 0 || t[e] >= n) return fail("solver_islands: branch end out of range");
+    if (out_ptr[0] != 0) return fail("solver_islands: outage pointers must start at 0");
+    for (int c = 0; c < L; ++c)
+        if (out_ptr[c + 1] < out_ptr[c]) return fail("solver_islands: outage pointers must not decrease");
+    const int nout = out_ptr[L];
+    for (int q = 0; q < nout; ++q)
+        if (out_idx[q] < 0 || out_idx[q] >= m) return fail("solver_islands: outage index out of range");
+    const int grid = std::max(1, std::min(L, 4 * s->nsm));
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t nl = (size_t)n * L;
+    const size_t b_f = up((size_t)m * 4), b_l = up((size_t)m), b_op = up((size_t)(L + 1) * 4),
+                 b_oi = up((size_t)std::max(nout, 1) * 4), b_s = up((size_t)n), b_p = up((size_t)n * 8);
+    CK(s->iin.ensure(2 * b_f + b_l + b_op + b_oi + b_s + b_p));
+    CK(s->iscr.ensure((size_t)grid * 4 * n * 4));
+    CK(s->ibest.ensure((size_t)grid * n * 8));
+    const size_t b_lab = up(nl * 4), b_sv = up(nl), b_ni = up((size_t)L * 4);
+    CK(s->iout.ensure(2 * b_lab + b_sv + b_ni + 256));
+    char* in = s->iin.as<char>();
+    int* df = reinterpret_cast<int*>(in);
+    int* dt = reinterpret_cast<int*>(in + b_f);
+    uint8_t* dl = reinterpret_cast<uint8_t*>(in + 2 * b_f);
+    int* dop = reinterpret_cast<int*>(in + 2 * b_f + b_l);
+    int* doi = reinterpret_cast<int*>(in + 2 * b_f + b_l + b_op);
+    uint8_t* ds = reinterpret_cast<uint8_t*>(in + 2 * b_f + b_l + b_op + b_oi);
+    double* dp = reinterpret_cast<double*>(in + 2 * b_f + b_l + b_op + b_oi + b_s);
+    char* out = s->iout.as<char>();
+    int* dlab = reinterpret_cast<int*>(out);
+    int* dref = reinterpret_cast<int*>(out + b_lab);
+    uint8_t* dsv = reinterpret_cast<uint8_t*>(out + 2 * b_lab);
+    int* dni = reinterpret_cast<int*>(out + 2 * b_lab + b_sv);
+    int* derr = reinterpret_cast<int*>(out + 2 * b_lab + b_sv + b_ni);
+    cudaStream_t st = s->stream;
+    if (m) {
+        CK(cudaMemcpyAsync(df, f, (size_t)m * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dt, t, (size_t)m * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dl, live, (size_t)m, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(dop, out_ptr, (size_t)(L + 1) * 4, cudaMemcpyHostToDevice, st));
+    if (nout) CK(cudaMemcpyAsync(doi, out_idx, (size_t)nout * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ds, is_slack, (size_t)n, cudaMemcpyHostToDevice, st));
+    if (gen_prio)
+        CK(cudaMemcpyAsync(dp, gen_prio, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    else
+        CK(cudaMemsetAsync(dp, 0, (size_t)n * 8, st));
+    CK(cudaMemsetAsync(derr, 0, 4, st));
+    CK(gbpf::launch_islands(n, m, df, dt, dl, L, dop, doi, ds, dp, reslack, s->iscr.as<int>(),
+                            s->ibest.as<unsigned long long>(), dlab, dsv, dref, dni, derr, grid, st));
+    int kerr = 0;
+    CK(cudaMemcpyAsync(&kerr, derr, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(labels, dlab, nl * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(served, dsv, nl, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ref_bus, dref, nl * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(n_islands, dni, (size_t)L * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (kerr) return fail("solver_islands: label propagation did not settle");
+    return 0;
 }
 
 gbpf_group* gbpf_group_create(void) {

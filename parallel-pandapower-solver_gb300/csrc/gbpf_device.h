@@ -83,7 +83,7 @@ struct Batch {
     int mixed;               // 0: all factorizations double; 1: vote per case
     double mixed_switch;
     int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
-    double polish;           // GB300 rule: float-factor cases iterate to polish * tol
+    double tol_polish;       // GB300 rule: float-factor cases iterate until mismatch < tol_polish
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch
@@ -136,6 +136,11 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
                               double2* R, cudaStream_t stream);
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d);
+// islanding kernel (islands.cu): scratch 4 n ints and n u64 per CTA of `grid`
+cudaError_t launch_islands(int n, int m, const int* f, const int* t, const uint8_t* live, int L, const int* out_ptr,
+                           const int* out_idx, const uint8_t* is_slack, const double* prio, int reslack, int* scratch,
+                           unsigned long long* best, int* labels, uint8_t* served, int* ref_bus, int* n_islands,
+                           int* err, int grid, cudaStream_t stream);
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
 const void* newton_kernel_ptr(int threads);
 

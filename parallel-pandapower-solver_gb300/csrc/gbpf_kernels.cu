@@ -876,17 +876,18 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 top = true;
             }
             if (top) {  // nr_klu.cpp:590-595 loop head
-                // Under the GB300 vote rule a case keeps stepping until its mismatch is below
-                // polish x tol: a float step (or a double step taken after float ones) lands
-                // anywhere below tol, so without the polish its voltage would only be as close
-                // to the exact solution as tol allows, where the double path's quadratic last
-                // step lands far below tol. `converged` still means mismatch < tol.
+                // Under the GB300 vote rule a case keeps stepping until its voltage is as
+                // exact as a double solve's: a float step lands anywhere below tol (it
+                // contracts the error by ~cond(J) 2^-24 instead of squaring it), so the case
+                // goes on until its mismatch is below tol_polish (the smaller of polish x tol
+                // and a bound on the voltage error divided by the grid's |J^-1| estimate).
+                // `converged` still means mismatch < tol.
                 const bool polish = Bt.mixed && Bt.vote_rule == 1;
-                const double tol_s = polish ? Bt.tol * Bt.polish : Bt.tol;
+                const bool done = s_nrm[s] < (polish ? Bt.tol_polish : Bt.tol);
                 if (s_it[s] >= Bt.max_iter) {
                     s_st[s] = SL_FINISH;
                     s_conv[s] = polish && s_nrm[s] < Bt.tol;
-                } else if (s_nrm[s] < tol_s) {
+                } else if (done) {
                     s_st[s] = SL_FINISH;
                     s_conv[s] = 1;
                 } else if (s_nrm[s] >= BIG) {

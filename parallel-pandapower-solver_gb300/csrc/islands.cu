@@ -145,6 +145,15 @@ int ifail(const std::string& m) {
 
 }  // namespace
 
+cudaError_t gbpf::launch_islands(int n, int m, const int* f, const int* t, const uint8_t* live, int L,
+                                 const int* out_ptr, const int* out_idx, const uint8_t* is_slack, const double* prio,
+                                 int reslack, int* scratch, unsigned long long* best, int* labels, uint8_t* served,
+                                 int* ref_bus, int* n_islands, int* err, int grid, cudaStream_t stream) {
+    islands_kernel<<<grid, NT, 0, stream>>>(n, m, f, t, live, L, out_ptr, out_idx, is_slack, prio, reslack, scratch,
+                                            best, labels, served, ref_bus, n_islands, err);
+    return cudaGetLastError();
+}
+
 extern "C" int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
                             const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack,
                             const double* gen_prio, int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus,

@@ -75,6 +75,8 @@ struct Plan {
     // statistics
     long long n_factor_pairs = 0, n_fwd_pairs = 0, n_bwd_pairs = 0;
     double rcond0 = 0.0;            // pivot ratio of the flat-start factorization
+    double jinv_est = 0.0;          // |J^-1| (infinity norm) estimate at the flat start
+    double y_rowsum = 0.0;          // largest row sum of |Ybus|
     std::vector<int> level_work;    // per level: max worker load (critical path estimate)
 };
 

@@ -34,6 +34,7 @@ class Params(C.Structure):
         ("pivot_ratio_single", C.c_double),
         ("vote_rule", C.c_int),
         ("polish", C.c_double),
+        ("vtol", C.c_double),
     ]
 
 
@@ -52,6 +53,7 @@ class Info(C.Structure):
         ("forward_pairs", C.c_longlong),
         ("backward_pairs", C.c_longlong),
         ("rcond0", C.c_double),
+        ("jinv_norm", C.c_double),
     ]
 
 
@@ -127,6 +129,8 @@ SIGNATURES = {
     "gbpf_group_solve_device": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
     "gbpf_group_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_group_set_shape": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "gbpf_solver_islands": (C.c_int, [_vp, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
+                                      _ip, _ip]),
     "gbpf_islands_device_static": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, _vp,
                                              _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -39,7 +39,9 @@ class PolarNewtonSolverCUDA:
         # "reference": the reference's votes (float above mixed_switch, double below it)
         self.vote_rule = "gb300"
         # gb300 rule: a case on float factors iterates until its mismatch is below polish * tol
+        # and below vtol / |J^-1| (a bound on the voltage error left)
         self.polish = 1e-3
+        self.vtol = 1e-8
         self.line_search = True
         self.fallback = "none"
         self.cpu_handoff = 0
@@ -60,7 +62,7 @@ class PolarNewtonSolverCUDA:
     def _params(self, max_iter, tol):
         return GpuSolver.params(max_iter, tol, self.line_search, self.precision, self.mixed_switch,
                                 pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single,
-                                vote_rule=self.vote_rule, polish=self.polish)
+                                vote_rule=self.vote_rule, polish=self.polish, vtol=self.vtol)
 
     def _record(self, B, r):
         st = self._s.stats

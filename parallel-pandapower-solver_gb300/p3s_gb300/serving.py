@@ -1,0 +1,346 @@
+"""Serving loop: continuous batching of power-flow requests over resident topologies.
+
+A ``Server`` keeps every registered topology resident on the device -- Ybus, plan and
+schedules (``GpuSolver``), its warm-start voltage (the converged base case) and its N-1
+data -- and serves a stream of requests:
+
+* ``single``: one operating point (n,) of injections;
+* ``chunk``: a time-series chunk (n, T), every step starting from the warm-start voltage;
+* ``n1``: an N-1 sweep over a list of branch outages (islands, re-slack, stamp-patched Ybus).
+
+Requests are admitted as they arrive. Whenever one of the server's launch contexts
+(``GpuGroup``: its own stream and scratch) is free, every admitted request waiting for a
+topology that no other launch is using joins ONE persistent-kernel launch over all those
+topologies (largest job first), within the device-memory budget; requests that arrive while
+launches run wait at most until the next context frees, and the launches of different
+contexts overlap on the device. Every case runs the same arithmetic alone and in any mix,
+so a request's result does not depend on what it was batched with.
+
+No reference counterpart: the reference solves one call at a time
+(p3s/cuda/nr_polar_solver.py:466-596, p3s/contingency/solver_cuda.py:30-119); its N-1
+semantics (islands, re-slack, V0 / pin) are those of ``contingency``.
+"""
+
+from __future__ import annotations
+
+import threading
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .group import GpuGroup, GroupJob
+from .solver import GpuSolver, c128
+
+
+@dataclass
+class Request:
+    rid: int
+    topo: int                 # index of a registered topology
+    kind: str                 # "single" | "chunk" | "n1"
+    arrival: float            # seconds from the start of the stream
+    S: np.ndarray             # (n,) or (n, T) injections (n1: the base-case injections)
+    outages: np.ndarray | None = None  # n1: branch indices, one outage case each
+
+
+@dataclass
+class Response:
+    rid: int
+    V: np.ndarray             # (n, T) complex; n1: NaN at unserved buses
+    iterations: np.ndarray
+    converged: np.ndarray
+    arrival: float
+    start: float              # launch start (seconds from the start of the stream)
+    done: float
+    launch: int               # launch sequence number
+    served: np.ndarray | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+def _slot_bytes(n: int, nv: int, nblk: int, mixed: bool) -> int:
+    """Device bytes of one case slot (the kernel's per-slot scratch)."""
+    b = nblk * 32 + nv * 32 + n * (32 + 32 + 16 + 8 + 16 + 1)
+    if mixed:
+        b += nblk * 16 + nv * 8
+    return b
+
+
+class Topology:
+    """A resident grid: solver, warm-start voltage and N-1 data."""
+
+    def __init__(self, grid, name: str = ""):
+        self.grid = grid
+        self.name = name or f"{grid.n}-bus"
+        self.solver = GpuSolver(grid.Yp, grid.Yj, grid.Yx, grid.pv, grid.pq)
+        info = self.solver.info
+        self.n = grid.n
+        self.nv = info["n_var_bus"]
+        self.nblk = info["n_blocks"]
+        base = self.solver.solve_batch(grid.Sbus[:, None], grid.V0, GpuSolver.params(precision="double"))
+        if not base["converged"][0]:
+            raise RuntimeError(f"{self.name}: the base case does not converge")
+        self.V_warm = np.ascontiguousarray(base["V"][:, 0])
+        self.f = np.ascontiguousarray(grid.f, dtype=np.int32)
+        self.t = np.ascontiguousarray(grid.t, dtype=np.int32)
+        self.live = np.ascontiguousarray((grid.stamp[:, 1] != 0) | (grid.stamp[:, 2] != 0), dtype=np.uint8)
+        self.is_slack = np.zeros(self.n, dtype=np.uint8)
+        self.is_slack[np.asarray(grid.ref, dtype=np.int64)] = 1
+        self.prio = np.zeros(self.n)
+        self.prio[grid.pv] = np.maximum(grid.p_gen[grid.pv], np.finfo(float).tiny)
+
+    def slot_bytes(self, mixed: bool) -> int:
+        return _slot_bytes(self.n, self.nv, self.nblk, mixed)
+
+    def n1_job(self, outages: np.ndarray, S_base: np.ndarray):
+        """Islanding of the outage cases on the device, then V0 / pin / stamps of the job."""
+        L = len(outages)
+        ptr = np.arange(L + 1, dtype=np.int32)
+        idx = np.ascontiguousarray(outages, dtype=np.int32)
+        labels = np.empty((self.n, L), dtype=np.int32)
+        served = np.empty((self.n, L), dtype=np.uint8)
+        ref_bus = np.empty((self.n, L), dtype=np.int32)
+        nis = np.empty(L, dtype=np.int32)
+        rc = _lib.load().gbpf_solver_islands(self.solver._h, len(self.f), _lib.i32(self.f), _lib.i32(self.t),
+                                             _lib.u8(self.live), L, _lib.i32(ptr), _lib.i32(idx),
+                                             _lib.u8(self.is_slack), _lib.d(self.prio), 1, _lib.i32(labels),
+                                             _lib.u8(served), _lib.i32(ref_bus), _lib.i32(nis))
+        _lib.check(rc, "solver_islands")
+        served = served.astype(bool)
+        V0 = np.repeat(self.V_warm[:, None], L, axis=1)
+        pin = np.zeros((self.n, L), dtype=np.uint8)
+        bus = np.arange(self.n)[:, None]
+        is_ref = (ref_bus == bus) & ~self.is_slack.astype(bool)[:, None]
+        V0[is_ref] = np.abs(np.broadcast_to(self.V_warm[:, None], V0.shape)[is_ref]) + 0j
+        pin[is_ref] = 1
+        V0[~served] = 1.0 + 0.0j
+        pin[~served] = 1
+        sp_ = np.arange(0, 4 * L + 1, 4, dtype=np.int32)
+        sk = np.ascontiguousarray(self.grid.stamp_pos[idx].ravel(), dtype=np.int32)
+        sv = c128(self.grid.stamp[idx].ravel())
+        job = GroupJob(self.solver, c128(S_base).ravel(), np.ascontiguousarray(V0), n_cases=L, pin=pin,
+                       stamps=(sp_, sk, sv))
+        return job, served
+
+
+@dataclass
+class _Launch:
+    seq: int
+    requests: list
+    jobs: list
+    served: dict = field(default_factory=dict)  # rid -> served mask (n1)
+    start: float = 0.0
+
+
+class Server:
+    """Continuous batching over resident topologies (see the module docstring).
+
+    precision: "mixed" or "double"; contexts: launches that may overlap on the device;
+    max_cases: cases per launch; hbm_budget: bytes of case-slot scratch all contexts may hold.
+    """
+
+    def __init__(self, topologies: list[Topology], precision: str = "mixed", contexts: int = 2,
+                 max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
+                 **solver_params):
+        self.topos = topologies
+        self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
+        self.mixed = precision == "mixed"
+        self.groups = [GpuGroup() for _ in range(max(1, contexts))]
+        self.max_cases = max_cases
+        self.hbm_budget = hbm_budget
+        self._cv = threading.Condition()
+
+    def warmup(self, cases: int = 64):
+        """Build every topology's schedules and grow every context's scratch to its largest
+        launch before serving, so that no launch allocates device memory (an allocation or
+        release synchronises the device and would stall the launches in flight)."""
+        big = max(self.topos, key=lambda tp: tp.nblk)
+        for grp in self.groups:
+            jobs = [GroupJob(tp.solver, tp.grid.Sbus, tp.V_warm, n_cases=1) for tp in self.topos]
+            jobs.append(GroupJob(big.solver, big.grid.Sbus, big.V_warm, n_cases=max(cases, 1)))
+            jobs += [GroupJob(tp.solver, tp.grid.Sbus, tp.V_warm, n_cases=cases) for tp in self.topos]
+            grp.solve(jobs, self.params)
+            for tp in self.topos:
+                job, _ = tp.n1_job(np.arange(min(4, len(tp.f)), dtype=np.int32), tp.grid.Sbus)
+                grp.solve([job], self.params)
+
+    # ------------------------------------------------------------------ batching
+    def _cases(self, r: Request) -> int:
+        if r.kind == "n1":
+            return len(r.outages)
+        return 1 if r.S.ndim == 1 else r.S.shape[1]
+
+    def _footprint(self, r: Request) -> float:
+        return self._cases(r) * self.topos[r.topo].slot_bytes(self.mixed)
+
+    def _form(self, pending: deque, busy_topos: set, budget_left: float):
+        """Take every pending request whose topology is idle, oldest first, within the
+        launch's case and memory limits."""
+        take, cases, mem, topos = [], 0, 0.0, set()
+        keep = deque()
+        while pending:
+            r = pending.popleft()
+            c, fp = self._cases(r), self._footprint(r)
+            if r.topo in busy_topos or (take and (cases + c > self.max_cases or mem + fp > budget_left)):
+                keep.append(r)
+                continue
+            take.append(r)
+            cases += c
+            mem += fp
+            topos.add(r.topo)
+        pending.extend(keep)
+        return take, topos, mem
+
+    def _jobs(self, reqs: list):
+        """One job per topology for its steady-state cases (single + chunk columns, all
+        starting from the warm-start voltage) and one per topology for its N-1 cases."""
+        ts, n1 = {}, {}
+        for r in reqs:
+            (n1 if r.kind == "n1" else ts).setdefault(r.topo, []).append(r)
+        jobs, layout, served = [], [], {}
+        for k, rs in ts.items():
+            tp = self.topos[k]
+            cols = [r.S[:, None] if r.S.ndim == 1 else r.S for r in rs]
+            S = np.ascontiguousarray(np.concatenate(cols, axis=1), dtype=np.complex128)
+            jobs.append(GroupJob(tp.solver, S, tp.V_warm))
+            at = 0
+            spans = []
+            for r, c in zip(rs, cols):
+                spans.append((r, at, at + c.shape[1]))
+                at += c.shape[1]
+            layout.append(spans)
+        for k, rs in n1.items():
+            tp = self.topos[k]
+            out = np.concatenate([r.outages for r in rs])
+            job, sv = tp.n1_job(out, rs[0].S)
+            jobs.append(job)
+            at = 0
+            spans = []
+            for r in rs:
+                L = len(r.outages)
+                spans.append((r, at, at + L))
+                served[r.rid] = sv[:, at:at + L]
+                at += L
+            layout.append(spans)
+        return jobs, layout, served
+
+    # ------------------------------------------------------------------ serving
+    def run(self, requests: list[Request], realtime: bool = True) -> list[Response]:
+        """Serve a request stream. realtime: each request is admitted at its arrival time
+        (wall clock from the call); otherwise all are admitted at once."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        pending: deque = deque()
+        responses: dict[int, Response] = {}
+        free = list(range(len(self.groups)))
+        busy_topos: set = set()
+        mem_in_use = [0.0]
+        inflight = [0]
+        errors: list = []
+        seq = [0]
+        t0 = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t0
+
+        def worker(gi: int, launch: _Launch, topos: set, mem: float, layout):
+            try:
+                res = self.groups[gi].solve(launch.jobs, self.params)
+                done = now()
+                out = []
+                for job_res, spans in zip(res, layout):
+                    for r, a, b in spans:
+                        V = job_res["V"][:, a:b].copy()
+                        sv = launch.served.get(r.rid)
+                        if sv is not None:
+                            V[~sv] = np.nan
+                        out.append(Response(r.rid, V, job_res["iterations"][a:b].copy(),
+                                            job_res["converged"][a:b].copy(), r.arrival, launch.start, done,
+                                            launch.seq, sv))
+            except Exception as e:  # reported to the caller after the stream
+                out = []
+                errors.append(e)
+            with self._cv:
+                for resp in out:
+                    responses[resp.rid] = resp
+                free.append(gi)
+                busy_topos.difference_update(topos)
+                mem_in_use[0] -= mem
+                inflight[0] -= 1
+                self._cv.notify_all()
+
+        i = 0
+        with self._cv:
+            while i < len(reqs) or pending or inflight[0]:
+                tnow = now()
+                while i < len(reqs) and (not realtime or reqs[i].arrival <= tnow):
+                    pending.append(reqs[i])
+                    i += 1
+                if errors:
+                    break
+                if pending and free:
+                    take, topos, mem = self._form(pending, busy_topos, self.hbm_budget - mem_in_use[0])
+                    if take:
+                        gi = free.pop()
+                        jobs, layout, served = self._jobs(take)
+                        launch = _Launch(seq[0], take, jobs, served, now())
+                        seq[0] += 1
+                        busy_topos.update(topos)
+                        mem_in_use[0] += mem
+                        inflight[0] += 1
+                        threading.Thread(target=worker, args=(gi, launch, topos, mem, layout), daemon=True).start()
+                        continue
+                wait = None
+                if i < len(reqs) and realtime:
+                    wait = max(0.0, reqs[i].arrival - now())
+                if wait is None and not inflight[0] and not pending:
+                    continue
+                self._cv.wait(timeout=wait if wait is not None else 0.05)
+        if errors:
+            raise errors[0]
+        return [responses[r.rid] for r in requests]
+
+
+def latency_summary(responses: list[Response], elapsed: float | None = None) -> dict:
+    """p50 / p99 latency (ms) and solves/s of a served stream."""
+    lat = np.array([r.latency for r in responses]) * 1e3
+    cases = int(sum(len(r.iterations) for r in responses))
+    span = elapsed if elapsed is not None else (max(r.done for r in responses) - min(r.arrival for r in responses))
+    conv = float(np.mean(np.concatenate([r.converged for r in responses])))
+    return {"requests": len(responses), "cases": cases, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "solves_per_s": cases / span if span > 0 else float("nan"), "converged_fraction": conv}
+
+
+def poisson_stream(topos: list[Topology], rate: float, duration: float, seed: int = 0, chunk: int = 96,
+                   n1_outages: int = 200, mix=(0.70, 0.25, 0.05)) -> list[Request]:
+    """Seeded Poisson request stream: single solves, time-series chunks and N-1 sweeps in the
+    proportions `mix`, each on a topology drawn uniformly; loads scaled U(0.8, 1.2)."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        k = int(rng.integers(len(topos)))
+        tp = topos[k]
+        g = tp.grid
+        u = rng.random()
+        kind = "single" if u < mix[0] else ("chunk" if u < mix[0] + mix[1] else "n1")
+        if kind == "single":
+            S = g.Sbus.copy()
+            S[g.pq] *= rng.uniform(0.8, 1.2, len(g.pq))
+            out.append(Request(len(out), k, kind, t, S))
+        elif kind == "chunk":
+            S = np.repeat(g.Sbus[:, None], chunk, axis=1)
+            S[g.pq, :] *= rng.uniform(0.8, 1.2, (len(g.pq), chunk))
+            out.append(Request(len(out), k, kind, t, np.ascontiguousarray(S)))
+        else:
+            nb = len(g.f)
+            L = min(n1_outages, nb)
+            outs = np.sort(rng.choice(nb, L, replace=False)).astype(np.int32)
+            out.append(Request(len(out), k, kind, t, g.Sbus.copy(), outs))
+    return out

@@ -118,12 +118,13 @@ class GpuSolver:
 
     @staticmethod
     def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False,
-               pivot_ratio_double=1e-3, pivot_ratio_single=1e-3, vote_rule="gb300", polish=1e-3):
+               pivot_ratio_double=1e-3, pivot_ratio_single=1e-3, vote_rule="gb300", polish=1e-3, vtol=1e-8):
         if precision not in ("double", "mixed"):
             raise ValueError(f"precision must be 'double' or 'mixed', got {precision!r}")
         return _lib.Params(int(max_iter), float(tol), int(bool(line_search)), 1 if precision == "mixed" else 0,
                            float(mixed_switch), int(bool(check_v0)), float(pivot_ratio_double),
-                           float(pivot_ratio_single), 0 if vote_rule == "reference" else 1, float(polish))
+                           float(pivot_ratio_single), 0 if vote_rule == "reference" else 1, float(polish),
+                           float(vtol))
 
     # -------------------------------------------------------------- values
     def update_Y(self, Yx):

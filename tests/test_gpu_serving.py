@@ -1,0 +1,51 @@
+"""Serving loop on the GPU: continuous batching over resident topologies. Each request's
+result is the same alone and in the mix (bar: bit for bit -- every case runs the same
+arithmetic whatever it is batched with), N-1 requests keep the islanding semantics, and
+the mixed path stays within 1e-9 of the converged double solution."""
+
+import numpy as np
+import pytest
+
+from p3s_gb300.serving import Server, Topology, latency_summary, poisson_stream
+from p3s_gb300.synthetic import grid_118, make_grid
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def topos():
+    grids = [grid_118(), make_grid(400, seed=21), make_grid(1500, seed=22), make_grid(5000, seed=23)]
+    return [Topology(g) for g in grids]
+
+
+def test_results_are_the_same_alone_and_in_the_mix(topos):
+    reqs = poisson_stream(topos, rate=400.0, duration=0.25, seed=5, chunk=12, n1_outages=24,
+                          mix=(0.6, 0.3, 0.1))
+    kinds = {r.kind for r in reqs}
+    assert kinds == {"single", "chunk", "n1"}
+    server = Server(topos, precision="mixed", contexts=2)
+    server.warmup(cases=8)
+    mixed_run = server.run(reqs, realtime=True)
+    summary = latency_summary(mixed_run)
+    assert summary["converged_fraction"] == 1.0 and summary["requests"] == len(reqs)
+    launches = {r.launch for r in mixed_run}
+    assert len(launches) < len(reqs)  # requests were batched together
+    alone = Server(topos, precision="mixed", contexts=1)
+    for r, got in zip(reqs, mixed_run):
+        ref = alone.run([r], realtime=False)[0]
+        assert np.array_equal(got.iterations, ref.iterations) and np.array_equal(got.converged, ref.converged)
+        assert np.array_equal(np.isnan(got.V), np.isnan(ref.V))
+        assert np.array_equal(np.nan_to_num(got.V), np.nan_to_num(ref.V))
+        if r.kind == "n1":
+            assert np.array_equal(got.served, ref.served) and (~got.served).sum() >= 0
+
+
+def test_served_mixed_results_match_the_converged_double_solution(topos):
+    reqs = poisson_stream(topos, rate=200.0, duration=0.2, seed=9, chunk=8, n1_outages=16, mix=(0.5, 0.4, 0.1))
+    mixed = Server(topos, precision="mixed").run(reqs, realtime=False)
+    tight = Server(topos, precision="double", tol=1e-12).run(reqs, realtime=False)
+    for a, b in zip(mixed, tight):
+        assert np.array_equal(a.converged, b.converged)
+        ok = a.converged
+        if ok.any():
+            assert np.nanmax(np.abs(a.V[:, ok] - b.V[:, ok])) < 1e-9
