@@ -10,6 +10,10 @@ mismatch by ONE launch of the persistent sm_103a kernel.
           region (CUDA events from the first copy in to the last copy out)
   fp64  : the same for the plain double-precision path (the headline value is the mixed path)
 
+Beside the headline (rank 0, outside the timed steps): the full N-1 sweep of the same grid
+(3,001 cases), the uneven multi-grid batch (256 grids x 16 scenarios in one launch), and the
+serving loop (Poisson stream over 32 resident topologies; p50 / p99 latency per rate).
+
 N > 1 (torchrun): every rank solves its own 8,760-hour series (weak scaling, no collective on
 the data path); value = all ranks' solves / the slowest rank's time.
 `--impl reference` times the CPU oracle (the restatement of the reference's nr_klu solver,
@@ -331,6 +335,77 @@ def run_n1(args):
     return out
 
 
+def run_multigrid(args):
+    """256 synthetic grids with bus counts log-uniform in [30, 20,000] (1.5 n branches, 10 % PV
+    buses), 16 load scenarios each (base loads x U(0.8, 1.2)): ONE persistent launch over all
+    of them (a group), against the same grids solved one launch per grid."""
+    from p3s_gb300.group import GpuGroup, GroupJob
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.synthetic import multigrid_batch
+
+    grids, scen = multigrid_batch()
+    solvers = [GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq) for g in grids]
+    grp = GpuGroup()
+    jobs = [GroupJob(s, S, g.V0) for s, S, g in zip(solvers, scen, grids)]
+    cases = sum(S.shape[1] for S in scen)
+    out = {"grids": len(grids), "cases": cases, "bus_range": [min(g.n for g in grids), max(g.n for g in grids)]}
+    for prec in ("mixed", "double"):
+        p = GpuSolver.params(precision=prec)
+        for _ in range(args.warmup):
+            res = grp.solve(jobs, p)
+        kern, call = [], []
+        for _ in range(max(1, args.steps // 2)):
+            res = grp.solve(jobs, p)
+            kern.append(grp.stats["kernel_ms"])
+            call.append(grp.stats["call_ms"])
+        per_grid = 0.0
+        for s, S, g in zip(solvers, scen, grids):
+            s.solve_batch(S, g.V0, p)
+            per_grid += s.stats["kernel_ms"]
+        its = np.concatenate([r["iterations"] for r in res])
+        cv = np.concatenate([r["converged"] for r in res])
+        out["fp64" if prec == "double" else prec] = {
+            "value": round(cases / (np.mean(kern) * 1e-3), 1), "unit": "solves/s", "kernel_ms": round(float(np.mean(kern)), 3),
+            "e2e_solves_per_s": round(cases / (np.mean(call) * 1e-3), 1),
+            "one_launch_per_grid_kernel_ms": round(per_grid, 2),
+            "iterations_mean": float(its.mean()), "converged": int(cv.sum()),
+            "threads_per_cta": grp.stats["threads_per_cta"], "grid_ctas": grp.stats["grid"],
+        }
+    return out
+
+
+def run_serving(args):
+    """Poisson request stream over 32 resident topologies of 100..50,000 buses (70 % single
+    solves, 25 % 96-step chunks, 5 % 200-outage N-1 sweeps), served with continuous batching;
+    the rate is raised until p99 latency exceeds 50 ms. Latency = completion - arrival (wall
+    clock, host arrays in and out)."""
+    from p3s_gb300.serving import Server, Topology, latency_summary, poisson_stream
+    from p3s_gb300.synthetic import make_grid
+
+    rng = np.random.default_rng(5)
+    sizes = np.sort(np.exp(rng.uniform(np.log(100), np.log(50000), 32)).astype(int))
+    topos = [Topology(make_grid(int(n), seed=500 + i, max_drop_pu=0.05)) for i, n in enumerate(sizes)]
+    out = {"topologies": len(topos), "bus_range": [int(sizes[0]), int(sizes[-1])], "stream_s": args.serve_seconds}
+    for prec in ("mixed", "double"):
+        srv = Server(topos, precision=prec, contexts=4)
+        srv.warmup(cases=64)
+        sweep = []
+        for rate in (25, 50, 100, 200, 400, 800):
+            reqs = poisson_stream(topos, rate=float(rate), duration=args.serve_seconds, seed=rate)
+            s = latency_summary(srv.run(reqs))
+            sweep.append({"rate_per_s": rate, **{k: (round(v, 3) if isinstance(v, float) else v) for k, v in s.items()}})
+            if s["p99_ms"] > 50.0:
+                break
+        ok = [x for x in sweep if x["p99_ms"] <= 50.0]
+        best = ok[-1] if ok else None
+        out["fp64" if prec == "double" else prec] = {
+            "max_rate_p99_le_50ms": best["rate_per_s"] if best else None,
+            "solves_per_s": best["solves_per_s"] if best else None,
+            "p50_ms": best["p50_ms"] if best else None, "p99_ms": best["p99_ms"] if best else None,
+            "sweep": sweep}
+    return out
+
+
 def gpu_line(args, res, rank, world):
     out = res["out"]
     T = res["T"]
@@ -407,6 +482,8 @@ def gpu_line(args, res, rank, world):
         "fp64": fp64,
         "accuracy": res["accuracy"],
         "n1_sweep": res.get("n1"),
+        "multigrid": res.get("multigrid"),
+        "serving": res.get("serving"),
         "roofline": roof,
         "cpu_baseline": cb,
         "e2e": {"value": round(world * T / (e2e_ms * 1e-3), 1), "unit": "solves/s",
@@ -507,6 +584,9 @@ def main():
     ap.add_argument("--mixed-switch", type=float, default=1e-3)
     ap.add_argument("--cpu-hours", type=int, default=HOURS)
     ap.add_argument("--no-n1", action="store_true", help="skip the N-1 sweep block")
+    ap.add_argument("--no-multigrid", action="store_true", help="skip the uneven multi-grid block")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving block")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving stream")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":  # rank 0 alone times the CPU reference; other ranks exit at once
@@ -517,6 +597,10 @@ def main():
     res = run_gpu(args, rank, world, local)
     if rank == 0 and not args.no_n1:
         res["n1"] = run_n1(args)
+    if rank == 0 and not args.no_multigrid:
+        res["multigrid"] = run_multigrid(args)
+    if rank == 0 and not args.no_serving:
+        res["serving"] = run_serving(args)
     line = gpu_line(args, res, rank, world)
     if line is not None:
         print(json.dumps(line), flush=True)

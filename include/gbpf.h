@@ -175,6 +175,14 @@ typedef struct gbpf_job {
     int32_t* iterations;     /* out: (n_cases,) */
     uint8_t* converged;      /* out: (n_cases,) */
     int cases_per_cta;       /* 0: by the group rule (fewer for large grids), else a power of two <= 32 */
+    /* Outage cases (the solver's branch table set by gbpf_set_branches; S and V0 (n,)): case c
+     * removes branches out_idx[out_ptr[c] .. out_ptr[c+1]) (at most 8). Islands are found on the
+     * device (gbpf_islands semantics, reslack as given); an island re-slacked to bus r starts
+     * rotated so that r has angle 0 (r pinned at |V0[r]| + 0j); unserved buses are pinned at
+     * 1 + 0j and returned as NaN. NULL: not an outage job. */
+    const int32_t* out_ptr;
+    const int32_t* out_idx;
+    int reslack;
 } gbpf_job;
 
 gbpf_group* gbpf_group_create(void);
@@ -201,6 +209,13 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
 int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
                  const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
                  int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands);
+
+/* Branch table of the topology for outage cases: branch e joins f[e] - t[e]; its 2x2 stamp
+ * (Yff, Yft, Ytf, Ytt) sits at CSR positions stamp_pos[4e .. 4e+3] with values stamp_val (4
+ * complex per branch, the values an outage subtracts; case_generator.py:270-317, 505-524);
+ * is_slack (n), gen_prio (n, re-slack ranking; NULL = none). */
+int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const int32_t* stamp_pos,
+                      const double* stamp_val, const uint8_t* is_slack, const double* gen_prio);
 
 /* gbpf_islands for the topology of `s` (n = its bus count) on the solver's stream, with
  * device buffers the solver keeps and grows (no allocation once they are large enough):

@@ -135,12 +135,16 @@ struct gbpf_solver {
     DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab, bjobs;
     // islanding buffers (grow-only)
     DBuf iin, iscr, ibest, iout;
+    // branch table for outage cases (gbpf_set_branches)
+    int m = 0;
+    DBuf dbr_f, dbr_t, dbr_live, dbr_pos, dbr_val, dslack, dprio;
     gbpf_stats last{};
     ~gbpf_solver() {
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
-                        &btab, &bjobs, &iin, &iscr, &ibest, &iout})
+                        &btab, &bjobs, &iin, &iscr, &ibest, &iout, &dbr_f, &dbr_t, &dbr_live, &dbr_pos, &dbr_val,
+                        &dslack, &dprio})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -499,12 +503,12 @@ struct gbpf_group {
     int device = 0, nsm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
-    DBuf scr, bjobs, bctl, btab, bin, bout;
+    DBuf scr, bjobs, bctl, btab, bin, bout, bisl;
     gbpf_stats last{};
     int fixed_NT = 0;              // threads per CTA (0: by the group rule)
     int slot_budget = 8192;        // variable buses x case slots a CTA may hold per job
     ~gbpf_group() {
-        for (DBuf* b : {&scr, &bjobs, &bctl, &btab, &bin, &bout}) b->release();
+        for (DBuf* b : {&scr, &bjobs, &bctl, &btab, &bin, &bout, &bisl}) b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -524,6 +528,11 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
             return fail(std::string(who) + ": job " + std::to_string(j) + " lacks an input or output array");
         if (J.cases_per_cta < 0 || J.cases_per_cta > gbpf::MAX_SLOTS || (J.cases_per_cta & (J.cases_per_cta - 1)))
             return fail(std::string(who) + ": job " + std::to_string(j) + ": cases_per_cta must be 0 or a power of two in 1..32");
+        if (J.out_ptr) {
+            if (!J.solver->m) return fail(std::string(who) + ": job " + std::to_string(j) + ": outage cases need the solver's branch table (gbpf_set_branches)");
+            if (J.s_per_col || J.v0_per_col || !J.out_idx)
+                return fail(std::string(who) + ": job " + std::to_string(j) + ": outage cases take one S and one V0 (n,) and out_ptr / out_idx");
+        }
         units += J.n_cases;
     }
     int NT = 0, Gmax = 0;
@@ -542,8 +551,26 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
     unsigned long long cta_bytes = 0;
     long long want = 0;
     int occ = 1 << 20;
-    size_t tab_bytes = 0;
-    for (int j = 0; j < nj; ++j) tab_bytes += jobs[j].v0_per_col ? 0 : (size_t)jobs[j].solver->n * 64;
+    size_t tab_bytes = 0, isl_bytes = 0;
+    auto up256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    for (int j = 0; j < nj; ++j) {
+        const gbpf_job& J = jobs[j];
+        tab_bytes += J.v0_per_col ? 0 : (size_t)J.solver->n * 64;
+        if (J.out_ptr) {
+            const size_t n = J.solver->n, L = J.n_cases, gi = std::min<size_t>(L, 4 * (size_t)g->nsm);
+            isl_bytes += 3 * up256(n * L * 4) + up256(L * 4) + up256(gi * 4 * n * 4) + up256(gi * n * 8);
+        }
+    }
+    CK(g->bisl.ensure(std::max<size_t>(isl_bytes, 256)));
+    size_t isl_at = 0;
+    struct IslLaunch {
+        const gbpf_solver* s;
+        const gbpf_job* J;
+        int *labels, *served_i, *ref_bus, *nis, *scr, *err;
+        unsigned long long* best;
+        int grid;
+    };
+    std::vector<IslLaunch> isl;
     CK(g->bctl.ensure((size_t)nj * 32 * sizeof(unsigned long long)));
     CK(g->btab.ensure(std::max<size_t>(tab_bytes, 64)));
     auto* ctl = g->bctl.as<unsigned long long>();
@@ -586,12 +613,36 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
             b.st_k = J.st_k;
             b.st_v = reinterpret_cast<const double2*>(J.st_val);
         }
+        unsigned long long* c = ctl + (size_t)q * 32;
+        if (J.out_ptr) {  // outage cases: islands on the device, stamps from the branch table
+            const size_t n = s->n, L = J.n_cases;
+            char* base = g->bisl.as<char>() + isl_at;
+            IslLaunch il{};
+            il.s = s;
+            il.J = &J;
+            il.labels = reinterpret_cast<int*>(base);
+            il.ref_bus = reinterpret_cast<int*>(base + up256(n * L * 4));
+            il.served_i = reinterpret_cast<int*>(base + 2 * up256(n * L * 4));
+            il.nis = reinterpret_cast<int*>(base + 3 * up256(n * L * 4));
+            il.grid = (int)std::min<size_t>(L, 4 * (size_t)g->nsm);
+            il.scr = reinterpret_cast<int*>(base + 3 * up256(n * L * 4) + up256(L * 4));
+            il.best = reinterpret_cast<unsigned long long*>(base + 3 * up256(n * L * 4) + up256(L * 4) +
+                                                            up256((size_t)il.grid * 4 * n * 4));
+            il.err = reinterpret_cast<int*>(c + 24) + 6;
+            isl_at += 3 * up256(n * L * 4) + up256(L * 4) + up256((size_t)il.grid * 4 * n * 4) +
+                      up256((size_t)il.grid * n * 8);
+            isl.push_back(il);
+            b.ymode = 3;
+            b.out_ptr = J.out_ptr;
+            b.out_idx = J.out_idx;
+            b.ref_bus = il.ref_bus;
+            b.sref = (long long)L;
+        }
         b.Vout = reinterpret_cast<double2*>(J.V);
         b.sV = J.n_cases;
         b.iters = J.iterations;
         b.conv = J.converged;
         fill_common(b, s, p);
-        unsigned long long* c = ctl + (size_t)q * 32;
         b.counter = reinterpret_cast<int*>(c + 16);
         b.stats = c;
         b.err = reinterpret_cast<int*>(c + 24);
@@ -612,6 +663,14 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         if (b.v0_shared)
             CK(gbpf::launch_v0_table(b.V0, hj[q].P.n, b.check_v0, const_cast<double4_32a*>(b.v0tab), b.err,
                                      g->stream));
+    }
+    for (const IslLaunch& il : isl) {
+        const gbpf_solver* s = il.s;
+        CK(gbpf::launch_islands(s->n, s->m, s->dbr_f.as<int>(), s->dbr_t.as<int>(), s->dbr_live.as<uint8_t>(),
+                                il.J->n_cases, il.J->out_ptr, il.J->out_idx, s->dslack.as<uint8_t>(),
+                                s->dprio.as<double>(), il.J->reslack, il.scr, il.best, il.labels,
+                                reinterpret_cast<uint8_t*>(il.served_i), il.ref_bus, il.nis, il.err, il.grid,
+                                g->stream));
     }
     CK(gbpf::launch_newton(L, grid, NT, g->stream));
     CK(cudaEventRecord(g->e1, g->stream));
@@ -646,6 +705,10 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         if (err[0] == gbpf::DE_STAMPS)
             return fail(job + "case " + std::to_string(err[2]) + " has " + std::to_string(err[1]) +
                         " outage stamp entries, more than the " + std::to_string(gbpf::MAX_STAMPS) + " supported");
+        if (err[0] == gbpf::DE_OUTAGE)
+            return fail(job + "case " + std::to_string(err[2]) + " outages branch " + std::to_string(err[1]) +
+                        ", which does not exist");
+        if (err[6]) return fail(job + "island labels did not settle");
     }
     return 0;
 }
@@ -1012,6 +1075,45 @@ void gbpf_host_free(void* p) {
     if (p) cudaFreeHost(p);
 }
 
+int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const int32_t* stamp_pos,
+                      const double* stamp_val, const uint8_t* is_slack, const double* gen_prio) {
+    if (!s) return fail("null solver");
+    if (m <= 0 || !f || !t || !stamp_pos || !stamp_val || !is_slack) return fail("set_branches: invalid arguments");
+    const int n = s->n;
+    std::vector<uint8_t> live(m);
+    for (int e = 0; e < m; ++e) {
+        if (f[e] < 0 || f[e] >= n || t[e] < 0 || t[e] >= n) return fail("set_branches: branch end out of range");
+        for (int q = 0; q < 4; ++q)
+            if (stamp_pos[4 * e + q] < 0 || stamp_pos[4 * e + q] >= s->nnz)
+                return fail("set_branches: stamp position out of range");
+        // a branch couples its ends while its transfer admittances are nonzero
+        live[e] = (stamp_val[8 * (size_t)e + 2] != 0.0 || stamp_val[8 * (size_t)e + 3] != 0.0 ||
+                   stamp_val[8 * (size_t)e + 4] != 0.0 || stamp_val[8 * (size_t)e + 5] != 0.0);
+    }
+    std::vector<int> vf(f, f + m), vt(t, t + m), vp(stamp_pos, stamp_pos + 4 * (size_t)m);
+    std::vector<double> vv(stamp_val, stamp_val + 8 * (size_t)m);
+    std::vector<uint8_t> vs(is_slack, is_slack + n);
+    std::vector<double> vprio(n, 0.0);
+    if (gen_prio) vprio.assign(gen_prio, gen_prio + n);
+    CK(upload(s->dbr_f, vf));
+    CK(upload(s->dbr_t, vt));
+    CK(upload(s->dbr_live, live));
+    CK(upload(s->dbr_pos, vp));
+    CK(upload(s->dbr_val, vv));
+    CK(upload(s->dslack, vs));
+    CK(upload(s->dprio, vprio));
+    s->m = m;
+    auto fill = [&](gbpf::DevPlan& d) {
+        d.m = m;
+        d.br_pos = s->dbr_pos.as<int4>();
+        d.br_val = s->dbr_val.as<double2>();
+        d.is_slack = s->dslack.as<uint8_t>();
+    };
+    fill(s->dp);
+    for (auto& sh : s->shapes) fill(sh->dp);
+    return 0;
+}
+
 int gbpf_solver_islands(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
                         const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack, const double* gen_prio,
                         int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus, int32_t* n_islands) {
@@ -1128,6 +1230,17 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
         in_bytes += up(n * (J.s_per_col ? T : 1) * 16) + up(n * (J.v0_per_col ? T : 1) * 16) + (J.pin ? up(n * T) : 0);
         if (J.st_ptr) in_bytes += up((T + 1) * 4) + up((size_t)std::max(J.st_ptr[T], 1) * 4) +
                                   up((size_t)std::max(J.st_ptr[T], 1) * 16);
+        if (J.out_ptr) {
+            if (!J.out_idx || J.out_ptr[0] != 0) return fail("group_solve: job " + std::to_string(j) + ": outage pointers must start at 0");
+            for (size_t c = 0; c < T; ++c)
+                if (J.out_ptr[c + 1] < J.out_ptr[c] || J.out_ptr[c + 1] - J.out_ptr[c] > gbpf::MAX_STAMPS / 4)
+                    return fail("group_solve: job " + std::to_string(j) + " case " + std::to_string(c) +
+                                ": at most " + std::to_string(gbpf::MAX_STAMPS / 4) + " outaged branches per case");
+            for (int e = 0; e < J.out_ptr[T]; ++e)
+                if (J.out_idx[e] < 0 || J.out_idx[e] >= J.solver->m)
+                    return fail("group_solve: job " + std::to_string(j) + ": outage branch index out of range");
+            in_bytes += up((T + 1) * 4) + up((size_t)std::max(J.out_ptr[T], 1) * 4);
+        }
         out_at[j] = out_bytes;
         out_bytes += up(n * T * 16) + up(T * 4) + up(T);
     }
@@ -1160,6 +1273,11 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
             D.st_ptr = static_cast<const int32_t*>(put(J.st_ptr, (T + 1) * 4));
             D.st_k = static_cast<const int32_t*>(put(J.st_k, ne * 4));
             D.st_val = static_cast<const double*>(put(J.st_val, ne * 16));
+            CK(g_copy_error);
+        }
+        if (J.out_ptr) {
+            D.out_ptr = static_cast<const int32_t*>(put(J.out_ptr, (T + 1) * 4));
+            D.out_idx = static_cast<const int32_t*>(put(J.out_idx, (size_t)J.out_ptr[T] * 4));
             CK(g_copy_error);
         }
         char* o = g->bout.as<char>() + out_at[j];

@@ -29,6 +29,7 @@ enum DevError : int {
     DE_V0_NONFINITE = 1,
     DE_V0_MAGNITUDE = 2,
     DE_STAMPS = 3,
+    DE_OUTAGE = 4,           // a case's outage list is malformed (err[1] = index, err[2] = case)
 };
 
 struct DevPlan {
@@ -50,6 +51,11 @@ struct DevPlan {
     const uint8_t* row_pq;   // block row is PQ (two real pivots)
     const int* bus_of_row;
     const int* dpos;         // block row -> its diagonal block (base)
+    // branch table (outage mode): per branch its 4 Ybus CSR positions and stamp values
+    int m;
+    const int4* br_pos;
+    const double2* br_val;   // [branch][4]
+    const uint8_t* is_slack; // [bus]
 };
 
 struct Batch {
@@ -65,12 +71,17 @@ struct Batch {
     long long sV0;
     const double4_32a* v0tab; // shared start: per bus (Vm, Va, cos, sin), (e, f, 1/Vm, 0)
     int check_v0;            // validate V0 like nr_klu's solve_batch
-    int ymode;               // 0 base Ybus, 1 base minus per-case stamps, 2 dense per case
+    int ymode;               // 0 base Ybus, 1 base minus per-case stamps, 2 dense per case,
+                             // 3 base minus the stamps of per-case branch outages (out_ptr / out_idx)
     const int* st_ptr;       // stamps of case c: [st_ptr[c], st_ptr[c+1])
     const int* st_k;
     const double2* st_v;
     const double2* Yd;       // dense per-case Ybus Yd[k * sYd + case]
     long long sYd;
+    const int* out_ptr;      // outage mode: case c removes branches out_idx[out_ptr[c] .. out_ptr[c+1])
+    const int* out_idx;
+    const int* ref_bus;      // island reference bus of every bus and case [bus * sref + case] (-1
+    long long sref;          // unserved) or null: starts rotated to the reference, pins, NaN output
     const uint8_t* pin;      // pin[bus * spin + case] or null
     long long spin;
     double2* Vout;           // result Vout[bus * sV + case]

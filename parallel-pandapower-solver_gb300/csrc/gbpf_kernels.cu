@@ -596,7 +596,36 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
                     int nst = 0;
-                    if (Bt.ymode == 1) {
+                    if (Bt.ymode == 3) {  // the stamps of the case's outaged branches
+                        const int e0 = Bt.out_ptr[c], e1 = Bt.out_ptr[c + 1];
+                        int nb = e1 - e0;
+                        if (nb < 0 || 4 * nb > MAX_STAMPS) {
+                            if (atomicCAS(&Bt.err[0], 0, DE_STAMPS) == 0) {
+                                Bt.err[1] = 4 * nb;
+                                Bt.err[2] = (int)c;
+                            }
+                            nb = nb < 0 ? 0 : MAX_STAMPS / 4;
+                        }
+                        for (int q = 0; q < nb; ++q) {
+                            const int b = Bt.out_idx[e0 + q];
+                            if (b < 0 || b >= P.m) {  // never indexes the branch table out of range
+                                if (atomicCAS(&Bt.err[0], 0, DE_OUTAGE) == 0) {
+                                    Bt.err[1] = b;
+                                    Bt.err[2] = (int)c;
+                                }
+                                continue;
+                            }
+                            const int4 pos = P.br_pos[b];
+                            s_stk[s][nst] = pos.x;
+                            s_stv[s][nst++] = P.br_val[4 * b];
+                            s_stk[s][nst] = pos.y;
+                            s_stv[s][nst++] = P.br_val[4 * b + 1];
+                            s_stk[s][nst] = pos.z;
+                            s_stv[s][nst++] = P.br_val[4 * b + 2];
+                            s_stk[s][nst] = pos.w;
+                            s_stv[s][nst++] = P.br_val[4 * b + 3];
+                        }
+                    } else if (Bt.ymode == 1) {
                         const int e0 = Bt.st_ptr[c], e1 = Bt.st_ptr[c + 1];
                         nst = e1 - e0;
                         if (nst > MAX_STAMPS) {
@@ -662,7 +691,40 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 Ei[idx] = iv;
                 V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), d2f_fast(iv), 0.f);
             }
-            spin[idx] = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
+            uint8_t pinned = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
+            if (Bt.ref_bus) {
+                // islands of an outage case (solver_cpp.py:121-134): an unserved bus is pinned at
+                // 1 + 0j; an island re-slacked to bus r starts rotated so that r has angle 0 (r
+                // itself at |v0| + 0j, pinned); islands holding a slack keep the start as it is
+                const int r = Bt.ref_bus[(size_t)bus * Bt.sref + c];
+                if (r < 0 || !P.is_slack[r]) {
+                    double4_32a v;
+                    double iv;
+                    if (r < 0) {
+                        v = make_double4_32a(1.0, 0.0, 1.0, 0.0);
+                        iv = 1.0;
+                        pinned = 1;
+                    } else {
+                        const double4_32a t0 = Vt[idx];
+                        iv = Ei[idx];
+                        if (r == bus) {
+                            v = make_double4_32a(t0.x, 0.0, 1.0, 0.0);
+                            pinned = 1;
+                        } else {
+                            const double4_32a tr = Bt.v0tab[2 * r];
+                            v = make_double4_32a(t0.x, t0.y - tr.y, fma(t0.z, tr.z, t0.w * tr.w),
+                                                 fma(t0.w, tr.z, -t0.z * tr.w));
+                        }
+                    }
+                    Vc[idx] = v;
+                    Vt[idx] = v;
+                    const double e = v.x * v.z, f = v.x * v.w;
+                    Et[idx] = make_double2(e, f);
+                    Ei[idx] = iv;
+                    V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), d2f_fast(iv), 0.f);
+                }
+            }
+            spin[idx] = pinned;
         }
 
         // ---------------------------------------------------------------- linear solve
@@ -706,7 +768,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 const int bus = idx >> lg;
                 const int row = P.row_of_bus[bus];
                 if (row < 0) continue;
-                EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
+                EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
                 eval_row<1>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0), fac64, R,
                             false);
             }
@@ -804,7 +866,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
             const bool pinned = spin[idx] != 0;
             const bool pq = P.bus_pq[bus] != 0;
-            EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
+            EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;
             if (st == SL_BACKTRACK)
                 worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
@@ -907,7 +969,10 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             if (s_st[s] != SL_FINISH) continue;
             const int bus = idx >> lg;
             const double4_32a v = Vt[idx];
-            Bt.Vout[(size_t)bus * Bt.sV + s_case[s]] = make_double2(v.x * v.z, v.x * v.w);
+            double2 o = make_double2(v.x * v.z, v.x * v.w);
+            if (Bt.ref_bus && Bt.ref_bus[(size_t)bus * Bt.sref + s_case[s]] < 0)
+                o = make_double2(__longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0x7ff8000000000000LL));
+            Bt.Vout[(size_t)bus * Bt.sV + s_case[s]] = o;
         }
         __syncthreads();
         if (tid < G && s_st[tid] == SL_FINISH) {

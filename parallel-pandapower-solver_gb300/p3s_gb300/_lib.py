@@ -90,6 +90,9 @@ class Job(C.Structure):
         ("iterations", _vp),
         ("converged", _vp),
         ("cases_per_cta", C.c_int),
+        ("out_ptr", _vp),
+        ("out_idx", _vp),
+        ("reslack", C.c_int),
     ]
 
 
@@ -129,6 +132,7 @@ SIGNATURES = {
     "gbpf_group_solve_device": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
     "gbpf_group_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_group_set_shape": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "gbpf_set_branches": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, _bp, _dp]),
     "gbpf_solver_islands": (C.c_int, [_vp, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                       _ip, _ip]),
     "gbpf_islands_device_static": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, _vp,

@@ -145,28 +145,64 @@ def start_and_pins(batch: ContingencyBatch, v_start, served, ref_bus):
     return np.ascontiguousarray(V0), np.ascontiguousarray(pin)
 
 
+def outage_lists(groups):
+    """(ptr (L+1,), idx) int32 outage lists of case groups (branch index lists)."""
+    ptr = np.zeros(len(groups) + 1, dtype=np.int32)
+    ptr[1:] = np.cumsum([len(g) for g in groups])
+    idx = np.concatenate([np.asarray(g, dtype=np.int32) for g in groups]) if ptr[-1] else np.zeros(0, np.int32)
+    return ptr, idx.astype(np.int32)
+
+
 def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, max_iter: int = 30,
-                        precision: str = "double", groups=None, gen_prio=None, v_start=None, solver=None):
+                        precision: str = "double", groups=None, gen_prio=None, v_start=None, solver=None,
+                        return_islands: bool = True):
     """Solve every N-1 case of ``grid`` on the device (``solve_contingencies_cuda`` semantics,
-    solver_cuda.py:30-119, with ``init="flat"``)."""
-    batch = build_batch(grid, groups)
-    n = batch.n_bus
-    if len(batch.groups) == 0:
+    solver_cuda.py:30-119, with ``init="flat"``).
+
+    The grid's branch table stays resident with the solver; every case is an outage list, so
+    islanding, the re-slack start and the outage-patched Ybus are all made on the device in the
+    solve's launch (no per-case arrays cross the bus but the results). Unserved buses come back
+    as NaN. ``return_islands`` adds the island labels and reference buses (one more islanding
+    call); without it ``served`` is read off the NaNs."""
+    from .group import GpuGroup, GroupJob
+
+    n = grid.n
+    if groups is None:
+        groups = [[]] + [[b] for b in range(grid.n_branch)]
+    groups = [list(map(int, g)) for g in groups]
+    if len(groups) == 0:
         e = np.empty((n, 0))
         return ContingencyResultTable([], e.astype(np.complex128), e.astype(bool), np.empty(0, bool),
                                       np.empty(0, int))
     if gen_prio is None:
         gen_prio = np.zeros(n)
         gen_prio[grid.pv] = np.maximum(grid.p_gen[grid.pv], np.finfo(float).tiny)
-    labels, served, ref_bus, _ = islands(batch, reslack_islands, gen_prio)
+    gen_prio = np.ascontiguousarray(gen_prio, dtype=np.float64)
     if v_start is None:
         v_start = grid.V0
-    V0, pin = start_and_pins(batch, v_start, served, ref_bus)
     if solver is None:
-        solver = PolarNewtonSolverCUDA(batch.Yp, batch.Yj, batch.Yx_base, batch.pv, batch.pq)
+        solver = PolarNewtonSolverCUDA(grid.Yp, grid.Yj, grid.Yx, grid.pv, grid.pq)
+    gs = solver._s
+    key = (id(grid), gen_prio.tobytes())
+    if getattr(solver, "_branch_key", None) != key:
+        is_slack = np.zeros(n, dtype=np.uint8)
+        is_slack[np.asarray(grid.ref, dtype=np.int64)] = 1
+        gs.set_branches(grid.f, grid.t, grid.stamp_pos, grid.stamp, is_slack, gen_prio)
+        solver._branch_key = key
+    if getattr(solver, "_group", None) is None:
+        solver._group = GpuGroup()
     solver.precision = precision
-    res = solver.solve_batch_contingency_stamp(batch.stamp, grid.Sbus, V0, pin, max_iter=max_iter, tol=tol)
-    V = res["V"].copy()
-    V[~served] = np.nan
-    return ContingencyResultTable(batch.groups, V, served, np.asarray(res["converged"], bool),
+    ptr, idx = outage_lists(groups)
+    job = GroupJob(gs, np.asarray(grid.Sbus), np.asarray(v_start), n_cases=len(groups), outages=(ptr, idx),
+                   reslack=reslack_islands)
+    res = solver._group.solve([job], solver._params(max_iter, tol))[0]
+    solver._record(len(groups), res, solver._group.stats)
+    V = res["V"]
+    labels = ref_bus = None
+    if return_islands:
+        batch = build_batch(grid, groups)
+        labels, served, ref_bus, _ = islands(batch, reslack_islands, gen_prio)
+    else:
+        served = ~np.isnan(V)
+    return ContingencyResultTable(groups, V, served, np.asarray(res["converged"], bool),
                                   np.asarray(res["iterations"], int), labels, ref_bus)

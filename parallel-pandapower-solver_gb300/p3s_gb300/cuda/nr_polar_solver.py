@@ -64,8 +64,8 @@ class PolarNewtonSolverCUDA:
                                 pivot_ratio_double=self._rcond_ratio, pivot_ratio_single=self._rcond_ratio_single,
                                 vote_rule=self.vote_rule, polish=self.polish, vtol=self.vtol)
 
-    def _record(self, B, r):
-        st = self._s.stats
+    def _record(self, B, r, st=None):
+        st = self._s.stats if st is None else st
         failed = int((~r["converged"]).sum())
         self.last_stats = {
             "systems": B,

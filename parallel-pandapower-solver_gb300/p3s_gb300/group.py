@@ -22,7 +22,9 @@ from .solver import GpuSolver, c128
 @dataclass
 class GroupJob:
     """One topology's cases. S: (n, T) or (n,) with T from V0; V0: (n,) or (n, T); pin: (n, T)
-    or None; stamps: (ptr (T+1,), k, val) outage stamps subtracted from the base Ybus, or None."""
+    or None; stamps: (ptr (T+1,), k, val) outage stamps subtracted from the base Ybus, or None;
+    outages: (ptr (T+1,), idx) branch outages of every case, islanded on the device (the
+    solver's branch table must be set, S and V0 are (n,)), or None."""
 
     solver: GpuSolver
     S: np.ndarray
@@ -31,6 +33,8 @@ class GroupJob:
     pin: np.ndarray | None = None
     stamps: tuple | None = None
     cases_per_cta: int = 0
+    outages: tuple | None = None
+    reslack: bool = True
 
 
 class GpuGroup:
@@ -101,6 +105,14 @@ class GpuGroup:
                 keep += [ptr, k, val]
             J.V, J.iterations, J.converged = V.ctypes.data, it.ctypes.data, cv.ctypes.data
             J.cases_per_cta = int(jb.cases_per_cta)
+            if jb.outages is not None:
+                optr, oidx = jb.outages
+                optr = np.ascontiguousarray(optr, dtype=np.int32)
+                oidx = np.ascontiguousarray(oidx, dtype=np.int32)
+                if optr.shape != (T + 1,):
+                    raise ValueError(f"job {i}: outage pointers must be (T + 1,)")
+                J.out_ptr, J.out_idx, J.reslack = optr.ctypes.data, oidx.ctypes.data, int(bool(jb.reslack))
+                keep += [optr, oidx]
             outs.append((V, it, cv))
         rc = _lib.load().gbpf_group_solve(self._h, len(jobs), arr, C.byref(params))
         _lib.check(rc, "group_solve")

@@ -30,7 +30,6 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib
 from .group import GpuGroup, GroupJob
 from .solver import GpuSolver, c128
 
@@ -86,45 +85,23 @@ class Topology:
             raise RuntimeError(f"{self.name}: the base case does not converge")
         self.V_warm = np.ascontiguousarray(base["V"][:, 0])
         self.f = np.ascontiguousarray(grid.f, dtype=np.int32)
-        self.t = np.ascontiguousarray(grid.t, dtype=np.int32)
-        self.live = np.ascontiguousarray((grid.stamp[:, 1] != 0) | (grid.stamp[:, 2] != 0), dtype=np.uint8)
         self.is_slack = np.zeros(self.n, dtype=np.uint8)
         self.is_slack[np.asarray(grid.ref, dtype=np.int64)] = 1
         self.prio = np.zeros(self.n)
         self.prio[grid.pv] = np.maximum(grid.p_gen[grid.pv], np.finfo(float).tiny)
+        # the branch table stays resident: N-1 cases are islanded and patched on the device
+        self.solver.set_branches(grid.f, grid.t, grid.stamp_pos, grid.stamp, self.is_slack, self.prio)
 
     def slot_bytes(self, mixed: bool) -> int:
         return _slot_bytes(self.n, self.nv, self.nblk, mixed)
 
-    def n1_job(self, outages: np.ndarray, S_base: np.ndarray):
-        """Islanding of the outage cases on the device, then V0 / pin / stamps of the job."""
+    def n1_job(self, outages: np.ndarray, S_base: np.ndarray) -> GroupJob:
+        """Single-branch outage cases from the warm start: the launch islands them, re-slacks
+        islands (each starting rotated to its new reference) and patches the Ybus on the device."""
         L = len(outages)
         ptr = np.arange(L + 1, dtype=np.int32)
         idx = np.ascontiguousarray(outages, dtype=np.int32)
-        labels = np.empty((self.n, L), dtype=np.int32)
-        served = np.empty((self.n, L), dtype=np.uint8)
-        ref_bus = np.empty((self.n, L), dtype=np.int32)
-        nis = np.empty(L, dtype=np.int32)
-        rc = _lib.load().gbpf_solver_islands(self.solver._h, len(self.f), _lib.i32(self.f), _lib.i32(self.t),
-                                             _lib.u8(self.live), L, _lib.i32(ptr), _lib.i32(idx),
-                                             _lib.u8(self.is_slack), _lib.d(self.prio), 1, _lib.i32(labels),
-                                             _lib.u8(served), _lib.i32(ref_bus), _lib.i32(nis))
-        _lib.check(rc, "solver_islands")
-        served = served.astype(bool)
-        V0 = np.repeat(self.V_warm[:, None], L, axis=1)
-        pin = np.zeros((self.n, L), dtype=np.uint8)
-        bus = np.arange(self.n)[:, None]
-        is_ref = (ref_bus == bus) & ~self.is_slack.astype(bool)[:, None]
-        V0[is_ref] = np.abs(np.broadcast_to(self.V_warm[:, None], V0.shape)[is_ref]) + 0j
-        pin[is_ref] = 1
-        V0[~served] = 1.0 + 0.0j
-        pin[~served] = 1
-        sp_ = np.arange(0, 4 * L + 1, 4, dtype=np.int32)
-        sk = np.ascontiguousarray(self.grid.stamp_pos[idx].ravel(), dtype=np.int32)
-        sv = c128(self.grid.stamp[idx].ravel())
-        job = GroupJob(self.solver, c128(S_base).ravel(), np.ascontiguousarray(V0), n_cases=L, pin=pin,
-                       stamps=(sp_, sk, sv))
-        return job, served
+        return GroupJob(self.solver, c128(S_base).ravel(), self.V_warm, n_cases=L, outages=(ptr, idx), reslack=True)
 
 
 @dataclass
@@ -132,7 +109,7 @@ class _Launch:
     seq: int
     requests: list
     jobs: list
-    served: dict = field(default_factory=dict)  # rid -> served mask (n1)
+    served: dict = field(default_factory=dict)  # rids of N-1 requests (served = not NaN)
     start: float = 0.0
 
 
@@ -164,9 +141,8 @@ class Server:
             jobs.append(GroupJob(big.solver, big.grid.Sbus, big.V_warm, n_cases=max(cases, 1)))
             jobs += [GroupJob(tp.solver, tp.grid.Sbus, tp.V_warm, n_cases=cases) for tp in self.topos]
             grp.solve(jobs, self.params)
-            for tp in self.topos:
-                job, _ = tp.n1_job(np.arange(min(4, len(tp.f)), dtype=np.int32), tp.grid.Sbus)
-                grp.solve([job], self.params)
+            grp.solve([tp.n1_job(np.arange(min(64, len(tp.f)), dtype=np.int32), tp.grid.Sbus) for tp in self.topos],
+                      self.params)
 
     # ------------------------------------------------------------------ batching
     def _cases(self, r: Request) -> int:
@@ -216,14 +192,13 @@ class Server:
         for k, rs in n1.items():
             tp = self.topos[k]
             out = np.concatenate([r.outages for r in rs])
-            job, sv = tp.n1_job(out, rs[0].S)
-            jobs.append(job)
+            jobs.append(tp.n1_job(out, rs[0].S))
             at = 0
             spans = []
             for r in rs:
                 L = len(r.outages)
                 spans.append((r, at, at + L))
-                served[r.rid] = sv[:, at:at + L]
+                served[r.rid] = True
                 at += L
             layout.append(spans)
         return jobs, layout, served
@@ -254,9 +229,7 @@ class Server:
                 for job_res, spans in zip(res, layout):
                     for r, a, b in spans:
                         V = job_res["V"][:, a:b].copy()
-                        sv = launch.served.get(r.rid)
-                        if sv is not None:
-                            V[~sv] = np.nan
+                        sv = ~np.isnan(V) if r.rid in launch.served else None  # unserved buses are NaN
                         out.append(Response(r.rid, V, job_res["iterations"][a:b].copy(),
                                             job_res["converged"][a:b].copy(), r.arrival, launch.start, done,
                                             launch.seq, sv))

@@ -126,6 +126,23 @@ class GpuSolver:
                            float(pivot_ratio_single), 0 if vote_rule == "reference" else 1, float(polish),
                            float(vtol))
 
+    def set_branches(self, f, t, stamp_pos, stamp, is_slack, gen_prio=None):
+        """Branch table for outage cases: ends (m,), stamp CSR positions (m, 4) and values (m, 4)
+        complex (Yff, Yft, Ytf, Ytt), slack flags (n,), re-slack priorities (n,) or None."""
+        f = np.ascontiguousarray(f, dtype=np.int32)
+        t = np.ascontiguousarray(t, dtype=np.int32)
+        pos = np.ascontiguousarray(stamp_pos, dtype=np.int32)
+        val = c128(stamp)
+        sl = np.ascontiguousarray(is_slack, dtype=np.uint8)
+        pr = None if gen_prio is None else np.ascontiguousarray(gen_prio, dtype=np.float64)
+        m = len(f)
+        if t.shape != (m,) or pos.shape != (m, 4) or val.shape != (m, 4) or sl.shape != (self.n,):
+            raise ValueError("set_branches: f, t (m,), stamp_pos / stamp (m, 4), is_slack (n_bus,)")
+        rc = _lib.load().gbpf_set_branches(self._h, m, _lib.i32(f), _lib.i32(t), _lib.i32(pos), _lib.cview(val),
+                                           _lib.u8(sl), None if pr is None else _lib.d(pr))
+        _lib.check(rc, "set_branches")
+        self.branches = m
+
     # -------------------------------------------------------------- values
     def update_Y(self, Yx):
         Yx = c128(Yx)
