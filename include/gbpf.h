@@ -240,6 +240,37 @@ int gbpf_islands_device_static(int n, int m, const int32_t* d_f, const int32_t* 
                                const uint8_t* d_is_slack, const double* d_gen_prio, int reslack, int32_t* d_labels,
                                uint8_t* d_served, int32_t* d_ref_bus, int32_t* d_n_islands, void* stream);
 
+/* ------------------------------------------------------------- either side of the path
+ * Time-series injections (p3s/timeseries.py:36-141, build_sbus_matrix / _fill_sbus):
+ * out[i, t] = s0[i] + sum_k coef[k] * (series[row[k] * T + t] - base[k]) over k = ptr[i] ..
+ * ptr[i+1] - 1 in that order, added to the imaginary part where imag[k]. s0 (n) and out (n, T)
+ * complex; series (R, T) float64 (every element-variable series stacked). Same operations and
+ * order as the reference's loop, without fused multiply-adds. The _device variant takes device
+ * pointers and runs on `stream` (a cudaStream_t; NULL = legacy default stream). */
+int gbpf_build_sbus(int n, int T, int R, const double* s0, const int64_t* ptr, const int32_t* row, const double* coef,
+                    const double* base, const uint8_t* imag, const double* series, double* out);
+int gbpf_build_sbus_device(int n, int T, const double* s0, const int64_t* ptr, const int32_t* row, const double* coef,
+                           const double* base, const uint8_t* imag, const double* series, double* out, void* stream);
+
+/* Branch flows and loading of L solved cases (p3s/contingency/find_overloads.py:128-260,
+ * compute_branch_loading): branch b joins f[b] -> t[b] with 2x2 admittance y[4b..4b+3] =
+ * (Yff, Yft, Ytf, Ytt) complex; S_from = conj(Yff V_f + Yft V_t) V_f sn_mva, S_to likewise;
+ * i_end = |S_end| / (vn_end |V_end| sqrt 3) (kA); i_max = max; loading = i_max / rating x 100
+ * (kind 0, line: rating in kA) or max(i_from vn_from, i_to vn_to) sqrt 3 / rating x 100 (kind
+ * 1, trafo: rating in MVA). Case c's outaged branches out_idx[out_ptr[c] ..] (out_ptr NULL:
+ * none) report 0, non-converged cases NaN, NaN voltages propagate. V (n, L) complex; outputs
+ * (nbr, L). */
+int gbpf_branch_flows(int n, int nbr, int L, const int32_t* f, const int32_t* t, const double* y,
+                      const double* vn_from, const double* vn_to, const double* rating, const uint8_t* kind,
+                      double sn_mva, const double* V, const uint8_t* converged, const int32_t* out_ptr,
+                      const int32_t* out_idx, double* S_from, double* S_to, double* i_from, double* i_to,
+                      double* i_max, double* loading);
+int gbpf_branch_flows_device(int nbr, int L, const int32_t* f, const int32_t* t, const double* y,
+                             const double* vn_from, const double* vn_to, const double* rating, const uint8_t* kind,
+                             double sn_mva, const double* V, const uint8_t* converged, const int32_t* out_ptr,
+                             const int32_t* out_idx, double* S_from, double* S_to, double* i_from, double* i_to,
+                             double* i_max, double* loading, void* stream);
+
 /* Host-only check of the planner and the device schedule (runs without a GPU): plan for
  * `workers` workers, Jacobian at (Vm, Va) with injections S (n complex), the schedule
  * executed serially with a structural race check per level. dx (n x 2): Newton step per

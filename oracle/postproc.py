@@ -1,0 +1,62 @@
+"""Oracle for the steps either side of the Newton path (test infrastructure only).
+
+* ``fill_sbus`` restates the reference's ``_fill_sbus`` (p3s/timeseries.py:122-141): every bus
+  row starts at its base injection and takes its contributions in order, each
+  ``coef * (x - base)`` added to the real or the imaginary part -- numpy, one contribution at
+  a time over all time steps, the same IEEE operations as the reference's loop.
+* ``branch_loading`` restates ``compute_branch_loading`` (p3s/contingency/find_overloads.py:
+  128-260) with the branch admittance rows as scipy sparse matrices, like the reference.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+
+
+def fill_sbus(s0, ptr, row, coef, base, imag, series):
+    n = len(s0)
+    T = series.shape[1]
+    out = np.empty((n, T), dtype=np.complex128)
+    re = np.repeat(np.asarray(s0).real[:, None], T, axis=1)
+    im = np.repeat(np.asarray(s0).imag[:, None], T, axis=1)
+    for i in range(n):
+        for k in range(ptr[i], ptr[i + 1]):
+            d = coef[k] * (series[row[k]] - base[k])
+            if imag[k]:
+                im[i] = im[i] + d
+            else:
+                re[i] = re[i] + d
+    out.real = re
+    out.imag = im
+    return out
+
+
+def branch_loading(n, f, t, y, V, converged, vn_from, vn_to, rating, kind, sn_mva, outaged):
+    """(S_from, S_to, i_from, i_to, i_max, loading), each (nbr, L); outaged (nbr, L) bool."""
+    nbr = len(f)
+    rows = np.repeat(np.arange(nbr), 2)
+    yf = sp.csr_matrix((np.c_[y[:, 0], y[:, 1]].ravel(), (rows, np.c_[f, t].ravel())), shape=(nbr, n))
+    yt = sp.csr_matrix((np.c_[y[:, 2], y[:, 3]].ravel(), (rows, np.c_[f, t].ravel())), shape=(nbr, n))
+    yf.sort_indices()
+    yt.sort_indices()
+    S_from = np.conj(yf @ V) * V[f, :] * sn_mva
+    S_to = np.conj(yt @ V) * V[t, :] * sn_mva
+    vm = np.abs(V)
+    sqrt3 = np.sqrt(3.0)
+    vf = np.asarray(vn_from, dtype=float)[:, None]
+    vt = np.asarray(vn_to, dtype=float)[:, None]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        i_from = np.abs(S_from) / (vf * vm[f, :] * sqrt3)
+        i_to = np.abs(S_to) / (vt * vm[t, :] * sqrt3)
+        i_max = np.maximum(i_from, i_to)
+        line = np.asarray(kind)[:, None] == 0
+        s_max = np.maximum(i_from * vf * sqrt3, i_to * vt * sqrt3)
+        loading = np.where(line, i_max / np.asarray(rating, float)[:, None] * 100.0,
+                           s_max / np.asarray(rating, float)[:, None] * 100.0)
+    for arr in (S_from, S_to, i_from, i_to, i_max, loading):
+        arr[outaged] = 0.0
+    bad = ~np.asarray(converged, dtype=bool)
+    for arr in (S_from, S_to, i_from, i_to, i_max, loading):
+        arr[:, bad] = np.nan
+    return S_from, S_to, i_from, i_to, i_max, loading

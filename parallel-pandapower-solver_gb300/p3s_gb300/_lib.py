@@ -132,6 +132,12 @@ SIGNATURES = {
     "gbpf_group_solve_device": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
     "gbpf_group_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_group_set_shape": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "gbpf_build_sbus": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _lp, _ip, _dp, _dp, _bp, _dp, _dp]),
+    "gbpf_build_sbus_device": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbpf_branch_flows": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _bp, C.c_double, _dp,
+                                    _bp, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "gbpf_branch_flows_device": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, _vp,
+                                           _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbpf_set_branches": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, _bp, _dp]),
     "gbpf_solver_islands": (C.c_int, [_vp, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                       _ip, _ip]),

@@ -17,7 +17,7 @@ CSRC = os.path.join(os.path.dirname(PKG), "csrc")
 INCLUDE = os.path.join(os.path.dirname(os.path.dirname(PKG)), "include")
 LIB = os.path.join(PKG, "libgbpf.so")
 
-CU_SOURCES = ["gbpf.cu", "gbpf_kernels.cu", "islands.cu"]
+CU_SOURCES = ["gbpf.cu", "gbpf_kernels.cu", "islands.cu", "postproc.cu"]
 CXX_SOURCES = ["plan.cpp"]
 HEADERS = ["gbpf_device.h", "plan.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

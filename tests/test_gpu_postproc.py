@@ -1,0 +1,57 @@
+"""Either side of the path on the GPU: the time-series injection matrix against the
+reference's own output (bit for bit), and branch flows / loading of solved N-1 cases against
+the restated compute_branch_loading (zeros and NaNs exactly; values to 1e-11 relative / 1e-10
+absolute: a branch's end power is the small difference of terms ~|y| larger, so rounding of
+the host's complex products -- which may fuse multiply-adds -- shows at ~1e-12)."""
+
+import numpy as np
+import pytest
+
+from oracle.postproc import branch_loading
+from p3s_gb300 import contingency
+from p3s_gb300.flows import compute_branch_loading
+from p3s_gb300.synthetic import grid_118
+from p3s_gb300.timeseries import build_sbus_matrix
+from test_postproc_cpu import golden_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def test_device_sbus_matches_the_reference_bit_for_bit():
+    d, elements, ts = golden_inputs()
+    S = build_sbus_matrix(d["s0"], elements, ts, float(d["sn_mva"]))
+    assert np.array_equal(S, d["Sbus"])
+
+
+def test_branch_loading_of_an_n1_sweep_matches_the_restated_reference():
+    g = grid_118()
+    res = contingency.solve_contingencies(g, reslack_islands=True)
+    assert (~res.served).any() and res.converged.all()
+    rng = np.random.default_rng(4)
+    nbr = g.n_branch
+    vn = rng.choice([110.0, 220.0], nbr)
+    kind = (rng.random(nbr) < 0.2).astype(np.uint8)
+    rating = np.where(kind == 0, rng.uniform(0.2, 1.0, nbr), rng.uniform(50, 300, nbr))
+    conv = res.converged.copy()
+    conv[5] = False  # a non-converged column is reported NaN
+    res.converged = conv
+    tab = compute_branch_loading(g, res, vn, rating, kind, sn_mva=100.0)
+    outaged = np.zeros((nbr, len(res.groups)), bool)
+    for c, grp in enumerate(res.groups):
+        outaged[grp, c] = True
+    assert np.array_equal(tab.outaged, outaged)
+    ref = branch_loading(g.n, g.f, g.t, g.stamp, res.V, conv, vn, vn, rating, kind, 100.0, outaged)
+    got = (tab.p_from_mw + 1j * tab.q_from_mvar, tab.p_to_mw + 1j * tab.q_to_mvar, tab.i_from_ka, tab.i_to_ka,
+           tab.i_ka, tab.loading_percent)
+    for a, b in zip(got, ref):
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        assert np.array_equal(a[outaged & conv[None, :]], b[outaged & conv[None, :]])  # zeros
+        m = ~np.isnan(b)
+        assert np.allclose(a[m], b[m], rtol=1e-11, atol=1e-10)
+    assert np.isnan(tab.loading_percent[:, 5]).all()
+    # a branch touching an unserved bus has undefined flow
+    c = int(np.nonzero((~res.served).any(axis=0))[0][0])
+    dead = np.nonzero(~res.served[:, c])[0]
+    touch = np.isin(g.f, dead) | np.isin(g.t, dead)
+    touch &= ~outaged[:, c]
+    assert np.isnan(tab.i_ka[touch, c]).all()
