@@ -139,6 +139,13 @@ int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double*
  * Backs debug_J (nr_klu.cpp:1283-1304, 1332-1342). */
 int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const uint8_t* pin, double* blocks,
                        double* residual);
+/* DC start voltage (p3s/timeseries.py:200-247 dc_initial_voltage, NewtonPowerflowCpp.py:422-440
+ * _pre_dc_solve): angles from B[pvpq, pvpq] theta = Pinj[pvpq] - B[pvpq, ref] theta_ref with
+ * B the branch susceptance Laplacian (-Im Ybus off the diagonal, the diagonal their negated
+ * row sum), factored and solved on the device by the solver's block LU; every non-slack
+ * bus keeps its magnitude from V0 (n complex) with the DC angle, slack buses keep V0. Returns 0,
+ * or 1 when the DC system is singular or gives non-finite angles (Vout = V0, the flat start). */
+int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* Vout);
 /* Block row of each bus (-1 for slack), length n. */
 int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
 

@@ -60,3 +60,24 @@ def branch_loading(n, f, t, y, V, converged, vn_from, vn_to, rating, kind, sn_mv
     for arr in (S_from, S_to, i_from, i_to, i_max, loading):
         arr[:, bad] = np.nan
     return S_from, S_to, i_from, i_to, i_max, loading
+
+
+def dc_initial_voltage(Yp, Yj, Yx, pv, pq, ref, Pinj, V0):
+    """``dc_initial_voltage`` / ``_pre_dc_solve`` (p3s/timeseries.py:200-247,
+    NewtonPowerflowCpp.py:422-440): B[pvpq, pvpq] theta = Pinj[pvpq] - B[pvpq, ref] theta_ref
+    with B the branch susceptance Laplacian (-Im Ybus off the diagonal, the diagonal their
+    negated row sum), scipy spsolve; magnitudes kept from V0."""
+    import scipy.sparse.linalg as spl
+
+    n = len(Yp) - 1
+    Y = sp.csr_matrix((np.asarray(Yx), Yj, Yp), shape=(n, n)).tocoo()
+    off = Y.row != Y.col
+    B = sp.coo_matrix((-Y.data.imag[off], (Y.row[off], Y.col[off])), shape=(n, n)).tocsr()
+    B = (B - sp.diags(np.asarray(B.sum(axis=1)).ravel())).tocsr()
+    pvpq = np.r_[pv, pq]
+    theta_ref = np.angle(V0[ref])
+    rhs = Pinj[pvpq] - B[pvpq, :][:, ref] @ theta_ref
+    th = np.real(spl.spsolve(B[pvpq, :][:, pvpq].tocsc(), rhs))
+    V = np.asarray(V0, dtype=np.complex128).copy()
+    V[pvpq] = np.abs(V0[pvpq]) * np.exp(1j * th)
+    return V

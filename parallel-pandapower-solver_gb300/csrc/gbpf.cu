@@ -1007,6 +1007,56 @@ int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double*
     return 0;
 }
 
+int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* Vout) {
+    if (!s || !Pinj || !V0 || !Vout) return fail("dc_start: null argument");
+    const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv);
+    Shape* sh = nullptr;
+    if (int rc = get_shape(s, 1024, 1, &sh)) return rc;
+    std::vector<double> th(n);
+    for (size_t i = 0; i < n; ++i) th[i] = std::atan2(V0[2 * i + 1], V0[2 * i]);
+    DBuf dP, dth, dfac, dR, dy, dout, dpiv;
+    auto cleanup = [&]() {
+        for (DBuf* b : {&dP, &dth, &dfac, &dR, &dy, &dout, &dpiv}) b->release();
+    };
+    struct Guard {
+        std::function<void()> f;
+        ~Guard() { f(); }
+    } guard{cleanup};
+    CK(dP.ensure(n * 8));
+    CK(dth.ensure(n * 8));
+    CK(dfac.ensure(nb * 32));
+    CK(dR.ensure(nv * 16));
+    CK(dy.ensure(nv * 16));
+    CK(dout.ensure(n * 8));
+    CK(dpiv.ensure(16));
+    CK(cudaMemcpyAsync(dP.p, Pinj, n * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dth.p, th.data(), n * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(gbpf::launch_dc(sh->dp, dP.as<double>(), dth.as<double>(), dfac.as<double4_32a>(), dR.as<double2>(),
+                       dy.as<double2>(), dout.as<double>(), dpiv.as<unsigned long long>(), s->stream));
+    unsigned long long piv[2];
+    CK(cudaMemcpyAsync(th.data(), dout.p, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(piv, dpiv.p, 16, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    // a zero or non-finite pivot (a DC island without a reference) or non-finite angles:
+    // the reference keeps the flat start then (timeseries.py:244-247)
+    double mn, mx;
+    std::memcpy(&mn, &piv[0], 8);
+    std::memcpy(&mx, &piv[1], 8);
+    bool ok = std::isfinite(mx) && mn > 0.0;
+    for (size_t i = 0; i < n && ok; ++i) ok = std::isfinite(th[i]);
+    for (size_t i = 0; i < n; ++i) {
+        const double vm = std::hypot(V0[2 * i], V0[2 * i + 1]);
+        if (!ok || s->plan.row_of_bus[i] < 0) {
+            Vout[2 * i] = V0[2 * i];
+            Vout[2 * i + 1] = V0[2 * i + 1];
+        } else {
+            Vout[2 * i] = vm * std::cos(th[i]);
+            Vout[2 * i + 1] = vm * std::sin(th[i]);
+        }
+    }
+    return ok ? 0 : 1;
+}
+
 int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const uint8_t* pin, double* blocks,
                        double* residual) {
     if (!s) return fail("null solver");

@@ -1031,6 +1031,60 @@ cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* ta
     return cudaGetLastError();
 }
 
+// DC start (NewtonPowerflowCpp.py:422-440 _pre_dc_solve): B[pvpq, pvpq] theta = Pinj[pvpq] -
+// B[pvpq, ref] theta_ref with B the branch susceptance Laplacian (B_ij = -Im Y_ij off the
+// diagonal, B_ii = -sum of the row's off-diagonal B_ij: no shunts, no tap asymmetry -- the DC
+// model), factored and solved by the Newton kernel's block LU (one case: every 2x2 block
+// carries B in its angle / P entry and the identity in its magnitude / Q entry). One CTA of
+// NTB threads; the plan's schedule has NTB workers.
+template <int NTB>
+__global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const double* Pinj, const double* theta_bus,
+                                                    double4_32a* fac, double2* R, double2* y, double* theta,
+                                                    unsigned long long* piv) {
+    __shared__ int s_on[1];
+    __shared__ unsigned long long s_min[1], s_max[1];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_on[0] = 1;
+        s_min[0] = ~0ULL;
+        s_max[0] = 0ULL;
+    }
+    for (int i = tid; i < P.n; i += NTB) {
+        const int row = P.row_of_bus[i];
+        if (row < 0) continue;
+        double rhs = Pinj[i], diag = 0.0;
+        for (int k = P.Yp[i]; k < P.Yp[i + 1]; ++k) {
+            const int j = P.Yj[k];
+            if (j == i) continue;
+            const double b = -P.Y[k].y;
+            diag -= b;
+            const int q = P.posmap[k];
+            if (q >= 0)
+                fac[q] = make_double4_32a(b, 0.0, 0.0, 0.0);
+            else if (P.row_of_bus[j] < 0)
+                rhs -= b * theta_bus[j];  // coupling to a reference bus at its angle
+        }
+        fac[P.dpos[row]] = make_double4_32a(diag, 0.0, 0.0, 1.0);
+        R[row] = make_double2(rhs, 0.0);
+    }
+    __syncthreads();
+    lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max);
+    for (int i = tid; i < P.n; i += NTB) {
+        const int row = P.row_of_bus[i];
+        theta[i] = row < 0 ? theta_bus[i] : y[row].x;
+    }
+    if (tid == 0) {
+        piv[0] = s_min[0];
+        piv[1] = s_max[0];
+    }
+}
+
+cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_bus, double4_32a* fac, double2* R,
+                      double2* y, double* theta, unsigned long long* piv, cudaStream_t stream) {
+    dc_kernel<1024><<<1, 1024, 0, stream>>>(P, Pinj, theta_bus, fac, R, y, theta, piv);
+    return cudaGetLastError();
+}
+
 // Jacobian blocks and residual at one given voltage (G = 1): debug_J and tests.
 __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const double2* Sbus, const uint8_t* pin,
                                   double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,

@@ -216,6 +216,19 @@ class GpuSolver:
         _lib.check(rc, "solve_batch_contingency")
         return {"V": V, "iterations": it, "converged": cv.astype(bool)}
 
+    def dc_start(self, Pinj, V0):
+        """DC start voltage (``dc_initial_voltage``): DC angles at every non-slack bus with V0's
+        magnitudes; V0 itself when the DC system is singular. Returns (V, used_dc)."""
+        P = np.ascontiguousarray(np.asarray(Pinj, dtype=np.float64).ravel())
+        V0 = c128(np.asarray(V0).ravel())
+        if P.shape != (self.n,) or V0.shape != (self.n,):
+            raise ValueError("dc_start: Pinj and V0 must be (n_bus,)")
+        out = np.empty(self.n, dtype=np.complex128)
+        rc = _lib.load().gbpf_dc_start(self._h, _lib.d(P), _lib.cview(V0), _lib.cview(out))
+        if rc < 0:
+            raise RuntimeError(_lib.last_error())
+        return out, rc == 0
+
     # -------------------------------------------------------------- Jacobian
     def eval_blocks(self, S, V, pin=None):
         """Device Jacobian blocks (n_blocks, 4) and residual (n_var_bus, 2) at one voltage."""

@@ -55,3 +55,21 @@ def test_branch_loading_of_an_n1_sweep_matches_the_restated_reference():
     touch = np.isin(g.f, dead) | np.isin(g.t, dead)
     touch &= ~outaged[:, c]
     assert np.isnan(tab.i_ka[touch, c]).all()
+
+
+def test_dc_start_matches_the_restated_reference_and_starts_newton():
+    from oracle import cpu
+    from oracle.postproc import dc_initial_voltage
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.synthetic import grid_2000
+
+    for g in (grid_118(), grid_2000()):
+        s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+        V, used = s.dc_start(g.Sbus.real, g.V0)
+        assert used
+        ref = dc_initial_voltage(g.Yp, g.Yj, g.Yx, g.pv, g.pq, g.ref, g.Sbus.real, g.V0)
+        assert np.abs(np.angle(V) - np.angle(ref)).max() < 1e-10
+        assert np.array_equal(np.abs(V)[g.ref], np.abs(g.V0)[g.ref])
+        r = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(g.Sbus[:, None], V)
+        flat = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(g.Sbus[:, None], g.V0)
+        assert r["converged"][0] and r["iterations"][0] <= flat["iterations"][0]
