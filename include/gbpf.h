@@ -97,6 +97,8 @@ int gbpf_get_stats(gbpf_solver* s, gbpf_stats* out);
 int gbpf_get_shape(gbpf_solver* s, long long units, int* threads_per_cta, int* cases_per_cta);
 int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cases_per_cta);
 
+/* The solver's current Ybus values (nnz complex), e.g. after gbpf_update_Y_from_branches. */
+int gbpf_get_Y(gbpf_solver* s, double* Yx);
 /* Ybus nnz -> Jacobian block position (-1 for slack rows/columns), length nnz. */
 int gbpf_get_posmap(gbpf_solver* s, int32_t* out);
 
@@ -223,6 +225,25 @@ int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t
  * is_slack (n), gen_prio (n, re-slack ranking; NULL = none). */
 int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const int32_t* stamp_pos,
                       const double* stamp_val, const uint8_t* is_slack, const double* gen_prio);
+
+/* Branch stamps of the general two-port (p3s/models/TwoWindingTransformerModel.py:172-175; a
+ * line is a = b = 1 with half its shunt admittance at each end, TransmissionLineModel.py:45-48):
+ * Yff = (ys + y_from) / |a|^2, Yft = -ys / (conj a conj b), Ytf = -ys / (a b),
+ * Ytt = (ys + y_to) / |b|^2 per branch (complex inputs of length m); out of service -> 0; an
+ * open end Kron-eliminated (TwoPort.py:69-105). stamps: (m, 4) complex out. in_service /
+ * open_from / open_to may be NULL (all in service, none open). */
+int gbpf_branch_stamps(int m, const double* ys, const double* y_from, const double* y_to, const double* a,
+                       const double* b, const uint8_t* in_service, const uint8_t* open_from, const uint8_t* open_to,
+                       double* stamps);
+int gbpf_branch_stamps_device(int m, const double* ys, const double* y_from, const double* y_to, const double* a,
+                              const double* b, const uint8_t* in_service, const uint8_t* open_from,
+                              const uint8_t* open_to, double* stamps, void* stream);
+/* Ybus values of the solver's topology from branch stamps (m x 4 complex, at the positions set
+ * by gbpf_set_branches) and bus shunts (n complex, or NULL), summed on the device
+ * (TwoPort.py:133-149 create_y_matrix): the resident Ybus and the branch table take the new
+ * values, like gbpf_update_Y (e.g. after tap changes). Replaces update_Y after a host rebuild
+ * of the Ybus (NewtonPowerflowCuda.py:137-165). */
+int gbpf_update_Y_from_branches(gbpf_solver* s, const double* stamps, const double* bus_shunt);
 
 /* gbpf_islands for the topology of `s` (n = its bus count) on the solver's stream, with
  * device buffers the solver keeps and grows (no allocation once they are large enough):

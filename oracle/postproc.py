@@ -81,3 +81,34 @@ def dc_initial_voltage(Yp, Yj, Yx, pv, pq, ref, Pinj, V0):
     V = np.asarray(V0, dtype=np.complex128).copy()
     V[pvpq] = np.abs(V0[pvpq]) * np.exp(1j * th)
     return V
+
+
+def branch_stamps(ys, y_from, y_to, a, b, in_service, open_from, open_to):
+    """The general two-port's stamps (p3s/models/TwoWindingTransformerModel.py:172-175), the
+    out-of-service mask (TwoPort.py:51-66) and the open-end Kron elimination
+    (TwoPort.py:69-105), in numpy."""
+    ff = (ys + y_from) / np.abs(a) ** 2
+    ft = -ys / (np.conj(a) * np.conj(b))
+    tf = -ys / (a * b)
+    tt = (ys + y_to) / np.abs(b) ** 2
+    ins = np.asarray(in_service, dtype=bool)
+    ff, ft, tf, tt = (np.where(ins, v, 0.0) for v in (ff, ft, tf, tt))
+    of, ot = np.asarray(open_from, dtype=bool), np.asarray(open_to, dtype=bool)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ff_red = np.where(tt != 0, ff - ft * tf / tt, ff)
+        tt_red = np.where(ff != 0, tt - tf * ft / ff, tt)
+    ff_new = np.where(of, 0.0, np.where(ot, ff_red, ff))
+    tt_new = np.where(ot, 0.0, np.where(of, tt_red, tt))
+    either = of | ot
+    return np.stack([ff_new, np.where(either, 0.0, ft), np.where(either, 0.0, tf), tt_new], axis=1)
+
+
+def ybus_from_stamps(n, f, t, stamps, bus_shunt):
+    """COO sum of the stamps and shunts (TwoPort.py:133-149 create_y_matrix) as CSR."""
+    rows = np.concatenate([f, f, t, t, np.arange(n)])
+    cols = np.concatenate([f, t, f, t, np.arange(n)])
+    data = np.concatenate([stamps[:, 0], stamps[:, 1], stamps[:, 2], stamps[:, 3], bus_shunt])
+    Y = sp.coo_matrix((data, (rows, cols)), shape=(n, n)).tocsr()
+    Y.sum_duplicates()
+    Y.sort_indices()
+    return Y

@@ -138,13 +138,16 @@ struct gbpf_solver {
     // branch table for outage cases (gbpf_set_branches)
     int m = 0;
     DBuf dbr_f, dbr_t, dbr_live, dbr_pos, dbr_val, dslack, dprio;
+    std::vector<int> br_pos;          // host copy of the stamp positions (m x 4)
+    DBuf dg_ptr, dg_src, dshunt;      // Ybus gather lists (gbpf_update_Y_from_branches)
+    bool gather_ready = false;
     gbpf_stats last{};
     ~gbpf_solver() {
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
                         &btab, &bjobs, &iin, &iscr, &ibest, &iout, &dbr_f, &dbr_t, &dbr_live, &dbr_pos, &dbr_val,
-                        &dslack, &dprio})
+                        &dslack, &dprio, &dg_ptr, &dg_src, &dshunt})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
             if (e) cudaEventDestroy(e);
@@ -822,6 +825,12 @@ int gbpf_get_stats(gbpf_solver* s, gbpf_stats* o) {
     return 0;
 }
 
+int gbpf_get_Y(gbpf_solver* s, double* Yx) {
+    if (!s || !Yx) return fail("null argument");
+    std::copy(s->Yx.begin(), s->Yx.end(), Yx);
+    return 0;
+}
+
 int gbpf_get_posmap(gbpf_solver* s, int32_t* out) {
     if (!s || !out) return fail("null argument");
     std::copy(s->plan.posmap.begin(), s->plan.posmap.end(), out);
@@ -1153,6 +1162,8 @@ int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t,
     CK(upload(s->dslack, vs));
     CK(upload(s->dprio, vprio));
     s->m = m;
+    s->br_pos = vp;
+    s->gather_ready = false;
     auto fill = [&](gbpf::DevPlan& d) {
         d.m = m;
         d.br_pos = s->dbr_pos.as<int4>();
@@ -1162,6 +1173,45 @@ int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t,
     fill(s->dp);
     for (auto& sh : s->shapes) fill(sh->dp);
     return 0;
+}
+
+int gbpf_update_Y_from_branches(gbpf_solver* s, const double* stamps, const double* bus_shunt) {
+    if (!s || !stamps) return fail("update_Y_from_branches: null argument");
+    if (!s->m) return fail("update_Y_from_branches: the branch table is not set (gbpf_set_branches)");
+    const int m = s->m, n = s->n, nnz = s->nnz;
+    if (!s->gather_ready) {
+        // contributions of every CSR entry in the order a COO sum of the stamps meets them
+        // (all Yff, then Yft, Ytf, Ytt, each in branch order; TwoPort.py:133-149), the bus
+        // shunt last
+        std::vector<std::vector<int>> lists(nnz);
+        for (int q = 0; q < 4; ++q)
+            for (int e = 0; e < m; ++e) lists[s->br_pos[4 * (size_t)e + q]].push_back(4 * e + q);
+        for (int i = 0; i < n; ++i)
+            if (s->plan.ydiag[i] >= 0) lists[s->plan.ydiag[i]].push_back(4 * m + i);
+        std::vector<int> ptr(nnz + 1, 0), src;
+        for (int k = 0; k < nnz; ++k) {
+            ptr[k + 1] = ptr[k] + (int)lists[k].size();
+            src.insert(src.end(), lists[k].begin(), lists[k].end());
+        }
+        CK(upload(s->dg_ptr, ptr));
+        CK(upload(s->dg_src, src));
+        s->gather_ready = true;
+    }
+    std::vector<double> sh(2 * (size_t)n, 0.0);
+    if (bus_shunt) sh.assign(bus_shunt, bus_shunt + 2 * (size_t)n);
+    CK(upload(s->dshunt, sh));
+    CK(cudaMemcpyAsync(s->dbr_val.p, stamps, 64 * (size_t)m, cudaMemcpyHostToDevice, s->stream));
+    CK(gbpf::launch_ybus_gather(nnz, 4 * m, s->dg_ptr.as<int>(), s->dg_src.as<int>(), s->dbr_val.as<double2>(),
+                                s->dshunt.as<double2>(), s->dY.as<double2>(), s->dY32.as<float2>(), s->stream));
+    CK(cudaMemcpyAsync(s->Yx.data(), s->dY.p, 16 * (size_t)nnz, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    // branches whose transfer terms vanished (out of service, an open end) no longer couple
+    std::vector<uint8_t> live(m);
+    for (int e = 0; e < m; ++e)
+        live[e] = (stamps[8 * (size_t)e + 2] != 0.0 || stamps[8 * (size_t)e + 3] != 0.0 ||
+                   stamps[8 * (size_t)e + 4] != 0.0 || stamps[8 * (size_t)e + 5] != 0.0);
+    CK(upload(s->dbr_live, live));
+    return compute_rcond0(s);
 }
 
 int gbpf_solver_islands(gbpf_solver* s, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,

@@ -150,6 +150,9 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
                               double2* R, cudaStream_t stream);
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d);
+// Ybus values from stamps (postproc.cu)
+cudaError_t launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,
+                               const double2* shunt, double2* Y, float2* Y32, cudaStream_t stream);
 // islanding kernel (islands.cu): scratch 4 n ints and n u64 per CTA of `grid`
 cudaError_t launch_islands(int n, int m, const int* f, const int* t, const uint8_t* live, int L, const int* out_ptr,
                            const int* out_idx, const uint8_t* is_slack, const double* prio, int reslack, int* scratch,

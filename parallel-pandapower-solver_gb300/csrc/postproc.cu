@@ -115,6 +115,76 @@ __global__ void __launch_bounds__(TB) flow_kernel(int nbr, int L, const int* __r
     }
 }
 
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {  // a / b, as (a conj(b)) / |b|^2
+    const double d = __dadd_rn(__dmul_rn(b.x, b.x), __dmul_rn(b.y, b.y));
+    const double2 num = cmul(a, make_double2(b.x, -b.y));
+    return make_double2(__ddiv_rn(num.x, d), __ddiv_rn(num.y, d));
+}
+
+// Branch stamps (Yff, Yft, Ytf, Ytt) of the general two-port of p3s/models/TwoWindingTransformer
+// Model.py:172-175 (a line is a = b = 1, y_from = y_to = half its shunt admittance,
+// TransmissionLineModel.py:45-48): Yff = (ys + y_from) / |a|^2, Yft = -ys / (conj a conj b),
+// Ytf = -ys / (a b), Ytt = (ys + y_to) / |b|^2; out of service -> 0; an open end Kron-eliminated
+// (TwoPort.py:69-105): Yff' = Yff - Yft Ytf / Ytt with the to end open (the from end analogous),
+// transfer terms 0, both ends open -> 0.
+__global__ void __launch_bounds__(TB) stamp_kernel(int m, const double2* __restrict__ ys, const double2* __restrict__ yf,
+                                                   const double2* __restrict__ yt, const double2* __restrict__ a,
+                                                   const double2* __restrict__ b, const uint8_t* __restrict__ in_service,
+                                                   const uint8_t* __restrict__ open_f, const uint8_t* __restrict__ open_t,
+                                                   double2* __restrict__ out) {
+    const int e = blockIdx.x * TB + threadIdx.x;
+    if (e >= m) return;
+    const double2 z = make_double2(0.0, 0.0);
+    if (in_service && !in_service[e]) {
+        out[4 * e] = out[4 * e + 1] = out[4 * e + 2] = out[4 * e + 3] = z;
+        return;
+    }
+    const double2 s = ys[e], A = a[e], B = b[e];
+    const double a2 = __dadd_rn(__dmul_rn(A.x, A.x), __dmul_rn(A.y, A.y));
+    const double b2 = __dadd_rn(__dmul_rn(B.x, B.x), __dmul_rn(B.y, B.y));
+    const double2 sf = cadd(s, yf[e]), st = cadd(s, yt[e]);
+    double2 ff = make_double2(__ddiv_rn(sf.x, a2), __ddiv_rn(sf.y, a2));
+    double2 tt = make_double2(__ddiv_rn(st.x, b2), __ddiv_rn(st.y, b2));
+    const double2 ms = make_double2(-s.x, -s.y);
+    double2 ft = cdiv(ms, cmul(make_double2(A.x, -A.y), make_double2(B.x, -B.y)));
+    double2 tf = cdiv(ms, cmul(A, B));
+    const bool of = open_f && open_f[e], ot = open_t && open_t[e];
+    if (of || ot) {
+        const bool tt0 = tt.x == 0.0 && tt.y == 0.0, ff0 = ff.x == 0.0 && ff.y == 0.0;
+        const double2 ff_red = tt0 ? ff : make_double2(__dsub_rn(ff.x, cdiv(cmul(ft, tf), tt).x),
+                                                       __dsub_rn(ff.y, cdiv(cmul(ft, tf), tt).y));
+        const double2 tt_red = ff0 ? tt : make_double2(__dsub_rn(tt.x, cdiv(cmul(tf, ft), ff).x),
+                                                       __dsub_rn(tt.y, cdiv(cmul(tf, ft), ff).y));
+        const double2 nff = of ? z : (ot ? ff_red : ff);
+        const double2 ntt = ot ? z : (of ? tt_red : tt);
+        ff = nff;
+        tt = ntt;
+        ft = tf = z;
+    }
+    out[4 * e] = ff;
+    out[4 * e + 1] = ft;
+    out[4 * e + 2] = tf;
+    out[4 * e + 3] = tt;
+}
+
+// Ybus values from branch stamps (TwoPort.py:133-149 create_y_matrix, then the bus shunts):
+// Yx[k] = sum over the contributions of CSR entry k in order; a contribution below 4 m is
+// stamp entry src of the branch table, 4 m + i the shunt of bus i.
+__global__ void __launch_bounds__(TB) gather_kernel(int nnz, int m4, const int* __restrict__ ptr,
+                                                    const int* __restrict__ src, const double2* __restrict__ stamps,
+                                                    const double2* __restrict__ shunt, double2* __restrict__ Y,
+                                                    float2* __restrict__ Y32) {
+    const int k = blockIdx.x * TB + threadIdx.x;
+    if (k >= nnz) return;
+    double2 v = make_double2(0.0, 0.0);
+    for (int q = ptr[k]; q < ptr[k + 1]; ++q) {
+        const int s = src[q];
+        v = cadd(v, s < m4 ? stamps[s] : shunt[s - m4]);
+    }
+    Y[k] = v;
+    if (Y32) Y32[k] = make_float2((float)v.x, (float)v.y);
+}
+
 template <typename T>
 struct DevVec {
     T* p = nullptr;
@@ -131,6 +201,12 @@ struct DevVec {
     } while (0)
 
 }  // namespace
+
+cudaError_t gbpf::launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,
+                                     const double2* shunt, double2* Y, float2* Y32, cudaStream_t stream) {
+    gather_kernel<<<(nnz + TB - 1) / TB, TB, 0, stream>>>(nnz, m4, ptr, src, stamps, shunt, Y, Y32);
+    return cudaGetLastError();
+}
 
 extern "C" {
 
@@ -181,6 +257,44 @@ int gbpf_build_sbus(int n, int T, int R, const double* s0, const int64_t* ptr, c
         return rc;
     PK(cudaDeviceSynchronize());
     PK(cudaMemcpy(out, dout.p, 16 * (size_t)n * T, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int gbpf_branch_stamps_device(int m, const double* ys, const double* y_from, const double* y_to, const double* a,
+                              const double* b, const uint8_t* in_service, const uint8_t* open_from,
+                              const uint8_t* open_to, double* stamps, void* stream) {
+    if (m <= 0) return pfail("branch_stamps: m must be > 0");
+    stamp_kernel<<<(m + TB - 1) / TB, TB, 0, static_cast<cudaStream_t>(stream)>>>(
+        m, reinterpret_cast<const double2*>(ys), reinterpret_cast<const double2*>(y_from),
+        reinterpret_cast<const double2*>(y_to), reinterpret_cast<const double2*>(a),
+        reinterpret_cast<const double2*>(b), in_service, open_from, open_to, reinterpret_cast<double2*>(stamps));
+    PK(cudaGetLastError());
+    return 0;
+}
+
+int gbpf_branch_stamps(int m, const double* ys, const double* y_from, const double* y_to, const double* a,
+                       const double* b, const uint8_t* in_service, const uint8_t* open_from, const uint8_t* open_to,
+                       double* stamps) {
+    if (m <= 0) return pfail("branch_stamps: m must be > 0");
+    DevVec<double> d[6];
+    DevVec<uint8_t> u[3];
+    const double* hin[5] = {ys, y_from, y_to, a, b};
+    for (int i = 0; i < 5; ++i) {
+        PK(d[i].alloc(2 * (size_t)m));
+        PK(cudaMemcpy(d[i].p, hin[i], 16 * (size_t)m, cudaMemcpyHostToDevice));
+    }
+    PK(d[5].alloc(8 * (size_t)m));
+    const uint8_t* uin[3] = {in_service, open_from, open_to};
+    for (int i = 0; i < 3; ++i)
+        if (uin[i]) {
+            PK(u[i].alloc(m));
+            PK(cudaMemcpy(u[i].p, uin[i], (size_t)m, cudaMemcpyHostToDevice));
+        }
+    if (int rc = gbpf_branch_stamps_device(m, d[0].p, d[1].p, d[2].p, d[3].p, d[4].p, u[0].p, u[1].p, u[2].p, d[5].p,
+                                           nullptr))
+        return rc;
+    PK(cudaDeviceSynchronize());
+    PK(cudaMemcpy(stamps, d[5].p, 64 * (size_t)m, cudaMemcpyDeviceToHost));
     return 0;
 }
 

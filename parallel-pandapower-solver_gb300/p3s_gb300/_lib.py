@@ -108,6 +108,7 @@ SIGNATURES = {
     "gbpf_get_info": (C.c_int, [_vp, C.POINTER(Info)]),
     "gbpf_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gbpf_get_posmap": (C.c_int, [_vp, _ip]),
+    "gbpf_get_Y": (C.c_int, [_vp, _dp]),
     "gbpf_get_shape": (C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gbpf_set_shape": (C.c_int, [_vp, C.c_longlong, C.c_int, C.c_int]),
     "gbpf_get_row_of_bus": (C.c_int, [_vp, _ip]),
@@ -139,6 +140,9 @@ SIGNATURES = {
                                     _bp, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gbpf_branch_flows_device": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                            _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbpf_branch_stamps": (C.c_int, [C.c_int, _dp, _dp, _dp, _dp, _dp, _bp, _bp, _bp, _dp]),
+    "gbpf_branch_stamps_device": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbpf_update_Y_from_branches": (C.c_int, [_vp, _dp, _dp]),
     "gbpf_set_branches": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, _bp, _dp]),
     "gbpf_solver_islands": (C.c_int, [_vp, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                       _ip, _ip]),

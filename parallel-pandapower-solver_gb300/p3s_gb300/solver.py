@@ -143,6 +143,21 @@ class GpuSolver:
         _lib.check(rc, "set_branches")
         self.branches = m
 
+    def update_Y_from_branches(self, stamps, bus_shunt=None):
+        """Ybus values summed on the device from branch stamps (m, 4) at the branch table's
+        positions and bus shunts (n,) -- e.g. after tap changes (see ``ybus.branch_stamps``)."""
+        st = c128(stamps)
+        if st.shape != (getattr(self, "branches", -1), 4):
+            raise ValueError("update_Y_from_branches: stamps must be (m, 4) for the branch table set")
+        sh = None if bus_shunt is None else c128(np.asarray(bus_shunt).ravel())
+        if sh is not None and sh.shape != (self.n,):
+            raise ValueError("update_Y_from_branches: bus_shunt must be (n_bus,)")
+        rc = _lib.load().gbpf_update_Y_from_branches(self._h, _lib.cview(st), None if sh is None else _lib.cview(sh))
+        _lib.check(rc, "update_Y_from_branches")
+        Yx = np.empty(self.nnz, dtype=np.complex128)
+        _lib.check(_lib.load().gbpf_get_Y(self._h, _lib.cview(Yx)), "gbpf_get_Y")
+        self.Yx = Yx
+
     # -------------------------------------------------------------- values
     def update_Y(self, Yx):
         Yx = c128(Yx)

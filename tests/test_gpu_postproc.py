@@ -73,3 +73,51 @@ def test_dc_start_matches_the_restated_reference_and_starts_newton():
         r = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(g.Sbus[:, None], V)
         flat = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(g.Sbus[:, None], g.V0)
         assert r["converged"][0] and r["iterations"][0] <= flat["iterations"][0]
+
+
+def test_ybus_from_branch_stamps_on_the_device():
+    """Two-port stamps (taps, phase shifts, out of service, open ends) and their Ybus summed on
+    the device against the restated reference models (1e-13 of the largest stamp: the Kron
+    elimination of an open end subtracts nearly equal terms, and the host divides complex
+    numbers by a different formula); a power flow on the device-built Ybus equals one on the
+    same Ybus handed to update_Y (bit for bit)."""
+    import scipy.sparse as sp
+
+    from oracle.postproc import branch_stamps as ref_stamps
+    from oracle.postproc import ybus_from_stamps
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.ybus import branch_stamps
+
+    g = grid_118()
+    m = g.n_branch
+    rng = np.random.default_rng(8)
+    x = 0.02 + 0.3 * rng.random(m)
+    ys = 1.0 / (x * rng.uniform(0.1, 0.4, m) + 1j * x)
+    ysh = 0.5j * rng.uniform(0.0, 0.05, m)
+    tap = np.where(rng.random(m) < 0.1, rng.uniform(0.9, 1.1, m), 1.0)
+    shift = np.where(rng.random(m) < 0.05, np.deg2rad(rng.uniform(-10, 10, m)), 0.0)
+    a = tap * np.exp(1j * shift)
+    ins = rng.random(m) > 0.03
+    of = rng.random(m) < 0.03
+    ot = rng.random(m) < 0.03
+    st = branch_stamps(ys, ysh, ysh, a, 1.0, ins, of, ot)
+    ref = ref_stamps(ys, ysh, ysh, a, np.ones(m), ins, of, ot)
+    assert np.abs(st - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.array_equal(st == 0, ref == 0)
+    shunt = np.zeros(g.n, complex)
+    shunt[g.pq[:5]] = 0.02j
+    Yref = ybus_from_stamps(g.n, g.f, g.t, ref, shunt)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    is_slack = np.zeros(g.n, np.uint8)
+    is_slack[g.ref] = 1
+    s.set_branches(g.f, g.t, g.stamp_pos, g.stamp, is_slack)
+    s.update_Y_from_branches(st, shunt)
+    # the device Ybus on the grid's pattern: entries outside Yref's pattern are zero
+    Ydev = sp.csr_matrix((s.Yx, g.Yj, g.Yp), shape=(g.n, g.n))
+    assert abs(Ydev - Yref).max() <= 1e-13 * abs(Yref).max()
+    host = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    host.update_Y(s.Yx)
+    p = GpuSolver.params()
+    S = g.Sbus[:, None] * np.ones((1, 4))
+    r1, r2 = s.solve_batch(S, g.V0, p), host.solve_batch(S, g.V0, p)
+    assert np.array_equal(r1["V"], r2["V"]) and np.array_equal(r1["iterations"], r2["iterations"])
