@@ -124,6 +124,18 @@ int gbpf_solve_lanes_device(gbpf_solver* s, int T, const double* dS, const doubl
                             const int64_t* d_offsets, const gbpf_params* p, double* dV, int32_t* d_iterations,
                             uint8_t* d_converged);
 
+/* gbpf_solve_lanes enqueued in `slot` (0..7) and returned at once: copies in, the launch and
+ * copies out run on the slot's own stream with the slot's own scratch, so calls in different
+ * slots overlap (one call's copies with another's kernel). S / V0 / offsets / V / iterations
+ * / converged must stay valid until gbpf_solve_wait(slot), which waits, reports device errors
+ * and sets the stats of that call. Page-locked host arrays (gbpf_host_alloc) let the copies
+ * overlap; with pageable ones the call itself waits for them. No reference counterpart (the
+ * reference's calls are synchronous). */
+int gbpf_solve_lanes_async(gbpf_solver* s, int slot, int T, const double* S, const double* V0, int K,
+                           const int64_t* offsets, const gbpf_params* p, double* V, int32_t* iterations,
+                           uint8_t* converged);
+int gbpf_solve_wait(gbpf_solver* s, int slot);
+
 /* N-1 batch: per-case Ybus values on the shared pattern, per-case pin mask.
  * S: (n,) complex; V0: (n, L) complex; pin: (n, L) uint8 (NULL = none).
  * Per-case Ybus either dense Yd (nnz, L) complex (replaces

@@ -115,6 +115,26 @@ struct Shape {
 
 constexpr int N_SIZE_CLASSES = 48;  // batch sizes by ceil(log2(work items))
 
+// Resources of one launch in flight: stream, events, scratch and buffers. The solver's own
+// (synchronous calls) and every asynchronous slot have their own, so calls in different slots
+// overlap (one's copies with another's kernel) without sharing anything they write.
+struct ExecSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
+    DBuf scr, bctl, btab, bjobs, bS, bV0, bV, bit, bcv, blane;
+    unsigned long long* host_ctl = nullptr;  // page-locked copy of the control block
+    bool pending = false;
+    int grid = 0, G = 0, NT = 0;
+    std::string who;
+    ~ExecSlot() {
+        for (DBuf* b : {&scr, &bctl, &btab, &bjobs, &bS, &bV0, &bV, &bit, &bcv, &blane}) b->release();
+        for (cudaEvent_t e : {e0, e1, c0, c1})
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+        if (host_ctl) cudaFreeHost(host_ctl);
+    }
+};
+
 struct gbpf_solver {
     gbpf::Plan plan;
     int n = 0, nnz = 0;
@@ -126,6 +146,7 @@ struct gbpf_solver {
     int fixed_NT = 0, fixed_G = 0;               // CTA shape requested at creation (0: by batch size)
     int table_NT[N_SIZE_CLASSES] = {}, table_G[N_SIZE_CLASSES] = {};  // shapes set per size class
     std::vector<std::unique_ptr<Shape>> shapes;
+    std::vector<std::unique_ptr<ExecSlot>> slots;  // asynchronous calls (gbpf_solve_lanes_async)
     // topology on the device
     DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos;
     gbpf::DevPlan dp{};  // topology part (schedule fields filled per shape)
@@ -143,6 +164,10 @@ struct gbpf_solver {
     bool gather_ready = false;
     gbpf_stats last{};
     ~gbpf_solver() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& sl : slots)
+            if (sl->stream) cudaStreamSynchronize(sl->stream);
+        slots.clear();
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
@@ -382,8 +407,17 @@ int check_params(const gbpf_params& p, const char* who) {
     return 0;
 }
 
-// Run the persistent kernel over `units` work items (cases, or lanes) and wait for it.
-int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
+// The launch of `units` work items (cases, or lanes) enqueued on a stream with its own
+// scratch and control block; read back with finish_launch.
+struct LaunchRes {
+    cudaStream_t stream;
+    cudaEvent_t e0, e1;
+    DBuf *scr, *bctl, *btab, *bjobs;
+    unsigned long long* host_ctl;  // 32 entries
+};
+
+int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units, const char* who, int* grid_out,
+                   int* G_out, int* NT_out) {
     if (units <= 0) return fail(std::string(who) + ": empty batch");
     int NT = 0, G = 0;
     choose_shape(s, units, &NT, &G);
@@ -396,44 +430,51 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     job.off = solver_offsets(s, G, b.mixed != 0);
     job.G = G;
     job.log2G = ilog2(G);
-    CK(s->scr.ensure((size_t)grid * job.off.total));
-    CK(s->bctl.ensure(64 * sizeof(unsigned long long)));
-    auto* ctl = s->bctl.as<unsigned long long>();
-    CK(cudaMemsetAsync(ctl, 0, 64 * sizeof(unsigned long long), s->stream));
+    CK(R.scr->ensure((size_t)grid * job.off.total));
+    CK(R.bctl->ensure(64 * sizeof(unsigned long long)));
+    auto* ctl = R.bctl->as<unsigned long long>();
+    CK(cudaMemsetAsync(ctl, 0, 64 * sizeof(unsigned long long), R.stream));
     b.counter = reinterpret_cast<int*>(ctl + 16);
     b.stats = ctl;
     b.err = reinterpret_cast<int*>(ctl + 24);
     if (b.v0_shared) {
-        CK(s->btab.ensure((size_t)s->n * 64));
-        b.v0tab = s->btab.as<double4_32a>();
+        CK(R.btab->ensure((size_t)s->n * 64));
+        b.v0tab = R.btab->as<double4_32a>();
     }
     job.B = b;
-    CK(s->bjobs.ensure(sizeof(gbpf::Job)));
-    CK(cudaMemcpyAsync(s->bjobs.p, &job, sizeof job, cudaMemcpyHostToDevice, s->stream));
+    CK(R.bjobs->ensure(sizeof(gbpf::Job)));
+    CK(cudaMemcpyAsync(R.bjobs->p, &job, sizeof job, cudaMemcpyHostToDevice, R.stream));
     gbpf::Launch L{};
-    L.jobs = s->bjobs.as<gbpf::Job>();
+    L.jobs = R.bjobs->as<gbpf::Job>();
     L.njobs = 1;
-    L.scratch = s->scr.as<char>();
+    L.scratch = R.scr->as<char>();
     L.cta_bytes = job.off.total;
-    CK(cudaEventRecord(s->e0, s->stream));
+    CK(cudaEventRecord(R.e0, R.stream));
     if (b.v0_shared)
-        CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, s->btab.as<double4_32a>(), b.err, s->stream));
-    CK(gbpf::launch_newton(L, grid, NT, s->stream));
-    CK(cudaEventRecord(s->e1, s->stream));
-    unsigned long long host_ctl[32];
-    CK(cudaMemcpyAsync(host_ctl, ctl, sizeof host_ctl, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+        CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, R.btab->as<double4_32a>(), b.err, R.stream));
+    CK(gbpf::launch_newton(L, grid, NT, R.stream));
+    CK(cudaEventRecord(R.e1, R.stream));
+    CK(cudaMemcpyAsync(R.host_ctl, ctl, 32 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.stream));
+    *grid_out = grid;
+    *G_out = G;
+    *NT_out = NT;
+    return 0;
+}
+
+// After the launch's stream has finished: its counters into `st`, its device errors reported.
+int finish_launch(const LaunchRes& R, int grid, int G, int NT, const char* who, gbpf_stats* st) {
     float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
-    s->last.single_factorizations = host_ctl[0];
-    s->last.double_factorizations = host_ctl[1];
-    s->last.single_rejected = host_ctl[2];
-    s->last.double_rejected = host_ctl[3];
-    s->last.macro_steps = host_ctl[4];
-    s->last.grid = grid;
-    s->last.cases_per_cta = G;
-    s->last.threads_per_cta = NT;
-    s->last.kernel_ms = ms;
+    CK(cudaEventElapsedTime(&ms, R.e0, R.e1));
+    const unsigned long long* host_ctl = R.host_ctl;
+    st->single_factorizations = host_ctl[0];
+    st->double_factorizations = host_ctl[1];
+    st->single_rejected = host_ctl[2];
+    st->double_rejected = host_ctl[3];
+    st->macro_steps = host_ctl[4];
+    st->grid = grid;
+    st->cases_per_cta = G;
+    st->threads_per_cta = NT;
+    st->kernel_ms = ms;
     const int* err = reinterpret_cast<const int*>(host_ctl + 24);
     if (err[0] == gbpf::DE_V0_NONFINITE)
         return fail(std::string(who) + ": invalid initial voltage at bus " + std::to_string(err[1]) + ", step " +
@@ -445,6 +486,16 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
         return fail(std::string(who) + ": case " + std::to_string(err[2]) + " has " + std::to_string(err[1]) +
                     " outage stamp entries, more than the " + std::to_string(gbpf::MAX_STAMPS) + " supported");
     return 0;
+}
+
+// Run the persistent kernel over `units` work items on the solver's own stream and wait.
+int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
+    unsigned long long host_ctl[32];
+    LaunchRes R{s->stream, s->e0, s->e1, &s->scr, &s->bctl, &s->btab, &s->bjobs, host_ctl};
+    int grid = 0, G = 0, NT = 0;
+    if (int rc = enqueue_launch(s, R, b, units, who, &grid, &G, &NT)) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return finish_launch(R, grid, G, NT, who, &s->last);
 }
 
 int record_call(gbpf_solver* s) {
@@ -946,6 +997,79 @@ int gbpf_solve_lanes(gbpf_solver* s, int T, const double* S, const double* V0, i
     CK(cudaEventRecord(s->c1, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return record_call(s);
+}
+
+int gbpf_solve_lanes_async(gbpf_solver* s, int slot, int T, const double* S, const double* V0, int K,
+                           const int64_t* off, const gbpf_params* pp, double* V, int32_t* it, uint8_t* cv) {
+    if (!s) return fail("null solver");
+    if (slot < 0 || slot >= 8) return fail("solve_lanes_async: slot must be in 0..7");
+    if (T <= 0 || K <= 0) return fail("solve_lanes_async: T and K must be > 0");
+    if (off[0] != 0 || off[K] != T) return fail("solve_lanes_async: offsets must start at 0 and end at T");
+    for (int l = 0; l < K; ++l)
+        if (off[l + 1] < off[l]) return fail("solve_lanes_async: offsets must be non-decreasing");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (int rc = check_params(p, "solve_lanes_async")) return rc;
+    while ((int)s->slots.size() <= slot) {
+        std::unique_ptr<ExecSlot> x(new ExecSlot);
+        CK(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&x->e0));
+        CK(cudaEventCreate(&x->e1));
+        CK(cudaEventCreate(&x->c0));
+        CK(cudaEventCreate(&x->c1));
+        CK(cudaMallocHost(&x->host_ctl, 32 * sizeof(unsigned long long)));
+        s->slots.push_back(std::move(x));
+    }
+    ExecSlot& X = *s->slots[slot];
+    if (X.pending) return fail("solve_lanes_async: slot " + std::to_string(slot) + " is still in flight (wait for it first)");
+    const size_t n = s->n;
+    const size_t sb = n * (size_t)T * 16, vb = n * 16;
+    CK(X.bS.ensure(sb));
+    CK(X.bV0.ensure(vb));
+    CK(X.bV.ensure(sb));
+    CK(X.bit.ensure((size_t)T * 4));
+    CK(X.bcv.ensure((size_t)T));
+    CK(X.blane.ensure((size_t)(K + 1) * 8));
+    CK(cudaEventRecord(X.c0, X.stream));
+    CK(cudaMemcpyAsync(X.bS.p, S, sb, cudaMemcpyHostToDevice, X.stream));
+    CK(cudaMemcpyAsync(X.bV0.p, V0, vb, cudaMemcpyHostToDevice, X.stream));
+    CK(cudaMemcpyAsync(X.blane.p, off, (size_t)(K + 1) * 8, cudaMemcpyHostToDevice, X.stream));
+    gbpf::Batch b{};
+    b.B = T;
+    b.lanes = 1;
+    b.K = K;
+    b.lane_off = X.blane.as<long long>();
+    b.S = X.bS.as<double2>();
+    b.sS = T;
+    b.V0 = X.bV0.as<double2>();
+    b.v0_shared = 1;
+    b.Vout = X.bV.as<double2>();
+    b.sV = T;
+    b.iters = X.bit.as<int32_t>();
+    b.conv = X.bcv.as<uint8_t>();
+    fill_common(b, s, p);
+    LaunchRes R{X.stream, X.e0, X.e1, &X.scr, &X.bctl, &X.btab, &X.bjobs, X.host_ctl};
+    if (int rc = enqueue_launch(s, R, b, K, "solve_lanes_async", &X.grid, &X.G, &X.NT)) return rc;
+    CK(cudaMemcpyAsync(V, X.bV.p, sb, cudaMemcpyDeviceToHost, X.stream));
+    CK(cudaMemcpyAsync(it, X.bit.p, (size_t)T * 4, cudaMemcpyDeviceToHost, X.stream));
+    CK(cudaMemcpyAsync(cv, X.bcv.p, (size_t)T, cudaMemcpyDeviceToHost, X.stream));
+    CK(cudaEventRecord(X.c1, X.stream));
+    X.pending = true;
+    return 0;
+}
+
+int gbpf_solve_wait(gbpf_solver* s, int slot) {
+    if (!s) return fail("null solver");
+    if (slot < 0 || slot >= (int)s->slots.size() || !s->slots[slot]->pending)
+        return fail("solve_wait: nothing in flight in slot " + std::to_string(slot));
+    ExecSlot& X = *s->slots[slot];
+    X.pending = false;
+    CK(cudaStreamSynchronize(X.stream));
+    LaunchRes R{X.stream, X.e0, X.e1, &X.scr, &X.bctl, &X.btab, &X.bjobs, X.host_ctl};
+    if (int rc = finish_launch(R, X.grid, X.G, X.NT, "solve_lanes_async", &s->last)) return rc;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, X.c0, X.c1));
+    s->last.call_ms = ms;
+    return 0;
 }
 
 int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double* V0, const uint8_t* pin,

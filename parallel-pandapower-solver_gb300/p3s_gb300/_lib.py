@@ -117,6 +117,9 @@ SIGNATURES = {
                                           _vp]),
     "gbpf_solve_lanes": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, _lp, C.POINTER(Params), _dp, _ip, _bp]),
     "gbpf_solve_lanes_device": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int, _vp, C.POINTER(Params), _vp, _vp, _vp]),
+    "gbpf_solve_lanes_async": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_int, _lp, C.POINTER(Params), _dp,
+                                         _ip, _bp]),
+    "gbpf_solve_wait": (C.c_int, [_vp, C.c_int]),
     "gbpf_solve_contingency": (C.c_int, [_vp, C.c_int, _dp, _dp, _bp, _dp, _ip, _ip, _dp, C.POINTER(Params), _dp,
                                          _ip, _bp]),
     "gbpf_dc_start": (C.c_int, [_vp, _dp, _dp, _dp]),

@@ -198,6 +198,29 @@ class GpuSolver:
         _lib.check(rc, "solve_lanes")
         return {"V": V, "iterations": it, "converged": cv.view(bool) if out is not None else cv.astype(bool)}
 
+    def solve_lanes_async(self, slot: int, S, V0, offsets, p: _lib.Params, out):
+        """Enqueue ``solve_lanes`` in `slot` and return at once; the arrays (use ``pinned_empty``
+        for S and the outputs) must stay alive until ``wait(slot)``. out = (V, iterations,
+        converged) caller-owned result arrays."""
+        V, it, cv = out
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        if not (S.flags.c_contiguous and S.dtype == np.complex128):
+            raise ValueError("solve_lanes_async: S must be a C-contiguous complex128 array")
+        V0 = c128(V0).ravel()
+        self._async_keep = getattr(self, "_async_keep", {})
+        self._async_keep[slot] = (S, V0, off, V, it, cv)
+        rc = _lib.load().gbpf_solve_lanes_async(self._h, int(slot), S.shape[1], _lib.cview(S), _lib.cview(V0),
+                                                len(off) - 1, _lib.i64(off), C.byref(p), _lib.cview(V), _lib.i32(it),
+                                                _lib.u8(cv))
+        _lib.check(rc, "solve_lanes_async")
+
+    def wait(self, slot: int):
+        """Wait for the call in `slot`; its results are in the arrays handed to it."""
+        rc = _lib.load().gbpf_solve_wait(self._h, int(slot))
+        keep = getattr(self, "_async_keep", {}).pop(slot, None)
+        _lib.check(rc, "solve_wait")
+        return keep
+
     def solve_lanes_device(self, dS: int, dV0: int, doff: int, T: int, K: int, p: _lib.Params, dV: int, dit: int,
                            dcv: int):
         """Device-pointer variant (inputs already resident); pointers as integers."""

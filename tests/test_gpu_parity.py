@@ -414,3 +414,31 @@ def test_uneven_grids_in_one_launch_match_their_own_solves():
                 ref = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(scen[i], g.V0)
                 assert np.array_equal(res[i]["iterations"], ref["iterations"])
                 assert np.abs(res[i]["V"] - ref["V"]).max() < TOL_V
+
+
+def test_async_slots_overlap_and_equal_the_synchronous_call(grid2000):
+    from p3s_gb300.solver import GpuSolver, pinned_empty
+
+    g = grid2000
+    T = 256
+    S = timeseries_injections(g, T)
+    off = lanes(T, 64)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    p = GpuSolver.params(precision="mixed")
+    ref = s.solve_lanes(S, g.V0, off, p)
+    outs = []
+    for slot in range(2):
+        Sh = pinned_empty(S.shape, np.complex128)
+        Sh[...] = S
+        out = (pinned_empty((g.n, T), np.complex128), pinned_empty((T,), np.int32), pinned_empty((T,), np.uint8))
+        s.solve_lanes_async(slot, Sh, g.V0, off, p, out)
+        outs.append(out)
+    with pytest.raises(RuntimeError, match="still in flight"):
+        s.solve_lanes_async(0, S, g.V0, off, p, outs[0])
+    for slot in range(2):
+        s.wait(slot)
+        V, it, cv = outs[slot]
+        assert np.array_equal(V, ref["V"]) and np.array_equal(it, ref["iterations"])
+        assert np.array_equal(cv.astype(bool), ref["converged"])
+    with pytest.raises(RuntimeError, match="nothing in flight"):
+        s.wait(0)
