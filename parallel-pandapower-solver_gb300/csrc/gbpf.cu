@@ -259,6 +259,15 @@ int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     return 0;
 }
 
+// CTAs of a launch that needs `want` of them: at most the resident ones; when more than one
+// per SM is needed, a whole number per SM, so that every SM gets the same share of the cases
+// (the case slots of the extra CTAs are filled by the work counter as cases free up).
+int grid_size(int nsm, int occ, long long want) {
+    const long long resident = (long long)nsm * std::max(1, occ);
+    if (want > nsm) want = (want + nsm - 1) / nsm * nsm;
+    return (int)std::max<long long>(1, std::min(want, resident));
+}
+
 int size_class(long long units) {
     int c = 0;
     while (c + 1 < N_SIZE_CLASSES && (1LL << c) < units) ++c;
@@ -423,8 +432,7 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     choose_shape(s, units, &NT, &G);
     Shape* sh = nullptr;
     if (int rc = get_shape(s, NT, G, &sh)) return rc;
-    const long long want = (units + G - 1) / G;
-    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)s->nsm * sh->occ));
+    const int grid = grid_size(s->nsm, sh->occ, (units + G - 1) / G);
     gbpf::Job job{};
     job.P = sh->dp;
     job.off = solver_offsets(s, G, b.mixed != 0);
@@ -702,7 +710,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         b.err = reinterpret_cast<int*>(c + 24);
         o.B = b;
     }
-    const int grid = (int)std::max<long long>(1, std::min<long long>(want, (long long)g->nsm * occ));
+    const int grid = grid_size(g->nsm, occ, want);
     CK(g->scr.ensure((size_t)grid * cta_bytes));
     CK(g->bjobs.ensure((size_t)nj * sizeof(gbpf::Job)));
     CK(cudaMemcpyAsync(g->bjobs.p, hj.data(), (size_t)nj * sizeof(gbpf::Job), cudaMemcpyHostToDevice, g->stream));
