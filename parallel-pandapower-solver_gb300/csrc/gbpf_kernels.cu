@@ -333,6 +333,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     const int W = P.W;
     const bool act = on[s] != 0;
     real pmin = sizeof(real) == 4 ? (real)FLT_MAX : (real)DBL_MAX, pmax = 0;
+    B4 dinv = z4<B4>();  // the worker's last inverse diagonal block: scales the L column after it
     for (int h = 0; h < P.nlev; ++h) {
         if (act) {
             const int t0 = __ldg(&P.ptrA[h * W + w]), t1 = __ldg(&P.ptrA[h * W + w + 1]);
@@ -405,24 +406,17 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     o.z = -acc.z * inv;
                     o.w = acc.x * inv;
                     fac[((size_t)task.x << lg) + s] = o;
+                    dinv = o;
+                } else if (task.y & 8) {  // L block: scaled by its column's inverse diagonal
+                    B4 o;
+                    o.x = acc.x * dinv.x + acc.y * dinv.z;
+                    o.y = acc.x * dinv.y + acc.y * dinv.w;
+                    o.z = acc.z * dinv.x + acc.w * dinv.z;
+                    o.w = acc.z * dinv.y + acc.w * dinv.w;
+                    fac[((size_t)task.x << lg) + s] = o;
                 } else {
                     fac[((size_t)task.x << lg) + s] = acc;
                 }
-            }
-        }
-        __syncthreads();
-        if (act) {
-            const int t0 = __ldg(&P.ptrB[h * W + w]), t1 = __ldg(&P.ptrB[h * W + w + 1]);
-            for (int t = t0; t < t1; ++t) {
-                const int2 sc = __ldg(&P.scl[t]);
-                const B4 l = fac[((size_t)sc.x << lg) + s];
-                const B4 d = fac[((size_t)sc.y << lg) + s];
-                B4 o;
-                o.x = l.x * d.x + l.y * d.z;
-                o.y = l.x * d.y + l.y * d.w;
-                o.z = l.z * d.x + l.w * d.z;
-                o.w = l.z * d.y + l.w * d.w;
-                fac[((size_t)sc.x << lg) + s] = o;
             }
         }
         __syncthreads();

@@ -80,7 +80,8 @@ using Task = PlanTask;
 void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& out, std::vector<int>& ptr,
             std::vector<int>* level_work, bool four) {
     std::vector<std::vector<int>> by_level(nlev);
-    for (int i = 0; i < (int)tasks.size(); ++i) by_level[tasks[i].level].push_back(i);
+    for (int i = 0; i < (int)tasks.size(); ++i)
+        if (tasks[i].head) by_level[tasks[i].level].push_back(i);
     ptr.assign((size_t)nlev * W + 1, 0);
     out.clear();
     std::vector<long long> wts;
@@ -88,19 +89,24 @@ void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& o
     for (int h = 0; h < nlev; ++h) {
         auto& ids = by_level[h];
         wts.resize(ids.size());
-        for (size_t i = 0; i < ids.size(); ++i) wts[i] = tasks[ids[i]].w;
+        for (size_t i = 0; i < ids.size(); ++i) {
+            wts[i] = 0;
+            for (int q = ids[i]; q >= 0; q = tasks[q].next) wts[i] += tasks[q].w;
+        }
         const int mx = deal(wts, W, who);
         if (level_work) (*level_work)[h] += mx;
         for (int w = 0; w < W; ++w) {
             ptr[(size_t)h * W + w] = four ? (int)(out.size() / 4) : (int)(out.size() / 2);
             for (size_t i = 0; i < ids.size(); ++i) {
                 if (who[i] != w) continue;
-                const Task& t = tasks[ids[i]];
-                out.push_back(t.dst);
-                out.push_back(t.code);
-                if (four) {
-                    out.push_back(t.p0);
-                    out.push_back(t.p1);
+                for (int q = ids[i]; q >= 0; q = tasks[q].next) {
+                    const Task& t = tasks[q];
+                    out.push_back(t.dst);
+                    out.push_back(t.code);
+                    if (four) {
+                        out.push_back(t.p0);
+                        out.push_back(t.p1);
+                    }
                 }
             }
         }
@@ -284,8 +290,10 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
     for (int t = 0; t < nv; ++t) {
         const int h = p.height[t];
         int p0, p1;
-        // diagonal
+        // diagonal, then its column of L on the same worker (each L block scaled by the
+        // inverse diagonal the worker just computed)
         add_pairs_factor(p.base[t], p0, p1);
+        int prev = (int)A.size();
         A.push_back({h, p.base[t], TK_DIAG | (inA[p.base[t]] ? 0 : TASK_FILL), p0, p1, 8LL * (p1 - p0) + 24});
         p.n_factor_pairs += p1 - p0;
         for (int x = p.Lp[t]; x < p.Lp[t + 1]; ++x) {
@@ -296,12 +304,13 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
                 A.push_back({h, qu, TK_U | (inA[qu] ? 0 : TASK_FILL), p0, p1, 8LL * (p1 - p0) + 8});
                 p.n_factor_pairs += p1 - p0;
             }
-            if (poff[ql + 1] > poff[ql] || !inA[ql]) {
-                add_pairs_factor(ql, p0, p1);
-                A.push_back({h, ql, TK_L | (inA[ql] ? 0 : TASK_FILL), p0, p1, 8LL * (p1 - p0) + 8});
-                p.n_factor_pairs += p1 - p0;
-            }
-            B.push_back({h, ql, p.base[t], 0, 0, 8});
+            add_pairs_factor(ql, p0, p1);
+            const int me = (int)A.size();
+            A.push_back({h, ql, TK_L | TASK_SCALE | (inA[ql] ? 0 : TASK_FILL), p0, p1, 8LL * (p1 - p0) + 12});
+            A[me].head = false;
+            A[prev].next = me;
+            prev = me;
+            p.n_factor_pairs += p1 - p0;
         }
         // forward substitution of block row t (its L row is final after lower levels)
         p0 = (int)(p.pairs.size() / 2);
@@ -421,7 +430,8 @@ bool host_factor(const Plan& p, double* blk, double* pmin, double* pmax) {
     bool ok = true;
     const int W = p.W;
     for (int h = 0; h < p.nlev; ++h) {
-        for (int w = 0; w < W; ++w)
+        for (int w = 0; w < W; ++w) {
+            double dinv[4] = {0, 0, 0, 0};  // the worker's last inverse diagonal block
             for (int t = p.ptrA[(size_t)h * W + w]; t < p.ptrA[(size_t)h * W + w + 1]; ++t) {
                 const int* T = &p.taskA[4 * (size_t)t];
                 const int kind = T[1] & 3;
@@ -450,10 +460,17 @@ bool host_factor(const Plan& p, double* blk, double* pmin, double* pmax) {
                     o[1] = -acc[1] * inv;
                     o[2] = -acc[2] * inv;
                     o[3] = acc[0] * inv;
+                    for (int e = 0; e < 4; ++e) dinv[e] = o[e];
+                } else if (T[1] & TASK_SCALE) {
+                    o[0] = acc[0] * dinv[0] + acc[1] * dinv[2];
+                    o[1] = acc[0] * dinv[1] + acc[1] * dinv[3];
+                    o[2] = acc[2] * dinv[0] + acc[3] * dinv[2];
+                    o[3] = acc[2] * dinv[1] + acc[3] * dinv[3];
                 } else {
                     for (int e = 0; e < 4; ++e) o[e] = acc[e];
                 }
             }
+        }
         for (int w = 0; w < W; ++w)
             for (int t = p.ptrB[(size_t)h * W + w]; t < p.ptrB[(size_t)h * W + w + 1]; ++t) {
                 double* l = blk + 4 * (size_t)p.scl[2 * t];
@@ -527,7 +544,9 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                 }
             }
         // execute the entry phase in reverse worker order (any order must give the same result)
-        for (int w = W - 1; w >= 0; --w)
+        for (int w = W - 1; w >= 0; --w) {
+            double dinv[4] = {0, 0, 0, 0};
+            int dinv_level = -1;
             for (int t = p.ptrA[(size_t)h * W + w]; t < p.ptrA[(size_t)h * W + w + 1]; ++t) {
                 const int* T = &p.taskA[4 * (size_t)t];
                 const int kind = T[1] & 3;
@@ -563,10 +582,19 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                     o[1] = -acc[1] * inv;
                     o[2] = -acc[2] * inv;
                     o[3] = acc[0] * inv;
+                    for (int e = 0; e < 4; ++e) dinv[e] = o[e];
+                    dinv_level = h;
+                } else if (T[1] & TASK_SCALE) {
+                    if (dinv_level != h) return "level " + std::to_string(h) + ": an L block without its diagonal";
+                    o[0] = acc[0] * dinv[0] + acc[1] * dinv[2];
+                    o[1] = acc[0] * dinv[1] + acc[1] * dinv[3];
+                    o[2] = acc[2] * dinv[0] + acc[3] * dinv[2];
+                    o[3] = acc[2] * dinv[1] + acc[3] * dinv[3];
                 } else {
                     for (int e = 0; e < 4; ++e) o[e] = acc[e];
                 }
             }
+        }
         for (int w = W - 1; w >= 0; --w)
             for (int t = p.ptrB[(size_t)h * W + w]; t < p.ptrB[(size_t)h * W + w + 1]; ++t) {
                 double* l = blk + 4 * (size_t)p.scl[2 * t];

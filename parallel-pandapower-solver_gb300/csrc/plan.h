@@ -12,9 +12,12 @@
 //    loads for the same 8 FMAs), and the elimination tree is the bus graph's -- half the
 //    height of the scalar one, i.e. half the barriers per factorization.
 //  * The fill-reducing order is a minimum-degree order of the bus graph.
-//  * Factor entries are computed in Crout form, one task per block; tasks are grouped by
-//    elimination-tree height (level) and dealt to the CTA's workers longest-first onto
-//    the least-loaded worker. The forward substitution rides along in the same levels.
+//  * Factor entries are computed in Crout form, one task per block; a pivot's diagonal block
+//    and its column of L form one chain on one worker (the inverse diagonal stays in
+//    registers and scales each L block as it is computed: no separate scaling pass, one
+//    barrier per level). Tasks and chains are grouped by elimination-tree height (level) and
+//    dealt to the CTA's workers longest-first onto the least-loaded worker. The forward
+//    substitution rides along in the same levels.
 #pragma once
 
 #include <cstdint>
@@ -24,20 +27,23 @@
 namespace gbpf {
 
 enum TaskKind { TK_DIAG = 0, TK_U = 1, TK_L = 2, TK_FWD = 3 };
-constexpr int TASK_FILL = 1 << 4;  // block not in the Jacobian: accumulate from zero
+constexpr int TASK_SCALE = 1 << 3;  // L block: multiply by the inverse diagonal block computed just before
+constexpr int TASK_FILL = 1 << 4;   // block not in the Jacobian: accumulate from zero
 
 // One unit of factorization work before it is dealt to a worker: its level, destination
 // block (or row), code, pair range and weight (the dealing key).
 struct PlanTask {
     int level, dst, code, p0, p1;
     long long w;
+    int next = -1;     // the next task of its chain (dealt to the same worker, laid out right after)
+    bool head = true;  // first task of a chain (or a task on its own)
 };
 
 // The worker-dependent part of a plan: the level tasks dealt to W workers.
 struct Schedule {
     int W = 0;
     std::vector<int> taskA, ptrA;   // entry tasks (4 ints) and per-(level, worker) ranges
-    std::vector<int> scl, ptrB;     // L scalings (2 ints)
+    std::vector<int> scl, ptrB;     // L scalings (2 ints; empty: L blocks are scaled in their column chain)
     std::vector<int> taskC, ptrC;   // backward substitution tasks (4 ints)
     std::vector<int> level_work;    // per level: max worker load
 };
