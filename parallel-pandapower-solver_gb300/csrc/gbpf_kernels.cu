@@ -523,8 +523,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     double2* R = reinterpret_cast<double2*>(region + off.R);
     double2* y64 = reinterpret_cast<double2*>(region + off.y64);
     float2* y32 = off.y32 != ~0ULL ? reinterpret_cast<float2*>(region + off.y32) : nullptr;
-    double4_32a* Vc = reinterpret_cast<double4_32a*>(region + off.Vc);
-    double4_32a* Vt = reinterpret_cast<double4_32a*>(region + off.Vt);
+    // two state buffers per slot: the last evaluated point lives in Vb[s_tb[s]], the committed
+    // point (while a line search backtracks) in the other -- accepting a step flips s_tb
+    // instead of copying the state
+    double4_32a* const Vb0 = reinterpret_cast<double4_32a*>(region + off.Vc);
+    double4_32a* const Vb1 = reinterpret_cast<double4_32a*>(region + off.Vt);
     double2* Et = reinterpret_cast<double2*>(region + off.Et);
     double* Ei = reinterpret_cast<double*>(region + off.Ei);
     float4* V32 = reinterpret_cast<float4*>(region + off.V32);
@@ -542,6 +545,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ double s_nrm[MAX_SLOTS], s_alpha[MAX_SLOTS], s_balpha[MAX_SLOTS], s_bnrm[MAX_SLOTS];
     __shared__ unsigned long long s_res[MAX_SLOTS], s_pmin[MAX_SLOTS], s_pmax[MAX_SLOTS];
     __shared__ int s_nst[MAX_SLOTS];
+    __shared__ int s_tb[MAX_SLOTS];
     __shared__ int s_stk[MAX_SLOTS][MAX_STAMPS];
     __shared__ double2 s_stv[MAX_SLOTS][MAX_STAMPS];
 
@@ -586,6 +590,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 } else {
                     s_case[s] = (int)c;
                     s_st[s] = SL_FRESH;
+                    if (!s_warm[s]) s_tb[s] = 0;
                     s_it[s] = 0;
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
@@ -649,13 +654,12 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int bus = idx >> lg;
             const int c = s_case[s];
             if (s_warm[s]) {
-                // previous hour of the lane converged here: its state is the start point
-                Vc[idx] = Vt[idx];
+                // previous hour of the lane converged here: its evaluated state is the start point
             } else if (Bt.v0_shared) {
                 // shared start: the state table built once per launch (v0_table_kernel)
                 const double4_32a t0 = Bt.v0tab[2 * bus], t1 = Bt.v0tab[2 * bus + 1];
-                Vc[idx] = t0;
-                Vt[idx] = t0;
+                Vb0[idx] = t0;
+                Vb1[idx] = t0;
                 Et[idx] = make_double2(t1.x, t1.y);
                 Ei[idx] = t1.z;
                 V32[idx] = make_float4(d2f_fast(t1.x), d2f_fast(t1.y), d2f_fast(t1.z), 0.f);
@@ -678,8 +682,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 double sn, cs;
                 sincos(va, &sn, &cs);
                 const double4_32a v = make_double4_32a(vm, va, cs, sn);
-                Vc[idx] = v;
-                Vt[idx] = v;
+                Vb0[idx] = v;
+                Vb1[idx] = v;
                 const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
                 Et[idx] = make_double2(e, f);
                 Ei[idx] = iv;
@@ -699,7 +703,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                         iv = 1.0;
                         pinned = 1;
                     } else {
-                        const double4_32a t0 = Vt[idx];
+                        const double4_32a t0 = Vb0[idx];
                         iv = Ei[idx];
                         if (r == bus) {
                             v = make_double4_32a(t0.x, 0.0, 1.0, 0.0);
@@ -710,8 +714,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                                                  fma(t0.w, tr.z, -t0.z * tr.w));
                         }
                     }
-                    Vc[idx] = v;
-                    Vt[idx] = v;
+                    Vb0[idx] = v;
+                    Vb1[idx] = v;
                     const double e = v.x * v.z, f = v.x * v.w;
                     Et[idx] = make_double2(e, f);
                     Ei[idx] = iv;
@@ -753,7 +757,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         if (anyre) {  // this step's factorization is double but the Jacobian was built in float
             for (int idx = tid; idx < nG; idx += NT) {
                 const int s = idx & (G - 1);
-                if (s_reeval[s]) Ei[idx] = recip_nr(Vt[idx].x);
+                if (s_reeval[s]) Ei[idx] = recip_nr((s_tb[s] ? Vb1 : Vb0)[idx].x);
             }
             __syncthreads();
             for (int idx = tid; idx < nG; idx += NT) {
@@ -794,13 +798,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int row = P.row_of_bus[bus];
             if (row < 0) continue;
             const bool active = st == SL_ACTIVE;
-            double4_32a vc;
-            if (active) {  // the point evaluated last was accepted: commit it
-                vc = Vt[idx];
-                Vc[idx] = vc;
-            } else {
-                vc = Vc[idx];
-            }
+            // committed point: the one evaluated last when it was accepted (ACTIVE), else the
+            // other buffer; the new trial goes to the buffer that is not committed
+            const int cb = active ? s_tb[s] : 1 - s_tb[s];
+            const double4_32a vc = (cb ? Vb1 : Vb0)[idx];
+            double4_32a* const Vt = cb ? Vb0 : Vb1;
             double dth, dvm;
             if (s_yprec[s]) {
                 const float2 dd = y32[((size_t)row << lg) + s];
@@ -876,6 +878,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         if (tid < G) {
             const int s = tid;
             const int st = s_st[s];
+            if (st == SL_ACTIVE) s_tb[s] ^= 1;  // the trial just evaluated is in the other buffer
             double nw = bitsd(s_res[s]);
             if (!(nw < BIG)) nw = BIG;
             bool top = false;
@@ -962,7 +965,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int s = idx & (G - 1);
             if (s_st[s] != SL_FINISH) continue;
             const int bus = idx >> lg;
-            const double4_32a v = Vt[idx];
+            const double4_32a v = (s_tb[s] ? Vb1 : Vb0)[idx];
             double2 o = make_double2(v.x * v.z, v.x * v.w);
             if (Bt.ref_bus && Bt.ref_bus[(size_t)bus * Bt.sref + s_case[s]] < 0)
                 o = make_double2(__longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0x7ff8000000000000LL));
