@@ -164,9 +164,11 @@ int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* 
 int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
 
 /* Device check of the kernels' integer-pipe float/double conversions: d2f[i] = in[i]
- * converted to float (round toward zero), f2d[i] = d2f[i] converted back to double. No
+ * converted to float (round toward zero), f2d[i] = d2f[i] converted back to double, and
+ * d2f_small[i] (optional, may be NULL) = in[i] through the short conversion the float
+ * Jacobian applies to voltage components (equal to d2f[i] for finite |in[i]| < 2^128). No
  * reference counterpart (a GB300-specific helper). */
-int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d);
+int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
 
 /* Page-locked host memory for fast transfers. */
 void* gbpf_host_alloc(size_t bytes);

@@ -96,7 +96,7 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
     o.Vt = take((unsigned long long)n * g * 32);
     o.Et = take((unsigned long long)n * g * 16);
     o.Ei = take((unsigned long long)n * g * 8);
-    o.V32 = take((unsigned long long)n * g * 16);
+    o.iv32 = take((unsigned long long)n * g * 4);
     o.pin = take((unsigned long long)n * g);
     o.total = at;
     return o;
@@ -106,10 +106,10 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
 // and the factorization schedule dealt to its NT / G workers (built on first use).
 struct Shape {
     int NT = 0, G = 0, lg = 0, occ = 1;
-    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC;
+    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dheadA, dheadC;
     gbpf::DevPlan dp{};
     ~Shape() {
-        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC}) b->release();
+        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC, &dheadA, &dheadC}) b->release();
     }
 };
 
@@ -329,6 +329,23 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
             if (p.row_pq[row]) sc.taskA[4 * t + 1] |= 32;
         }
     }
+    // the first two pairs of every task inline beside its record: a worker fetches them with
+    // the record, one task ahead, and starts the task's block loads without first waiting for
+    // its pair list
+    auto head_pairs = [&](const std::vector<int>& tasks) {
+        const size_t nt = tasks.size() / 4;
+        std::vector<int> head(4 * nt, -1);
+        for (size_t t = 0; t < nt; ++t) {
+            const int p0 = tasks[4 * t + 2], p1 = tasks[4 * t + 3];
+            for (int k = 0; k < 2 && p0 + k < p1; ++k) {
+                head[4 * t + 2 * k] = p.pairs[2 * (size_t)(p0 + k)];
+                head[4 * t + 2 * k + 1] = p.pairs[2 * (size_t)(p0 + k) + 1];
+            }
+        }
+        return head;
+    };
+    CK(upload(sh->dheadA, head_pairs(sc.taskA)));
+    CK(upload(sh->dheadC, head_pairs(sc.taskC)));
     CK(upload(sh->dtaskA, sc.taskA));
     CK(upload(sh->dptrA, sc.ptrA));
     CK(upload(sh->dscl, sc.scl));
@@ -343,6 +360,8 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     sh->dp.ptrB = sh->dptrB.as<int>();
     sh->dp.taskC = sh->dtaskC.as<int4>();
     sh->dp.ptrC = sh->dptrC.as<int>();
+    sh->dp.headA = sh->dheadA.as<int4>();
+    sh->dp.headC = sh->dheadC.as<int4>();
     *out = sh.get();
     s->shapes.push_back(std::move(sh));
     return 0;
@@ -382,6 +401,8 @@ int upload_plan(gbpf_solver* s) {
     d.ptrB = nullptr;
     d.taskC = nullptr;
     d.ptrC = nullptr;
+    d.headA = nullptr;
+    d.headC = nullptr;
     d.pairs = s->dpairs.as<int2>();
     d.row_pq = s->drow_pq.as<uint8_t>();
     d.bus_of_row = s->dbus_of_row.as<int>();
@@ -1202,9 +1223,9 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
                        double* residual) {
     if (!s) return fail("null solver");
     const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv);
-    DBuf dV, dSb, dpin, dVt, dEt, dEi, dV32, dblk, dR;
+    DBuf dV, dSb, dpin, dVt, dEt, dEi, div32, dblk, dR;
     auto cleanup = [&]() {
-        for (DBuf* b : {&dV, &dSb, &dpin, &dVt, &dEt, &dEi, &dV32, &dblk, &dR}) b->release();
+        for (DBuf* b : {&dV, &dSb, &dpin, &dVt, &dEt, &dEi, &div32, &dblk, &dR}) b->release();
     };
     struct Guard {
         std::function<void()> f;
@@ -1215,7 +1236,7 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
     CK(dVt.ensure(n * 32));
     CK(dEt.ensure(n * 16));
     CK(dEi.ensure(n * 8));
-    CK(dV32.ensure(n * 16));
+    CK(div32.ensure(n * 4));
     CK(dblk.ensure(nb * 32));
     CK(dR.ensure(nv * 16));
     CK(cudaMemcpy(dV.p, V, n * 16, cudaMemcpyHostToDevice));
@@ -1227,7 +1248,7 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
         CK(cudaMemcpy(dpin.p, pin, n, cudaMemcpyHostToDevice));
     }
     CK(gbpf::launch_eval_debug(s->dp, dV.as<double2>(), dSb.as<double2>(), pin ? dpin.as<uint8_t>() : nullptr,
-                               dVt.as<double4_32a>(), dEt.as<double2>(), dEi.as<double>(), dV32.as<float4>(),
+                               dVt.as<double4_32a>(), dEt.as<double2>(), dEi.as<double>(), div32.as<float>(),
                                dblk.as<double4_32a>(),
                                dR.as<double2>(), s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -1236,20 +1257,23 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
     return 0;
 }
 
-int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d) {
+int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small) {
     if (n <= 0) return 0;
-    DBuf a, b, c;
+    DBuf a, b, c, d;
     CK(a.ensure((size_t)n * 8));
     CK(b.ensure((size_t)n * 4));
     CK(c.ensure((size_t)n * 8));
+    CK(d.ensure((size_t)n * 4));
     CK(cudaMemcpy(a.p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
-    CK(gbpf::launch_conversions(a.as<double>(), n, b.as<float>(), c.as<double>()));
+    CK(gbpf::launch_conversions(a.as<double>(), n, b.as<float>(), c.as<double>(), d.as<float>()));
     CK(cudaDeviceSynchronize());
     CK(cudaMemcpy(d2f, b.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(f2d, c.p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    if (d2f_small) CK(cudaMemcpy(d2f_small, d.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
     a.release();
     b.release();
     c.release();
+    d.release();
     return 0;
 }
 

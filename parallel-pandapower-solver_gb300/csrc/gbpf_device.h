@@ -47,6 +47,8 @@ struct DevPlan {
     const int* ptrB;
     const int4* taskC;
     const int* ptrC;
+    const int4* headA;       // per taskA entry: its first two pairs inline (x0, y0, x1, y1; -1 = none)
+    const int4* headC;       // per taskC entry: likewise
     const int2* pairs;
     const uint8_t* row_pq;   // block row is PQ (two real pivots)
     const int* bus_of_row;
@@ -114,7 +116,7 @@ struct ScratchOffsets {
     unsigned long long Vt;     // [bus][slot] evaluation point (Vm, Va, cos, sin)
     unsigned long long Et;     // [bus][slot] evaluation point rectangular (e, f)
     unsigned long long Ei;     // [bus][slot] evaluation point 1 / Vm
-    unsigned long long V32;    // [bus][slot] evaluation point (e, f, 1 / Vm, 0) in float
+    unsigned long long iv32;   // [bus][slot] 1 / Vm of the evaluation point in float (PQ buses)
     unsigned long long pin;    // [bus][slot]
     unsigned long long total;  // bytes of the job's region
 };
@@ -146,10 +148,10 @@ cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t s
 cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_bus, double4_32a* fac, double2* R,
                       double2* y, double* theta, unsigned long long* piv, cudaStream_t stream);
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                              double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                              double4_32a* Vt, double2* Et, double* Ei, float* iv32, double4_32a* blocks,
                               double2* R, cudaStream_t stream);
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
-cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d);
+cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
 // Ybus values from stamps (postproc.cu)
 cudaError_t launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,
                                const double2* shunt, double2* Y, float2* Y32, cudaStream_t stream);

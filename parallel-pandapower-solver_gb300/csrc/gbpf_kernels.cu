@@ -78,6 +78,17 @@ __device__ __forceinline__ double f2d_fast(float f) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// double -> float by truncation for finite |x| < 2^128 (voltage components): the bits
+// d2f_fast gives there, in five integer operations -- the exponent is rebased by
+// subtracting (1023 - 127) << 23 from the funnel-shifted exponent / mantissa, and
+// magnitudes below 2^-126 go to a signed zero
+__device__ __forceinline__ float d2f_trunc(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned a = hi & 0x7fffffffu;
+    const unsigned m = __funnelshift_l(lo, a, 3) - (896u << 23);
+    return __uint_as_float((hi & 0x80000000u) | (a >= (897u << 20) ? m : 0u));
+}
+
 // |x| as ordered bits (sign cleared): compares like the magnitudes, NaN above everything
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
     return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
@@ -139,7 +150,7 @@ struct EvalCtx {
     const DevPlan* P;
     const double2* Et;   // [bus][slot] (e, f)
     const double* Ei;    // [bus][slot] 1 / Vm
-    const float4* V32;   // [bus][slot] (e, f, 1 / Vm, 0) in float
+    const float* iv32;   // [bus][slot] 1 / Vm in float (PQ buses)
     int lg;
     int ymode;
     const double2* Yd;
@@ -183,8 +194,10 @@ __device__ unsigned long long eval_row(const EvalCtx& c, int i, int s, int row, 
     const DevPlan& P = *c.P;
     const size_t si = ((size_t)i << c.lg) + s;
     const double2 ei = c.Et[si];
+    // float copy of the evaluation point for the float Jacobian: (e, f) truncated from the
+    // double phasor, 1 / Vm from its float array (read for PQ buses only)
     float4 vi32 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (JM == 2) vi32 = c.V32[si];
+    if (JM == 2) vi32 = make_float4(d2f_trunc(ei.x), d2f_trunc(ei.y), pq_i ? c.iv32[si] : 0.f, 0.f);
     double Ir = 0.0, Ii = 0.0, gii = 0.0, bii = 0.0;
     float gii32 = 0.f, bii32 = 0.f;
     const int k0 = __ldg(&P.Yp[i]), k1 = __ldg(&P.Yp[i + 1]);
@@ -237,7 +250,7 @@ __device__ unsigned long long eval_row(const EvalCtx& c, int i, int s, int row, 
                 gx = d2f_fast(y.x);
                 gy = d2f_fast(y.y);
             }
-            const float4 vj = c.V32[sj];
+            const float4 vj = make_float4(d2f_trunc(ej.x), d2f_trunc(ej.y), pq_j ? c.iv32[sj] : 0.f, 0.f);
             const float wr = fmaf(-gy, vj.y, gx * vj.x), wi = fmaf(gy, vj.x, gx * vj.y);
             const float Wr = fmaf(vi32.x, wr, vi32.y * wi), Wi = fmaf(vi32.y, wr, -vi32.x * wi);
             reinterpret_cast<float4*>(fac)[at] =
@@ -319,8 +332,8 @@ __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
 
 // One batched factorization + substitution pass over the slots flagged in `on` (G <= 32).
 // Worker w = (warp, lane / G) runs its task list of every level for its G slot lanes;
-// the CTA meets at a barrier after each level's entry phase and scale phase, and after
-// each backward level. Pivot statistics per slot go to smin / smax (as ordered bits).
+// the CTA meets at a barrier after each level, forward and backward. Pivot statistics per
+// slot go to smin / smax (as ordered bits).
 template <typename real>
 __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
                         const int* on, int lg, unsigned long long* smin, unsigned long long* smax) {
@@ -332,17 +345,29 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     const int w = (tid >> 5) * (32 >> lg) + (lane >> lg);
     const int W = P.W;
     const bool act = on[s] != 0;
+    // float passes take each task's first two pairs from its head record (the double pass
+    // keeps its registers for the wider blocks)
+    constexpr bool HEAD = sizeof(real) == 4;
     real pmin = sizeof(real) == 4 ? (real)FLT_MAX : (real)DBL_MAX, pmax = 0;
     B4 dinv = z4<B4>();  // the worker's last inverse diagonal block: scales the L column after it
     for (int h = 0; h < P.nlev; ++h) {
         if (act) {
             const int t0 = __ldg(&P.ptrA[h * W + w]), t1 = __ldg(&P.ptrA[h * W + w + 1]);
-            // the next task's record is fetched while the current one runs
-            int4 next = t0 < t1 ? __ldg(&P.taskA[t0]) : make_int4(0, 0, 0, 0);
+            // the next task's record and first two pairs are fetched while the current one
+            // runs, so a task's block loads all go out at once when it starts
+            int4 next = make_int4(0, 0, 0, 0), nhead = make_int4(0, 0, 0, 0);
+            if (t0 < t1) {
+                next = __ldg(&P.taskA[t0]);
+                if constexpr (HEAD) nhead = __ldg(&P.headA[t0]);
+            }
             for (int t = t0; t < t1; ++t) {
-                const int4 task = next;
-                if (t + 1 < t1) next = __ldg(&P.taskA[t + 1]);
+                const int4 task = next, hd = nhead;
+                if (t + 1 < t1) {
+                    next = __ldg(&P.taskA[t + 1]);
+                    if constexpr (HEAD) nhead = __ldg(&P.headA[t + 1]);
+                }
                 const int kind = task.y & 3;
+                const int np = HEAD ? min(task.w - task.z, 2) : 0;  // pairs taken from the head
                 if (kind == 3) {  // forward substitution of block row task.x
                     const double2 r = R[((size_t)task.x << lg) + s];
                     real y0, y1;
@@ -353,7 +378,23 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         y0 = r.x;
                         y1 = r.y;
                     }
-                    int p = task.z;
+                    if (np > 0) {
+                        const B4 l0 = fac[((size_t)hd.x << lg) + s];
+                        const B2 u0 = y[((size_t)hd.y << lg) + s];
+                        B4 l1 = z4<B4>();
+                        B2 u1 = {};
+                        if (np > 1) {
+                            l1 = fac[((size_t)hd.z << lg) + s];
+                            u1 = y[((size_t)hd.w << lg) + s];
+                        }
+                        y0 -= l0.x * u0.x + l0.y * u0.y;
+                        y1 -= l0.z * u0.x + l0.w * u0.y;
+                        if (np > 1) {
+                            y0 -= l1.x * u1.x + l1.y * u1.y;
+                            y1 -= l1.z * u1.x + l1.w * u1.y;
+                        }
+                    }
+                    int p = task.z + np;
                     for (; p + 1 < task.w; p += 2) {
                         const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
                         const B4 l0 = fac[((size_t)q0.x << lg) + s], l1 = fac[((size_t)q1.x << lg) + s];
@@ -377,7 +418,17 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     continue;
                 }
                 B4 acc = (task.y & 16) ? z4<B4>() : fac[((size_t)task.x << lg) + s];
-                int p = task.z;
+                if (np > 0) {
+                    const B4 a0 = fac[((size_t)hd.x << lg) + s], b0 = fac[((size_t)hd.y << lg) + s];
+                    if (np > 1) {
+                        const B4 a1 = fac[((size_t)hd.z << lg) + s], b1 = fac[((size_t)hd.w << lg) + s];
+                        mm_sub(acc, a0, b0);
+                        mm_sub(acc, a1, b1);
+                    } else {
+                        mm_sub(acc, a0, b0);
+                    }
+                }
+                int p = task.z + np;
                 for (; p + 1 < task.w; p += 2) {
                     const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
                     const B4 a0 = fac[((size_t)q0.x << lg) + s], b0 = fac[((size_t)q0.y << lg) + s];
@@ -424,13 +475,38 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     for (int h = 0; h < P.nblev; ++h) {
         if (act) {
             const int t0 = __ldg(&P.ptrC[h * W + w]), t1 = __ldg(&P.ptrC[h * W + w + 1]);
-            int4 next = t0 < t1 ? __ldg(&P.taskC[t0]) : make_int4(0, 0, 0, 0);
+            int4 next = make_int4(0, 0, 0, 0), nhead = make_int4(0, 0, 0, 0);
+            if (t0 < t1) {
+                next = __ldg(&P.taskC[t0]);
+                if constexpr (HEAD) nhead = __ldg(&P.headC[t0]);
+            }
             for (int t = t0; t < t1; ++t) {
-                const int4 task = next;
-                if (t + 1 < t1) next = __ldg(&P.taskC[t + 1]);
+                const int4 task = next, hd = nhead;
+                if (t + 1 < t1) {
+                    next = __ldg(&P.taskC[t + 1]);
+                    if constexpr (HEAD) nhead = __ldg(&P.headC[t + 1]);
+                }
+                const int np = HEAD ? min(task.w - task.z, 2) : 0;  // pairs taken from the head
                 const B2 yr = y[((size_t)task.x << lg) + s];
+                const B4 d = fac[((size_t)task.y << lg) + s];
                 real r0 = yr.x, r1 = yr.y;
-                int p = task.z;
+                if (np > 0) {
+                    const B4 u0 = fac[((size_t)hd.x << lg) + s];
+                    const B2 y0 = y[((size_t)hd.y << lg) + s];
+                    B4 u1 = z4<B4>();
+                    B2 y1 = {};
+                    if (np > 1) {
+                        u1 = fac[((size_t)hd.z << lg) + s];
+                        y1 = y[((size_t)hd.w << lg) + s];
+                    }
+                    r0 -= u0.x * y0.x + u0.y * y0.y;
+                    r1 -= u0.z * y0.x + u0.w * y0.y;
+                    if (np > 1) {
+                        r0 -= u1.x * y1.x + u1.y * y1.y;
+                        r1 -= u1.z * y1.x + u1.w * y1.y;
+                    }
+                }
+                int p = task.z + np;
                 for (; p + 1 < task.w; p += 2) {
                     const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
                     const B4 u0 = fac[((size_t)q0.x << lg) + s], u1 = fac[((size_t)q1.x << lg) + s];
@@ -447,7 +523,6 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     r0 -= u0.x * y0.x + u0.y * y0.y;
                     r1 -= u0.z * y0.x + u0.w * y0.y;
                 }
-                const B4 d = fac[((size_t)task.y << lg) + s];
                 B2 o;
                 o.x = d.x * r0 + d.y * r1;
                 o.y = d.z * r0 + d.w * r1;
@@ -530,7 +605,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     double4_32a* const Vb1 = reinterpret_cast<double4_32a*>(region + off.Vt);
     double2* Et = reinterpret_cast<double2*>(region + off.Et);
     double* Ei = reinterpret_cast<double*>(region + off.Ei);
-    float4* V32 = reinterpret_cast<float4*>(region + off.V32);
+    float* iv32 = reinterpret_cast<float*>(region + off.iv32);
     uint8_t* spin = reinterpret_cast<uint8_t*>(region + off.pin);
     __syncthreads();
     const DevPlan& P = s_plan;
@@ -662,7 +737,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 Vb1[idx] = t0;
                 Et[idx] = make_double2(t1.x, t1.y);
                 Ei[idx] = t1.z;
-                V32[idx] = make_float4(d2f_fast(t1.x), d2f_fast(t1.y), d2f_fast(t1.z), 0.f);
+                iv32[idx] = d2f_fast(t1.z);
             } else {
                 const double2 v0 = Bt.V0[(size_t)bus * Bt.sV0 + c];
                 if (Bt.check_v0 && (!finite_d(v0.x) || !finite_d(v0.y))) {
@@ -687,7 +762,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
                 Et[idx] = make_double2(e, f);
                 Ei[idx] = iv;
-                V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), d2f_fast(iv), 0.f);
+                iv32[idx] = d2f_fast(iv);
             }
             uint8_t pinned = Bt.pin ? Bt.pin[(size_t)bus * Bt.spin + c] : (uint8_t)0;
             if (Bt.ref_bus) {
@@ -719,7 +794,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     const double e = v.x * v.z, f = v.x * v.w;
                     Et[idx] = make_double2(e, f);
                     Ei[idx] = iv;
-                    V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), d2f_fast(iv), 0.f);
+                    iv32[idx] = d2f_fast(iv);
                 }
             }
             spin[idx] = pinned;
@@ -766,7 +841,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 const int bus = idx >> lg;
                 const int row = P.row_of_bus[bus];
                 if (row < 0) continue;
-                EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
+                EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
                 eval_row<1>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0), fac64, R,
                             false);
             }
@@ -831,17 +906,15 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             Vt[idx] = make_double4_32a(vm, va, cs, sn);
             const double e = vm * cs, f = vm * sn;
             Et[idx] = make_double2(e, f);
-            float ivf;
-            if (!pq) {
-                ivf = V32[idx].z;  // magnitude fixed: 1/Vm unchanged since the case was loaded
-            } else if (!Bt.mixed || s_vote[s] != 1) {  // the next Jacobian is double
-                const double iv = recip_nr(vm);
-                Ei[idx] = iv;
-                ivf = d2f_fast(iv);
-            } else {
-                ivf = __frcp_rn(d2f_fast(vm));
+            if (pq) {  // PV buses keep the magnitude they were loaded with (and never read iv32)
+                if (!Bt.mixed || s_vote[s] != 1) {  // the next Jacobian is double
+                    const double iv = recip_nr(vm);
+                    Ei[idx] = iv;
+                    iv32[idx] = d2f_fast(iv);
+                } else {
+                    iv32[idx] = __frcp_rn(d2f_fast(vm));
+                }
             }
-            V32[idx] = make_float4(d2f_fast(e), d2f_fast(f), ivf, 0.f);
         }
         if (tid < G) {
             const int st = s_st[tid];
@@ -862,7 +935,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
             const bool pinned = spin[idx] != 0;
             const bool pq = P.bus_pq[bus] != 0;
-            EvalCtx ec{&P, Et, Ei, V32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
+            EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;
             if (st == SL_BACKTRACK)
                 worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
@@ -1011,15 +1084,16 @@ __global__ void v0_table_kernel(const double2* V0, int n, int check, double4_32a
 }
 
 // Conversion helpers applied elementwise (tests compare them with IEEE casts).
-__global__ void conversions_kernel(const double* in, int n, float* d2f, double* f2d) {
+__global__ void conversions_kernel(const double* in, int n, float* d2f, double* f2d, float* d2f_small) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         d2f[i] = d2f_fast(in[i]);
         f2d[i] = f2d_fast(d2f[i]);
+        d2f_small[i] = d2f_trunc(in[i]);
     }
 }
 
-cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d) {
-    conversions_kernel<<<(n + 255) / 256, 256>>>(in, n, d2f, f2d);
+cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small) {
+    conversions_kernel<<<(n + 255) / 256, 256>>>(in, n, d2f, f2d, d2f_small);
     return cudaGetLastError();
 }
 
@@ -1084,7 +1158,7 @@ cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_
 
 // Jacobian blocks and residual at one given voltage (G = 1): debug_J and tests.
 __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                                  double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                                  double4_32a* Vt, double2* Et, double* Ei, float* iv32, double4_32a* blocks,
                                   double2* R) {
     const int n = P.n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1094,13 +1168,13 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
         Vt[i] = make_double4_32a(vm, va, cs, sn);
         Et[i] = make_double2(vm * cs, vm * sn);
         Ei[i] = 1.0 / vm;
-        V32[i] = make_float4((float)(vm * cs), (float)(vm * sn), (float)(1.0 / vm), 0.f);
+        iv32[i] = (float)(1.0 / vm);
     }
     __syncthreads();  // single-CTA launch
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int row = P.row_of_bus[i];
         if (row < 0) continue;
-        EvalCtx ec{&P, Et, Ei, V32, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
+        EvalCtx ec{&P, Et, Ei, iv32, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
         eval_row<1>(ec, i, 0, row, pin && pin[i], P.bus_pq[i] != 0, Sbus[i], blocks, R, true);
     }
 }
@@ -1118,9 +1192,9 @@ cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t s
 }
 
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
-                              double4_32a* Vt, double2* Et, double* Ei, float4* V32, double4_32a* blocks,
+                              double4_32a* Vt, double2* Et, double* Ei, float* iv32, double4_32a* blocks,
                               double2* R, cudaStream_t stream) {
-    eval_debug_kernel<<<1, 256, 0, stream>>>(P, V, Sbus, pin, Vt, Et, Ei, V32, blocks, R);
+    eval_debug_kernel<<<1, 256, 0, stream>>>(P, V, Sbus, pin, Vt, Et, Ei, iv32, blocks, R);
     return cudaGetLastError();
 }
 

@@ -308,8 +308,10 @@ def test_integer_pipe_conversions_match_ieee():
     x = np.ascontiguousarray(x)
     d2f = np.empty(len(x), np.float32)
     f2d = np.empty(len(x), np.float64)
-    rc = _lib.load().gbpf_selftest_conversions(_lib.d(x), len(x), d2f.ctypes.data_as(C.POINTER(C.c_float)),
-                                               _lib.d(f2d))
+    small = np.empty(len(x), np.float32)
+    fp = C.POINTER(C.c_float)
+    rc = _lib.load().gbpf_selftest_conversions(_lib.d(x), len(x), d2f.ctypes.data_as(fp), _lib.d(f2d),
+                                               small.ctypes.data_as(fp))
     assert rc == 0, _lib.last_error()
     ref = x.astype(np.float32)
     normal = np.isfinite(ref) & (np.abs(ref) >= np.finfo(np.float32).tiny)
@@ -319,6 +321,9 @@ def test_integer_pipe_conversions_match_ieee():
     assert np.array_equal(f2d[normal], d2f[normal].astype(np.float64))  # exact widening
     assert np.isnan(d2f[-1]) and np.isinf(d2f[-3]) and d2f[-3] > 0 and np.isinf(d2f[-2]) and d2f[-2] < 0
     assert d2f[x == 0.0].tolist() == [0.0, 0.0]
+    # the float Jacobian's short conversion: the same bits wherever it is used (|x| < 2^128)
+    inr = np.isfinite(x) & (np.abs(x) < 2.0 ** 128)
+    assert np.array_equal(small[inr].view(np.uint32), d2f[inr].view(np.uint32))
 
 
 def test_n1_sweep_of_the_2000_bus_grid(grid2000):
