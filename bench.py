@@ -115,10 +115,11 @@ def n_lanes(T, cases_per_cta=32, threads_per_cta=512, nsm=None):
     return min(T, nsm * (1024 // threads_per_cta) * cases_per_cta)
 
 
-def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
-    """Bytes a case-iteration must move (the hot path's per-unit traffic model): eval (V state,
-    S, Jacobian write, residual), refactor (read A, write LU), solve (read LU and residual,
-    write step), step (read step, rewrite the state). Index arrays are shared by the batch
+def algorithmic_bytes(info: dict, g, mixed: bool):
+    """Bytes a case-iteration must move (the hot path's per-unit traffic model), split into the
+    part every iteration moves -- eval (V state, S, Jacobian write, residual), solve (read LU
+    and residual, write step), step (read step, rewrite the state) -- and the refactorization
+    (read A, write LU), which a chord step leaves out. Index arrays are shared by the batch
     and excluded. b = 8 (double path) or 4 (float Jacobian/LU in the mixed path)."""
     n = g.n
     m = len(g.pv) + 2 * len(g.pq)  # scalar unknowns
@@ -127,8 +128,15 @@ def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
     nnzJ = len(jacobian_pattern(g.Yp, g.Yj, g.pv, g.pq)[1])
     nnzLU = 4 * info["n_blocks"]
     b = 4 if mixed else 8
-    return (3 * n * 8 + 2 * n * 8 + b * nnzJ + 8 * m) + (b * nnzJ + b * nnzLU) + (b * nnzLU + 16 * m) + (
-        8 * m + 6 * n * 8)
+    per_iteration = (3 * n * 8 + 2 * n * 8 + b * nnzJ + 8 * m) + (b * nnzLU + 16 * m) + (8 * m + 6 * n * 8)
+    per_factorization = b * nnzJ + b * nnzLU
+    return per_iteration, per_factorization
+
+
+def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
+    """The model's bytes of a case-iteration that refactors."""
+    it, fac = algorithmic_bytes(info, g, mixed)
+    return it + fac
 
 
 class Clocks:
@@ -443,7 +451,10 @@ def gpu_line(args, res, rank, world):
     hbm = peaks.get("hbm_gbs")
     its_mixed = int(mixed["it"].sum())
     B = algorithmic_bytes_per_iteration(info, g, True)
-    achieved = B * its_mixed / (mixed["ms"] * 1e-3) / 1e9
+    B_it, B_fac = algorithmic_bytes(info, g, True)
+    n_fac = int(mixed["stats"]["single_factorizations"] + mixed["stats"]["double_factorizations"])
+    launch_bytes = B_it * its_mixed + B_fac * n_fac  # chord steps leave the refactorization out
+    achieved = launch_bytes / (mixed["ms"] * 1e-3) / 1e9
     traffic = load_traffic()
     tr = traffic.get("mixed_bytes_per_case_iteration")
     roof = {
@@ -458,7 +469,10 @@ def gpu_line(args, res, rank, world):
         "peak_source": "measured" if hbm else "fallback",
         "kernel": "newton_kernel",
         "algorithmic_bytes_per_case_iteration": B,
+        "algorithmic_bytes_per_launch": launch_bytes,
         "case_iterations_per_launch": its_mixed,
+        "factorizations_per_launch": n_fac,
+        "chord_steps_per_launch": int(mixed["stats"].get("chord_steps", 0)),
     }
     # fp64 pipe roofline of the double path (GB300: ~1.2 TFLOP/s)
     fp64 = {

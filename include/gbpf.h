@@ -41,6 +41,10 @@ typedef struct gbpf_params {
                             voltage error left (1e-8 p.u.; 0: no bound) -- though not below twice
                             the double mismatch's rounding floor -- so its voltage is as accurate
                             as a double solve's on ill-conditioned grids too */
+    double chord_tol;    /* vote_rule 1: once an accepted float step leaves the mismatch below this
+                            (1e-8 p.u.: the polish steps), the next step reuses the float factors it
+                            was solved with (a chord step: substitutions only, no factorization) for
+                            as long as each such step cuts the mismatch tenfold; 0: always refactor */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -60,6 +64,7 @@ typedef struct gbpf_stats {
     double kernel_ms; /* device time of the Newton kernel, CUDA events on the solver's stream */
     double call_ms;   /* device time of the last host-pointer call: first copy in to last copy out */
     int threads_per_cta; /* CTA shape of the last launch (with cases_per_cta) */
+    unsigned long long chord_steps; /* steps solved with the previous float factors (chord_tol) */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);

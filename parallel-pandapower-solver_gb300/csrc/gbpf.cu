@@ -89,6 +89,7 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
     const unsigned long long g = (unsigned long long)G;
     o.fac64 = take((unsigned long long)nblk * g * 32);
     o.fac32 = mixed ? take((unsigned long long)nblk * g * 16) : ~0ULL;
+    o.fac32b = mixed ? take((unsigned long long)nblk * g * 16) : ~0ULL;
     o.R = take((unsigned long long)nv * g * 16);
     o.y64 = take((unsigned long long)nv * g * 16);
     o.y32 = mixed ? take((unsigned long long)nv * g * 8) : ~0ULL;
@@ -106,10 +107,11 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
 // and the factorization schedule dealt to its NT / G workers (built on first use).
 struct Shape {
     int NT = 0, G = 0, lg = 0, occ = 1;
-    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dheadA, dheadC;
+    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dheadA, dheadC, dtaskF, dheadF, dptrF;
     gbpf::DevPlan dp{};
     ~Shape() {
-        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC, &dheadA, &dheadC}) b->release();
+        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC, &dheadA, &dheadC, &dtaskF, &dheadF, &dptrF})
+            b->release();
     }
 };
 
@@ -259,12 +261,14 @@ int setup(gbpf_solver* s, int cases_per_cta, int threads_per_cta) {
     return 0;
 }
 
-// CTAs of a launch that needs `want` of them: at most the resident ones; when more than one
-// per SM is needed, a whole number per SM, so that every SM gets the same share of the cases
-// (the case slots of the extra CTAs are filled by the work counter as cases free up).
-int grid_size(int nsm, int occ, long long want) {
+// CTAs of a launch that needs `want` of them: at most the resident ones. Mixed-precision
+// launches (latency-bound factorizations: a CTA's pass costs about the same however many of
+// its slots are busy) take a whole number per SM when more than one per SM is needed, so
+// that every SM gets the same share of the cases; double launches keep their slots full
+// instead (the FP64 pipe is their bound, and a warp of half-empty slots still occupies it).
+int grid_size(int nsm, int occ, long long want, bool balance) {
     const long long resident = (long long)nsm * std::max(1, occ);
-    if (want > nsm) want = (want + nsm - 1) / nsm * nsm;
+    if (balance && want > nsm) want = (want + nsm - 1) / nsm * nsm;
     return (int)std::max<long long>(1, std::min(want, resident));
 }
 
@@ -346,6 +350,20 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     };
     CK(upload(sh->dheadA, head_pairs(sc.taskA)));
     CK(upload(sh->dheadC, head_pairs(sc.taskC)));
+    // substitution-only lists for chord passes: every worker's forward tasks of each level,
+    // the ones it runs inside the full factor-level lists
+    std::vector<int> taskF, ptrF((size_t)p.nlev * sc.W + 1, 0);
+    for (size_t q = 0; q + 1 < sc.ptrA.size(); ++q) {
+        ptrF[q] = (int)(taskF.size() / 4);
+        for (int t = sc.ptrA[q]; t < sc.ptrA[q + 1]; ++t)
+            if ((sc.taskA[4 * (size_t)t + 1] & 3) == gbpf::TK_FWD)
+                for (int k = 0; k < 4; ++k) taskF.push_back(sc.taskA[4 * (size_t)t + k]);
+    }
+    ptrF.back() = (int)(taskF.size() / 4);
+    if (taskF.empty()) taskF.assign(4, 0);  // keeps the upload non-empty for a grid without forward tasks
+    CK(upload(sh->dheadF, head_pairs(taskF)));
+    CK(upload(sh->dtaskF, taskF));
+    CK(upload(sh->dptrF, ptrF));
     CK(upload(sh->dtaskA, sc.taskA));
     CK(upload(sh->dptrA, sc.ptrA));
     CK(upload(sh->dscl, sc.scl));
@@ -362,6 +380,9 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     sh->dp.ptrC = sh->dptrC.as<int>();
     sh->dp.headA = sh->dheadA.as<int4>();
     sh->dp.headC = sh->dheadC.as<int4>();
+    sh->dp.taskF = sh->dtaskF.as<int4>();
+    sh->dp.headF = sh->dheadF.as<int4>();
+    sh->dp.ptrF = sh->dptrF.as<int>();
     *out = sh.get();
     s->shapes.push_back(std::move(sh));
     return 0;
@@ -403,6 +424,9 @@ int upload_plan(gbpf_solver* s) {
     d.ptrC = nullptr;
     d.headA = nullptr;
     d.headC = nullptr;
+    d.taskF = nullptr;
+    d.headF = nullptr;
+    d.ptrF = nullptr;
     d.pairs = s->dpairs.as<int2>();
     d.row_pq = s->drow_pq.as<uint8_t>();
     d.bus_of_row = s->dbus_of_row.as<int>();
@@ -427,6 +451,7 @@ gbpf_params default_params() {
     p.vote_rule = 1;
     p.polish = 1e-3;
     p.vtol = 1e-8;
+    p.chord_tol = 1e-8;
     return p;
 }
 
@@ -453,7 +478,7 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     choose_shape(s, units, &NT, &G);
     Shape* sh = nullptr;
     if (int rc = get_shape(s, NT, G, &sh)) return rc;
-    const int grid = grid_size(s->nsm, sh->occ, (units + G - 1) / G);
+    const int grid = grid_size(s->nsm, sh->occ, (units + G - 1) / G, b.mixed != 0);
     gbpf::Job job{};
     job.P = sh->dp;
     job.off = solver_offsets(s, G, b.mixed != 0);
@@ -500,6 +525,7 @@ int finish_launch(const LaunchRes& R, int grid, int G, int NT, const char* who, 
     st->single_rejected = host_ctl[2];
     st->double_rejected = host_ctl[3];
     st->macro_steps = host_ctl[4];
+    st->chord_steps = host_ctl[5];
     st->grid = grid;
     st->cases_per_cta = G;
     st->threads_per_cta = NT;
@@ -552,6 +578,9 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
         const double floor_ = 2.0 * DBL_EPSILON * s->plan.y_rowsum;
         b.tol_polish = std::min(b.tol_polish, std::max(p.vtol / k, floor_));
     }
+    // chord steps belong to the GB300 rule's float cases only (the double path refactors every
+    // step like nr_klu)
+    b.chord_tol = b.mixed && b.vote_rule == 1 && p.chord_tol > 0.0 ? p.chord_tol : 0.0;
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
@@ -731,7 +760,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         b.err = reinterpret_cast<int*>(c + 24);
         o.B = b;
     }
-    const int grid = grid_size(g->nsm, occ, want);
+    const int grid = grid_size(g->nsm, occ, want, mixed);
     CK(g->scr.ensure((size_t)grid * cta_bytes));
     CK(g->bjobs.ensure((size_t)nj * sizeof(gbpf::Job)));
     CK(cudaMemcpyAsync(g->bjobs.p, hj.data(), (size_t)nj * sizeof(gbpf::Job), cudaMemcpyHostToDevice, g->stream));
@@ -770,6 +799,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         st.single_rejected += c[2];
         st.double_rejected += c[3];
         st.macro_steps += c[4];
+        st.chord_steps += c[5];
     }
     st.grid = grid;
     st.cases_per_cta = Gmax;

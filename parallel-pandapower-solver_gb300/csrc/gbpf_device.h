@@ -49,6 +49,9 @@ struct DevPlan {
     const int* ptrC;
     const int4* headA;       // per taskA entry: its first two pairs inline (x0, y0, x1, y1; -1 = none)
     const int4* headC;       // per taskC entry: likewise
+    const int4* taskF;       // chord passes: the forward tasks of taskA, same levels and workers
+    const int4* headF;
+    const int* ptrF;         // nlev*W + 1
     const int2* pairs;
     const uint8_t* row_pq;   // block row is PQ (two real pivots)
     const int* bus_of_row;
@@ -97,10 +100,12 @@ struct Batch {
     double mixed_switch;
     int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
     double tol_polish;       // GB300 rule: float-factor cases iterate until mismatch < tol_polish
+    double chord_tol;        // GB300 rule: below this mismatch a step reuses the last float factors (0: never)
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch
     unsigned long long* stats;  // [0] fp32 factorizations [1] fp64 [2] fp32 rejected [3] fp64 rejected [4] macro steps
+                                // [5] chord steps
     int* err;                // [0] code [1] bus [2] case
 };
 
@@ -108,7 +113,9 @@ struct Batch {
 // every array is [item][slot]); ~0 for an array the job does not use.
 struct ScratchOffsets {
     unsigned long long fac64;  // [blk][slot] double 2x2 blocks (a00 a01 a10 a11)
-    unsigned long long fac32;  // [blk][slot] float blocks (mixed precision)
+    unsigned long long fac32;  // [blk][slot] float blocks (mixed precision): buffer 0 ...
+    unsigned long long fac32b; // ... and 1 -- a slot's last float factors stay in one while the
+                               // next Jacobian is written to the other
     unsigned long long R;      // [row][slot] residual (P, Q) = S - S(V)
     unsigned long long y64;    // [row][slot] step
     unsigned long long y32;

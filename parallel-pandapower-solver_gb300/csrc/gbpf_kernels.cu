@@ -30,6 +30,7 @@ namespace gbpf {
 
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
+constexpr double CHORD_RATE = 0.1; // a chord step must cut the mismatch tenfold for another one
 constexpr double BIG = DBL_MAX;    // nr_klu.cpp:434 NONFINITE_NORM
 
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
@@ -333,10 +334,13 @@ __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
 // One batched factorization + substitution pass over the slots flagged in `on` (G <= 32).
 // Worker w = (warp, lane / G) runs its task list of every level for its G slot lanes;
 // the CTA meets at a barrier after each level, forward and backward. Pivot statistics per
-// slot go to smin / smax (as ordered bits).
+// slot go to smin / smax (as ordered bits). Slots flagged in `chord` keep the factors already
+// in `fac` and run the substitutions only; when every slot of the CTA does (factor_any false),
+// the workers walk the substitution-only lists instead of skipping factor tasks one by one.
 template <typename real>
 __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
-                        const int* on, int lg, unsigned long long* smin, unsigned long long* smax) {
+                        const int* on, int lg, unsigned long long* smin, unsigned long long* smax,
+                        const int* chord, bool factor_any) {
     using B4 = typename V4<real>::t;
     using B2 = typename V4<real>::t2;
     const int tid = threadIdx.x;
@@ -345,6 +349,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     const int w = (tid >> 5) * (32 >> lg) + (lane >> lg);
     const int W = P.W;
     const bool act = on[s] != 0;
+    const bool factor = !(chord && chord[s]);
     // float passes take each task's first two pairs from its head record (the double pass
     // keeps its registers for the wider blocks)
     constexpr bool HEAD = sizeof(real) == 4;
@@ -352,22 +357,26 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
     B4 dinv = z4<B4>();  // the worker's last inverse diagonal block: scales the L column after it
     for (int h = 0; h < P.nlev; ++h) {
         if (act) {
-            const int t0 = __ldg(&P.ptrA[h * W + w]), t1 = __ldg(&P.ptrA[h * W + w + 1]);
+            const int* const PA = factor_any ? P.ptrA : P.ptrF;
+            const int4* const TA = factor_any ? P.taskA : P.taskF;
+            const int4* const HA = factor_any ? P.headA : P.headF;
+            const int t0 = __ldg(&PA[h * W + w]), t1 = __ldg(&PA[h * W + w + 1]);
             // the next task's record and first two pairs are fetched while the current one
             // runs, so a task's block loads all go out at once when it starts
             int4 next = make_int4(0, 0, 0, 0), nhead = make_int4(0, 0, 0, 0);
             if (t0 < t1) {
-                next = __ldg(&P.taskA[t0]);
-                if constexpr (HEAD) nhead = __ldg(&P.headA[t0]);
+                next = __ldg(&TA[t0]);
+                if constexpr (HEAD) nhead = __ldg(&HA[t0]);
             }
             for (int t = t0; t < t1; ++t) {
                 const int4 task = next, hd = nhead;
                 if (t + 1 < t1) {
-                    next = __ldg(&P.taskA[t + 1]);
-                    if constexpr (HEAD) nhead = __ldg(&P.headA[t + 1]);
+                    next = __ldg(&TA[t + 1]);
+                    if constexpr (HEAD) nhead = __ldg(&HA[t + 1]);
                 }
                 const int kind = task.y & 3;
                 const int np = HEAD ? min(task.w - task.z, 2) : 0;  // pairs taken from the head
+                if (kind != 3 && !factor) continue;
                 if (kind == 3) {  // forward substitution of block row task.x
                     const double2 r = R[((size_t)task.x << lg) + s];
                     real y0, y1;
@@ -595,6 +604,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     const int G = L.jobs[job].G, lg = L.jobs[job].log2G;  // case slots of this job's CTAs
     double4_32a* fac64 = reinterpret_cast<double4_32a*>(region + off.fac64);
     float4* fac32 = off.fac32 != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32) : nullptr;
+    float4* fac32b = off.fac32b != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32b) : nullptr;
     double2* R = reinterpret_cast<double2*>(region + off.R);
     double2* y64 = reinterpret_cast<double2*>(region + off.y64);
     float2* y32 = off.y32 != ~0ULL ? reinterpret_cast<float2*>(region + off.y32) : nullptr;
@@ -621,6 +631,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ unsigned long long s_res[MAX_SLOTS], s_pmin[MAX_SLOTS], s_pmax[MAX_SLOTS];
     __shared__ int s_nst[MAX_SLOTS];
     __shared__ int s_tb[MAX_SLOTS];
+    __shared__ int s_fb[MAX_SLOTS], s_chord[MAX_SLOTS];  // float factor buffer; next step is a chord step
     __shared__ int s_stk[MAX_SLOTS][MAX_STAMPS];
     __shared__ double2 s_stv[MAX_SLOTS][MAX_STAMPS];
 
@@ -666,6 +677,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     s_case[s] = (int)c;
                     s_st[s] = SL_FRESH;
                     if (!s_warm[s]) s_tb[s] = 0;
+                    s_fb[s] = 0;
+                    s_chord[s] = 0;
                     s_it[s] = 0;
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
@@ -813,16 +826,31 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         const int any32 = __syncthreads_or(tid < G && s_on32[tid]);
         if (any32) {
-            lu_pass<float>(P, fac32, R, y32, s_on32, lg, s_pmin, s_pmax);
+            // chord steps are decided per slot (a result never depends on the other cases of
+            // its CTA); the factorization is left out altogether when every float slot takes one
+            const int all_chord = __syncthreads_and(!(tid < G && s_on32[tid]) || s_chord[tid]);
+            {
+                // a slot factors the Jacobian in the buffer its last factors are not in; a chord
+                // step solves with those factors
+                const int sl = (tid & 31) & (G - 1);
+                const int buf = s_chord[sl] ? s_fb[sl] : 1 - s_fb[sl];
+                lu_pass<float>(P, buf ? fac32b : fac32, R, y32, s_on32, lg, s_pmin, s_pmax, s_chord, !all_chord);
+            }
             if (tid < G && s_on32[tid]) {
                 const int s = tid;
-                atomicAdd(&Bt.stats[0], 1ULL);
-                if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min32)) {
-                    atomicAdd(&Bt.stats[2], 1ULL);
-                    s_vote[s] = -1;
-                    s_on32[s] = 0;
-                    s_on64[s] = 1;
-                    s_reeval[s] = 1;
+                if (s_chord[s]) {
+                    atomicAdd(&Bt.stats[5], 1ULL);
+                } else {
+                    atomicAdd(&Bt.stats[0], 1ULL);
+                    if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min32)) {
+                        atomicAdd(&Bt.stats[2], 1ULL);
+                        s_vote[s] = -1;
+                        s_on32[s] = 0;
+                        s_on64[s] = 1;
+                        s_reeval[s] = 1;
+                    } else {
+                        s_fb[s] ^= 1;  // the factors now live in the buffer the Jacobian was in
+                    }
                 }
                 s_pmin[s] = ~0ULL;
                 s_pmax[s] = 0ULL;
@@ -850,7 +878,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         const int any64 = __syncthreads_or(tid < G && s_on64[tid]);
         if (any64) {
-            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax);
+            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true);
             if (tid < G && s_on64[tid]) {
                 const int s = tid;
                 atomicAdd(&Bt.stats[1], 1ULL);
@@ -939,8 +967,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             unsigned long long worst;
             if (st == SL_BACKTRACK)
                 worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
-            else if (Bt.mixed && s_jprec[s])
-                worst = eval_row<2>(ec, bus, s, row, pinned, pq, Ssp, fac32, R, true);
+            else if (Bt.mixed && s_jprec[s])  // into the buffer the slot's last float factors are not in
+                worst = eval_row<2>(ec, bus, s, row, pinned, pq, Ssp, s_fb[s] ? fac32 : fac32b, R, true);
             else
                 worst = eval_row<1>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
             atomicMax(&s_res[s], worst);
@@ -968,10 +996,14 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 top = true;
             } else if (st == SL_ACTIVE) {
                 const double old = s_nrm[s];
+                const bool was_chord = s_chord[s] != 0;
+                s_chord[s] = 0;
                 if (!Bt.line_search || nw <= (1.0 - ARMIJO_C) * old) {
                     if (Bt.mixed && s_vote[s] >= 0) {
                         if (Bt.vote_rule == 1) {
-                            if (s_vote[s] == 1 && !(nw <= 0.5 * old) && old < Bt.mixed_switch) s_vote[s] = -1;
+                            // (a chord step that contracts poorly only means: refactor next)
+                            if (!was_chord && s_vote[s] == 1 && !(nw <= 0.5 * old) && old < Bt.mixed_switch)
+                                s_vote[s] = -1;
                         } else if (s_vote[s] == 1 && !(nw <= 0.5 * old)) {
                             s_vote[s] = -1;
                         } else {
@@ -980,6 +1012,13 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     }
                     s_nrm[s] = nw;
                     top = true;
+                    // chord: near the solution the float factors of the last step are as good
+                    // as fresh ones (a fresh float factorization is itself off by ~cond(J) 2^-24),
+                    // so the next step reuses them while the mismatch is below chord_tol and each
+                    // chord step cuts it at least CHORD_RATE-fold
+                    if (Bt.chord_tol > 0.0 && s_vote[s] == 1 && s_yprec[s] == 1 && nw < Bt.chord_tol &&
+                        (!was_chord || nw <= CHORD_RATE * old))
+                        s_chord[s] = 1;
                 } else {
                     s_balpha[s] = 1.0;
                     s_bnrm[s] = nw;
@@ -1139,7 +1178,7 @@ __global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const doubl
         R[row] = make_double2(rhs, 0.0);
     }
     __syncthreads();
-    lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max);
+    lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max, nullptr, true);
     for (int i = tid; i < P.n; i += NTB) {
         const int row = P.row_of_bus[i];
         theta[i] = row < 0 ? theta_bus[i] : y[row].x;

@@ -35,6 +35,7 @@ class Params(C.Structure):
         ("vote_rule", C.c_int),
         ("polish", C.c_double),
         ("vtol", C.c_double),
+        ("chord_tol", C.c_double),
     ]
 
 
@@ -69,6 +70,7 @@ class Stats(C.Structure):
         ("kernel_ms", C.c_double),
         ("call_ms", C.c_double),
         ("threads_per_cta", C.c_int),
+        ("chord_steps", C.c_ulonglong),
     ]
 
 
