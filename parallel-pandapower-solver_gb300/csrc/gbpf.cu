@@ -87,9 +87,11 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
         return p;
     };
     const unsigned long long g = (unsigned long long)G;
-    o.fac64 = take((unsigned long long)nblk * g * 32);
-    o.fac32 = mixed ? take((unsigned long long)nblk * g * 16) : ~0ULL;
-    o.fac32b = mixed ? take((unsigned long long)nblk * g * 16) : ~0ULL;
+    // factor blocks, then the nv inverse diagonals
+    const unsigned long long nf = (unsigned long long)nblk + nv;
+    o.fac64 = take(nf * g * 32);
+    o.fac32 = mixed ? take(nf * g * 16) : ~0ULL;
+    o.fac32b = mixed ? take(nf * g * 16) : ~0ULL;
     o.R = take((unsigned long long)nv * g * 16);
     o.y64 = take((unsigned long long)nv * g * 16);
     o.y32 = mixed ? take((unsigned long long)nv * g * 8) : ~0ULL;
@@ -205,7 +207,7 @@ int compute_rcond0(gbpf_solver* s) {
         for (int k = s->Yp[r]; k < s->Yp[r + 1]; ++k) a += std::hypot(s->Yx[2 * (size_t)k], s->Yx[2 * (size_t)k + 1]);
         p.y_rowsum = std::max(p.y_rowsum, a);
     }
-    std::vector<double> Vm(s->n, 1.0), Va(s->n, 0.0), S(2 * (size_t)s->n, 0.0), blk(4 * (size_t)p.nblk),
+    std::vector<double> Vm(s->n, 1.0), Va(s->n, 0.0), S(2 * (size_t)s->n, 0.0), blk(4 * ((size_t)p.nblk + p.nv)),
         R(2 * (size_t)std::max(p.nv, 1));
     gbpf::host_eval(p, s->Yp.data(), s->Yj.data(), s->Yx.data(), Vm.data(), Va.data(), S.data(), nullptr, blk.data(),
                     R.data());
@@ -328,8 +330,7 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     // DIAG tasks carry the "two real pivots" flag (PQ row) in bit 5 of their code
     for (size_t t = 0; t < sc.taskA.size() / 4; ++t) {
         if ((sc.taskA[4 * t + 1] & 3) == gbpf::TK_DIAG) {
-            const int dst = sc.taskA[4 * t];
-            const int row = (int)(std::upper_bound(p.base.begin(), p.base.end(), dst) - p.base.begin()) - 1;
+            const int row = sc.taskA[4 * t + 1] >> gbpf::TASK_ROW_SHIFT;
             if (p.row_pq[row]) sc.taskA[4 * t + 1] |= 32;
         }
     }
@@ -1216,7 +1217,7 @@ int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* 
     } guard{cleanup};
     CK(dP.ensure(n * 8));
     CK(dth.ensure(n * 8));
-    CK(dfac.ensure(nb * 32));
+    CK(dfac.ensure((nb + nv) * 32));
     CK(dR.ensure(nv * 16));
     CK(dy.ensure(nv * 16));
     CK(dout.ensure(n * 8));

@@ -340,7 +340,7 @@ __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
 template <typename real>
 __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
                         const int* on, int lg, unsigned long long* smin, unsigned long long* smax,
-                        const int* chord, bool factor_any) {
+                        const int* chord, bool factor_any, typename V4<real>::t* dinv_smem) {
     using B4 = typename V4<real>::t;
     using B2 = typename V4<real>::t2;
     const int tid = threadIdx.x;
@@ -449,30 +449,35 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     const int2 q0 = __ldg(&P.pairs[p]);
                     mm_sub(acc, fac[((size_t)q0.x << lg) + s], fac[((size_t)q0.y << lg) + s]);
                 }
-                if (kind == 0) {  // pivots of the 2x2 diagonal block: a00 and det / a00
+                if (kind == 0) {  // diagonal block: its inverse, kept for the L blocks that follow
                     const real det = acc.x * acc.w - acc.y * acc.z;
-                    const real u0 = fabs(acc.x);
-                    pmin = fmin(pmin, u0);
-                    pmax = (u0 > pmax || u0 != u0) ? u0 : pmax;
-                    if (task.y & 32) {
-                        const real u1 = fabs(det / acc.x);
-                        pmin = fmin(pmin, u1);
-                        pmax = (u1 > pmax || u1 != u1) ? u1 : pmax;
-                    }
                     const real inv = (real)1 / det;
-                    B4 o;
-                    o.x = acc.w * inv;
-                    o.y = -acc.y * inv;
-                    o.z = -acc.z * inv;
-                    o.w = acc.x * inv;
-                    fac[((size_t)task.x << lg) + s] = o;
-                    dinv = o;
+                    dinv.x = acc.w * inv;
+                    dinv.y = -acc.y * inv;
+                    dinv.z = -acc.z * inv;
+                    dinv.w = acc.x * inv;
+                    if (dinv_smem) dinv_smem[tid] = dinv;
+                    // a chain segment's copy (TASK_NOSTORE) only recomputes it; the task itself
+                    // records the pivots (a00 and det / a00) and stores the inverse apart, at
+                    // block nblk + row (the Jacobian's diagonal stays for the copies)
+                    if (!(task.y & 64)) {
+                        const real u0 = fabs(acc.x);
+                        pmin = fmin(pmin, u0);
+                        pmax = (u0 > pmax || u0 != u0) ? u0 : pmax;
+                        if (task.y & 32) {
+                            const real u1 = fabs(det / acc.x);
+                            pmin = fmin(pmin, u1);
+                            pmax = (u1 > pmax || u1 != u1) ? u1 : pmax;
+                        }
+                        fac[((size_t)(P.nblk + (task.y >> 8)) << lg) + s] = dinv;
+                    }
                 } else if (task.y & 8) {  // L block: scaled by its column's inverse diagonal
                     B4 o;
-                    o.x = acc.x * dinv.x + acc.y * dinv.z;
-                    o.y = acc.x * dinv.y + acc.y * dinv.w;
-                    o.z = acc.z * dinv.x + acc.w * dinv.z;
-                    o.w = acc.z * dinv.y + acc.w * dinv.w;
+                    const B4 dv = dinv_smem ? dinv_smem[tid] : dinv;
+                    o.x = acc.x * dv.x + acc.y * dv.z;
+                    o.y = acc.x * dv.y + acc.y * dv.w;
+                    o.z = acc.z * dv.x + acc.w * dv.z;
+                    o.w = acc.z * dv.y + acc.w * dv.w;
                     fac[((size_t)task.x << lg) + s] = o;
                 } else {
                     fac[((size_t)task.x << lg) + s] = acc;
@@ -572,6 +577,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     char* const region = L.scratch + (size_t)blockIdx.x * L.cta_bytes;
     __shared__ DevPlan s_plan;
     __shared__ Batch s_batch;
+    __shared__ double4_32a s_dinv64[NTB];  // double passes: each worker's inverse diagonal (off the registers)
     __shared__ int s_job;
     int next_job = 0;  // thread 0: first job this CTA has not finished yet
     for (;;) {
@@ -834,7 +840,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 // step solves with those factors
                 const int sl = (tid & 31) & (G - 1);
                 const int buf = s_chord[sl] ? s_fb[sl] : 1 - s_fb[sl];
-                lu_pass<float>(P, buf ? fac32b : fac32, R, y32, s_on32, lg, s_pmin, s_pmax, s_chord, !all_chord);
+                lu_pass<float>(P, buf ? fac32b : fac32, R, y32, s_on32, lg, s_pmin, s_pmax, s_chord, !all_chord, nullptr);
             }
             if (tid < G && s_on32[tid]) {
                 const int s = tid;
@@ -878,7 +884,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         const int any64 = __syncthreads_or(tid < G && s_on64[tid]);
         if (any64) {
-            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true);
+            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true, s_dinv64);
             if (tid < G && s_on64[tid]) {
                 const int s = tid;
                 atomicAdd(&Bt.stats[1], 1ULL);
@@ -1178,7 +1184,7 @@ __global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const doubl
         R[row] = make_double2(rhs, 0.0);
     }
     __syncthreads();
-    lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max, nullptr, true);
+    lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max, nullptr, true, nullptr);
     for (int i = tid; i < P.n; i += NTB) {
         const int row = P.row_of_bus[i];
         theta[i] = row < 0 ? theta_bus[i] : y[row].x;

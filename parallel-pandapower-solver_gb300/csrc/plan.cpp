@@ -76,7 +76,12 @@ int deal(const std::vector<long long>& weight, int W, std::vector<int>& who) {
 
 using Task = PlanTask;
 
-// Lay tasks out grouped by (level, worker); `rec` ints per record.
+// Lay tasks out grouped by (level, worker); `four`: 4 ints per record (else 2). Chains
+// (a diagonal and its L column) go to one worker; a chain heavier than its level's share of a
+// worker (total weight / W) is cut into segments of at most that share (at least one L block
+// each), every segment after the first led by a copy of the diagonal task flagged
+// TASK_NOSTORE (it recomputes the inverse from the Jacobian's diagonal, which the pass
+// leaves in place). Units are dealt longest-first onto the least-loaded worker.
 void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& out, std::vector<int>& ptr,
             std::vector<int>* level_work, bool four) {
     std::vector<std::vector<int>> by_level(nlev);
@@ -86,28 +91,57 @@ void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& o
     out.clear();
     std::vector<long long> wts;
     std::vector<int> who;
+    std::vector<std::vector<int>> units;  // task indices; ~i = a recomputing copy of diagonal task i
+    auto emit = [&](int q) {
+        const Task& t = tasks[q < 0 ? ~q : q];
+        out.push_back(t.dst);
+        out.push_back(q < 0 ? (t.code | TASK_NOSTORE) : t.code);
+        if (four) {
+            out.push_back(t.p0);
+            out.push_back(t.p1);
+        }
+    };
     for (int h = 0; h < nlev; ++h) {
-        auto& ids = by_level[h];
-        wts.resize(ids.size());
-        for (size_t i = 0; i < ids.size(); ++i) {
-            wts[i] = 0;
-            for (int q = ids[i]; q >= 0; q = tasks[q].next) wts[i] += tasks[q].w;
+        const auto& ids = by_level[h];
+        long long total = 0;
+        for (int id : ids)
+            for (int q = id; q >= 0; q = tasks[q].next) total += tasks[q].w;
+        const long long cap = std::max<long long>(1, (total + W - 1) / W);
+        units.clear();
+        wts.clear();
+        for (int id : ids) {
+            long long cw = 0;
+            for (int q = id; q >= 0; q = tasks[q].next) cw += tasks[q].w;
+            if (cw <= cap || tasks[id].next < 0) {
+                units.emplace_back();
+                for (int q = id; q >= 0; q = tasks[q].next) units.back().push_back(q);
+                wts.push_back(cw);
+                continue;
+            }
+            // segments: [diagonal, L...], then [recomputed diagonal, L...] ...
+            units.emplace_back(1, id);
+            long long uw = tasks[id].w;
+            int nl = 0;
+            for (int q = tasks[id].next; q >= 0; q = tasks[q].next) {
+                if (nl > 0 && uw + tasks[q].w > cap) {
+                    wts.push_back(uw);
+                    units.emplace_back(1, ~id);
+                    uw = tasks[id].w;
+                    nl = 0;
+                }
+                units.back().push_back(q);
+                uw += tasks[q].w;
+                ++nl;
+            }
+            wts.push_back(uw);
         }
         const int mx = deal(wts, W, who);
         if (level_work) (*level_work)[h] += mx;
         for (int w = 0; w < W; ++w) {
             ptr[(size_t)h * W + w] = four ? (int)(out.size() / 4) : (int)(out.size() / 2);
-            for (size_t i = 0; i < ids.size(); ++i) {
+            for (size_t i = 0; i < units.size(); ++i) {
                 if (who[i] != w) continue;
-                for (int q = ids[i]; q >= 0; q = tasks[q].next) {
-                    const Task& t = tasks[q];
-                    out.push_back(t.dst);
-                    out.push_back(t.code);
-                    if (four) {
-                        out.push_back(t.p0);
-                        out.push_back(t.p1);
-                    }
-                }
+                for (int q : units[i]) emit(q);
             }
         }
     }
@@ -224,7 +258,8 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
     p.base.assign(nv + 1, 0);
     for (int t = 0; t < nv; ++t) p.base[t + 1] = p.base[t] + 1 + 2 * (p.Lp[t + 1] - p.Lp[t]);
     p.nblk = p.base[nv];
-    if ((long long)p.nblk * 4 >= (1LL << 31)) return "factor pattern too large for int32 positions";
+    if (((long long)p.nblk + p.nv) * 4 >= (1LL << 31)) return "factor pattern too large for int32 positions";
+    if (p.nv >= (1 << (31 - TASK_ROW_SHIFT))) return "too many buses for the task code's row field";
     auto cnt = [&](int t) { return p.Lp[t + 1] - p.Lp[t]; };
     auto posU = [&](int t, int b) { return p.base[t] + 1 + rank_in(p.Li, p.Lp[t], p.Lp[t + 1], b); };
     auto posL = [&](int a, int t) { return p.base[t] + 1 + cnt(t) + rank_in(p.Li, p.Lp[t], p.Lp[t + 1], a); };
@@ -294,7 +329,8 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
         // inverse diagonal the worker just computed)
         add_pairs_factor(p.base[t], p0, p1);
         int prev = (int)A.size();
-        A.push_back({h, p.base[t], TK_DIAG | (inA[p.base[t]] ? 0 : TASK_FILL), p0, p1, 8LL * (p1 - p0) + 24});
+        A.push_back({h, p.base[t], TK_DIAG | (inA[p.base[t]] ? 0 : TASK_FILL) | (t << TASK_ROW_SHIFT), p0, p1,
+                     8LL * (p1 - p0) + 24});
         p.n_factor_pairs += p1 - p0;
         for (int x = p.Lp[t]; x < p.Lp[t + 1]; ++x) {
             const int j = p.Li[x];
@@ -329,7 +365,7 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
         }
         p1 = (int)(p.pairs.size() / 2);
         p.n_bwd_pairs += p1 - p0;
-        C.push_back({p.depth[t], t, p.base[t], p0, p1, 4LL * (p1 - p0) + 8});
+        C.push_back({p.depth[t], t, p.nblk + t, p0, p1, 4LL * (p1 - p0) + 8});
     }
     if (p.pairs.size() / 2 >= (size_t)1 << 31) return "too many pairs";
     p.tasksA = std::move(A);
@@ -443,8 +479,14 @@ bool host_factor(const Plan& p, double* blk, double* pmin, double* pmax) {
                     mm_sub(acc, blk + 4 * (size_t)p.pairs[2 * q], blk + 4 * (size_t)p.pairs[2 * q + 1]);
                 double* o = blk + 4 * (size_t)T[0];
                 if (kind == TK_DIAG) {
-                    const int row = (int)(std::upper_bound(p.base.begin(), p.base.end(), T[0]) - p.base.begin()) - 1;
+                    const int row = T[1] >> TASK_ROW_SHIFT;
                     const double det = acc[0] * acc[3] - acc[1] * acc[2];
+                    const double inv = 1.0 / det;
+                    dinv[0] = acc[3] * inv;
+                    dinv[1] = -acc[1] * inv;
+                    dinv[2] = -acc[2] * inv;
+                    dinv[3] = acc[0] * inv;
+                    if (T[1] & TASK_NOSTORE) continue;  // a segment's copy: the inverse stays in dinv
                     const double u0 = std::fabs(acc[0]);
                     const double u1 = std::fabs(det / acc[0]);
                     if (!(u0 > 0.0) || !std::isfinite(u0) || !std::isfinite(det)) ok = false;
@@ -455,12 +497,7 @@ bool host_factor(const Plan& p, double* blk, double* pmin, double* pmax) {
                         mn = std::min(mn, u1);
                         mx = std::max(mx, u1);
                     }
-                    const double inv = 1.0 / det;
-                    o[0] = acc[3] * inv;
-                    o[1] = -acc[1] * inv;
-                    o[2] = -acc[2] * inv;
-                    o[3] = acc[0] * inv;
-                    for (int e = 0; e < 4; ++e) dinv[e] = o[e];
+                    for (int e = 0; e < 4; ++e) blk[4 * ((size_t)p.nblk + row) + e] = dinv[e];
                 } else if (T[1] & TASK_SCALE) {
                     o[0] = acc[0] * dinv[0] + acc[1] * dinv[2];
                     o[1] = acc[0] * dinv[1] + acc[1] * dinv[3];
@@ -505,7 +542,7 @@ void host_solve(const Plan& p, const double* blk, double* y) {
             r0 -= u[0] * y[2 * j] + u[1] * y[2 * j + 1];
             r1 -= u[2] * y[2 * j] + u[3] * y[2 * j + 1];
         }
-        const double* d = blk + 4 * (size_t)p.base[t];
+        const double* d = blk + 4 * ((size_t)p.nblk + t);
         y[2 * t] = d[0] * r0 + d[1] * r1;
         y[2 * t + 1] = d[2] * r0 + d[3] * r1;
     }
@@ -521,7 +558,7 @@ namespace gbpf {
 // check that no task of a level reads what another task of the same phase writes.
 std::string schedule_selftest(const Plan& p, double* blk, const double* R, double* y) {
     const int W = p.W;
-    std::vector<int> wstamp(p.nblk, -1), ystamp(std::max(p.nv, 1), -1);
+    std::vector<int> wstamp((size_t)p.nblk + p.nv, -1), ystamp(std::max(p.nv, 1), -1);
     for (int h = 0; h < p.nlev; ++h) {
         // structural: writes of the entry phase
         for (int w = 0; w < W; ++w)
@@ -529,13 +566,17 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                 const int* T = &p.taskA[4 * (size_t)t];
                 if ((T[1] & 3) == TK_FWD)
                     ystamp[T[0]] = h;
-                else
+                else if ((T[1] & 3) == TK_DIAG) {  // writes its inverse; the Jacobian's block stays
+                    if (!(T[1] & TASK_NOSTORE)) wstamp[(size_t)p.nblk + (T[1] >> TASK_ROW_SHIFT)] = h;
+                } else
                     wstamp[T[0]] = h;
             }
         for (int w = 0; w < W; ++w)
             for (int t = p.ptrA[(size_t)h * W + w]; t < p.ptrA[(size_t)h * W + w + 1]; ++t) {
                 const int* T = &p.taskA[4 * (size_t)t];
                 const bool fwd = (T[1] & 3) == TK_FWD;
+                if ((T[1] & 3) == TK_DIAG && wstamp[T[0]] == h)
+                    return "level " + std::to_string(h) + ": a diagonal block is rewritten in its level";
                 for (int q = T[2]; q < T[3]; ++q) {
                     const int a = p.pairs[2 * q], b = p.pairs[2 * q + 1];
                     if (wstamp[a] == h) return "level " + std::to_string(h) + ": a task reads a block written in its level";
@@ -578,12 +619,13 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                     const double det = acc[0] * acc[3] - acc[1] * acc[2];
                     if (!(std::fabs(det) > 0.0)) return "zero pivot block";
                     const double inv = 1.0 / det;
-                    o[0] = acc[3] * inv;
-                    o[1] = -acc[1] * inv;
-                    o[2] = -acc[2] * inv;
-                    o[3] = acc[0] * inv;
-                    for (int e = 0; e < 4; ++e) dinv[e] = o[e];
+                    dinv[0] = acc[3] * inv;
+                    dinv[1] = -acc[1] * inv;
+                    dinv[2] = -acc[2] * inv;
+                    dinv[3] = acc[0] * inv;
                     dinv_level = h;
+                    if (!(T[1] & TASK_NOSTORE))
+                        for (int e = 0; e < 4; ++e) blk[4 * ((size_t)p.nblk + (T[1] >> TASK_ROW_SHIFT)) + e] = dinv[e];
                 } else if (T[1] & TASK_SCALE) {
                     if (dinv_level != h) return "level " + std::to_string(h) + ": an L block without its diagonal";
                     o[0] = acc[0] * dinv[0] + acc[1] * dinv[2];
@@ -642,7 +684,8 @@ extern "C" int gbpf_plan_selftest(int n, const int32_t* Yp, const int32_t* Yj, c
     gbpf::Plan p;
     std::string e = gbpf::build_plan(p, n, Yp, Yj, nnz, pv, npv, pq, npq, workers);
     if (e.empty()) {
-        std::vector<double> blk(4 * (size_t)p.nblk), R(2 * (size_t)std::max(p.nv, 1)), y(2 * (size_t)std::max(p.nv, 1));
+        std::vector<double> blk(4 * ((size_t)p.nblk + p.nv)), R(2 * (size_t)std::max(p.nv, 1)),
+            y(2 * (size_t)std::max(p.nv, 1));
         gbpf::host_eval(p, Yp, Yj, Yx, Vm, Va, S, nullptr, blk.data(), R.data());
         e = gbpf::schedule_selftest(p, blk.data(), R.data(), y.data());
         if (e.empty()) {

@@ -15,9 +15,13 @@
 //  * Factor entries are computed in Crout form, one task per block; a pivot's diagonal block
 //    and its column of L form one chain on one worker (the inverse diagonal stays in
 //    registers and scales each L block as it is computed: no separate scaling pass, one
-//    barrier per level). Tasks and chains are grouped by elimination-tree height (level) and
-//    dealt to the CTA's workers longest-first onto the least-loaded worker. The forward
-//    substitution rides along in the same levels.
+//    barrier per level). The inverse diagonal is stored apart, at block nblk + row, so the
+//    Jacobian's diagonal block stays intact through the pass: a chain heavier than its
+//    level's share of a worker is cut into segments, each later segment led by a copy of
+//    the diagonal task that recomputes the inverse from it without storing anything. Tasks
+//    and chain segments are grouped by elimination-tree height (level) and dealt to the
+//    CTA's workers longest-first onto the least-loaded worker. The forward substitution
+//    rides along in the same levels.
 #pragma once
 
 #include <cstdint>
@@ -29,6 +33,9 @@ namespace gbpf {
 enum TaskKind { TK_DIAG = 0, TK_U = 1, TK_L = 2, TK_FWD = 3 };
 constexpr int TASK_SCALE = 1 << 3;  // L block: multiply by the inverse diagonal block computed just before
 constexpr int TASK_FILL = 1 << 4;   // block not in the Jacobian: accumulate from zero
+// (bit 5: the diagonal block has two real pivots -- a PQ row; set when a schedule is uploaded)
+constexpr int TASK_NOSTORE = 1 << 6;  // diagonal recomputed for a chain segment: keep the inverse in registers
+constexpr int TASK_ROW_SHIFT = 8;     // diagonal tasks: block row in code >> 8 (inverse at block nblk + row)
 
 // One unit of factorization work before it is dealt to a worker: its level, destination
 // block (or row), code, pair range and weight (the dealing key).
@@ -63,7 +70,8 @@ struct Plan {
     std::vector<int> Lp, Li;        // strict lower structure of each pivot column, ascending
     std::vector<int> parent, height, depth;
     std::vector<int> base;          // first block of each pivot (its diagonal), size nv+1
-    int nblk = 0;
+    int nblk = 0;                   // blocks of the pattern; factor arrays hold nblk + nv (the
+                                    // inverse diagonal of row r at block nblk + r)
     std::vector<int> posmap;        // Ybus nnz -> block position, -1 if a slack is involved
     std::vector<int> ydiag;         // bus -> CSR index of its diagonal, -1 if none
     // schedule for W workers
@@ -73,7 +81,7 @@ struct Plan {
     std::vector<int> ptrA;          // nlev*W + 1
     std::vector<int> scl;           // 2 ints: L block, diagonal block
     std::vector<int> ptrB;          // nlev*W + 1
-    std::vector<int> taskC;         // backward: 4 ints: row, diag block, p0, p1
+    std::vector<int> taskC;         // backward: 4 ints: row, inverse-diagonal block, p0, p1
     std::vector<int> ptrC;          // nblev*W + 1
     std::vector<int> pairs;         // 2 ints per pair
     // undealt tasks (entry, scale, backward), kept so other worker counts can be scheduled
@@ -95,6 +103,7 @@ void make_schedule(const Plan& p, int workers, Schedule& out);
 
 // Host replica of the device algorithm (double precision): Jacobian blocks at (Vm, Va)
 // written to `blocks` (nblk*4, zero where not in the Jacobian) and residual R (nv*2).
+// host_factor / host_solve take arrays of (nblk + nv) * 4 (the inverse diagonals after them).
 void host_eval(const Plan& p, const int* Yp, const int* Yj, const double* Yx, const double* Vm, const double* Va,
                const double* S, const uint8_t* pin, double* blocks, double* R);
 // Serial block LU with the plan (in place); returns min/max real pivot in pmin/pmax and

@@ -65,7 +65,7 @@ def _selftest(g, workers, seed=1):
     return np.abs(dx.reshape(-1, 2) - ref).max() / max(1.0, np.abs(ref).max()), shape
 
 
-@pytest.mark.parametrize("workers", [1, 16, 64])
+@pytest.mark.parametrize("workers", [1, 16, 64, 1024])
 def test_block_schedule_solves_the_power_flow_jacobian(workers):
     """The device's 2x2-block LU schedule, executed serially with a race check per level,
     solves what scipy solves (the reference's test_plan_solves_power_flow_jacobian)."""
