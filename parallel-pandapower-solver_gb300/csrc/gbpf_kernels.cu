@@ -203,11 +203,19 @@ __device__ unsigned long long eval_row(const EvalCtx& c, int i, int s, int row, 
     float gii32 = 0.f, bii32 = 0.f;
     const int k0 = __ldg(&P.Yp[i]), k1 = __ldg(&P.Yp[i + 1]);
     const unsigned mask = row_stamp_mask(c, k0, k1);
+    // the next nonzero's column and phasor are loaded while this one is worked on (the stores
+    // of the Jacobian blocks would otherwise keep them from being issued early)
+    int jn = k0 < k1 ? __ldg(&P.Yj[k0]) : 0;
+    double2 en = k0 < k1 ? c.Et[((size_t)jn << c.lg) + s] : make_double2(0.0, 0.0);
     for (int k = k0; k < k1; ++k) {
-        const int j = __ldg(&P.Yj[k]);
+        const int j = jn;
+        const double2 ej = en;
+        if (k + 1 < k1) {
+            jn = __ldg(&P.Yj[k + 1]);
+            en = c.Et[((size_t)jn << c.lg) + s];
+        }
         const double2 y = ybus_val(c, k, mask);
         const size_t sj = ((size_t)j << c.lg) + s;
-        const double2 ej = c.Et[sj];
         Ir = fma(y.x, ej.x, Ir);
         Ir = fma(-y.y, ej.y, Ir);
         Ii = fma(y.x, ej.y, Ii);

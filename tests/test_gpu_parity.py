@@ -447,3 +447,31 @@ def test_async_slots_overlap_and_equal_the_synchronous_call(grid2000):
         assert np.array_equal(cv.astype(bool), ref["converged"])
     with pytest.raises(RuntimeError, match="nothing in flight"):
         s.wait(0)
+
+
+def test_chord_polish_steps_keep_the_solution(grid2000):
+    """Polish steps that reuse the previous float factors (chord_tol) reach the same converged
+    voltages as refactoring every step: both within 1e-9 of the oracle solved to convergence,
+    every step counted once as a factorization or a chord step."""
+    from p3s_gb300.solver import GpuSolver
+
+    g = grid2000
+    S = timeseries_injections(g, 256)
+    ref = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(S, g.V0, tol=1e-12)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    off = lanes(256, 256)
+    out = {}
+    for ct in (0.0, 1e-8, 1e-6):
+        r = s.solve_lanes(S, g.V0, off, GpuSolver.params(precision="mixed", chord_tol=ct))
+        st = s.stats
+        assert r["converged"].all()
+        steps = int(r["iterations"].sum())
+        # every step one float factorization, chord step or double factorization (a rejected
+        # float factorization is redone in double in the same step)
+        assert (st["single_factorizations"] + st["double_factorizations"] + st["chord_steps"]
+                == steps + st["single_rejected"])
+        assert (st["chord_steps"] == 0) == (ct == 0.0)
+        assert np.abs(r["V"] - ref["V"]).max() < 1e-9  # tolerance: mixed path vs converged oracle
+        assert (_mismatch(g, r["V"][:, :8], S[:, :8]) <= 1e-8).all()
+        out[ct] = r
+    assert (out[1e-8]["iterations"] <= out[0.0]["iterations"] + 1).all()
