@@ -907,54 +907,74 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         __syncthreads();
 
         // ---------------------------------------------------------------- step
-        for (int idx = tid; idx < nG; idx += NT) {
-            const int s = idx & (G - 1);
+        // A thread's elements idx = tid + k NT all belong to slot tid & (G - 1) (NT is a
+        // multiple of G), so the slot's state is read once and the next element's committed
+        // point and step are loaded while the current one is worked on.
+        {
+            const int s = tid & (G - 1);
             const int st = s_st[s];
-            if (st != SL_ACTIVE && st != SL_BACKTRACK && st != SL_NEEDJ) continue;
-            const int bus = idx >> lg;
-            const int row = P.row_of_bus[bus];
-            if (row < 0) continue;
-            const bool active = st == SL_ACTIVE;
-            // committed point: the one evaluated last when it was accepted (ACTIVE), else the
-            // other buffer; the new trial goes to the buffer that is not committed
-            const int cb = active ? s_tb[s] : 1 - s_tb[s];
-            const double4_32a vc = (cb ? Vb1 : Vb0)[idx];
-            double4_32a* const Vt = cb ? Vb0 : Vb1;
-            double dth, dvm;
-            if (s_yprec[s]) {
-                const float2 dd = y32[((size_t)row << lg) + s];
-                dth = f2d_fast(dd.x);
-                dvm = f2d_fast(dd.y);
-            } else {
-                const double2 dd = y64[((size_t)row << lg) + s];
-                dth = dd.x;
-                dvm = dd.y;
-            }
-            // trial point (nr_klu.cpp:665-669 form_trial): committed + alpha * step
-            const double d = active ? dth : s_alpha[s] * dth;
-            const double va = vc.y + d;
-            const bool pq = __ldg(&P.bus_pq[bus]) != 0;
-            const double vm = !pq ? vc.x : (active ? vc.x + dvm : fma(s_alpha[s], dvm, vc.x));
-            double cs, sn;
-            const unsigned ahi = (unsigned)__double2hiint(d) & 0x7fffffffu;
-            if (ahi < 0x3FD00000u) {  // |d| < 1/4: rotate the committed phasor by d
-                double sd, cd;
-                sincos_small(d, ahi, &sd, &cd);
-                cs = fma(vc.z, cd, -vc.w * sd);
-                sn = fma(vc.w, cd, vc.z * sd);
-            } else {
-                sincos(va, &sn, &cs);
-            }
-            Vt[idx] = make_double4_32a(vm, va, cs, sn);
-            const double e = vm * cs, f = vm * sn;
-            Et[idx] = make_double2(e, f);
-            if (pq) {  // PV buses keep the magnitude they were loaded with (and never read iv32)
-                if (!Bt.mixed || s_vote[s] != 1) {  // the next Jacobian is double
-                    const double iv = recip_nr(vm);
-                    Ei[idx] = iv;
-                    iv32[idx] = d2f_fast(iv);
-                } else {
-                    iv32[idx] = __frcp_rn(d2f_fast(vm));
+            if (st == SL_ACTIVE || st == SL_BACKTRACK || st == SL_NEEDJ) {
+                const bool active = st == SL_ACTIVE;
+                // committed point: the one evaluated last when it was accepted (ACTIVE), else
+                // the other buffer; the new trial goes to the buffer that is not committed
+                const int cb = active ? s_tb[s] : 1 - s_tb[s];
+                const double4_32a* const Vc = cb ? Vb1 : Vb0;
+                double4_32a* const Vt = cb ? Vb0 : Vb1;
+                const bool ystep32 = s_yprec[s] != 0;
+                const double alpha = s_alpha[s];
+                const bool next_double = !Bt.mixed || s_vote[s] != 1;  // the next Jacobian is double
+                auto fetch = [&](int at, int& row, double4_32a& vc, double& dth, double& dvm) {
+                    row = P.row_of_bus[at >> lg];
+                    vc = Vc[at];
+                    if (row < 0) return;
+                    if (ystep32) {
+                        const float2 dd = y32[((size_t)row << lg) + s];
+                        dth = f2d_fast(dd.x);
+                        dvm = f2d_fast(dd.y);
+                    } else {
+                        const double2 dd = y64[((size_t)row << lg) + s];
+                        dth = dd.x;
+                        dvm = dd.y;
+                    }
+                };
+                int rown = -1;
+                double4_32a vcn = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+                double dthn = 0.0, dvmn = 0.0;
+                if (tid < nG) fetch(tid, rown, vcn, dthn, dvmn);
+                for (int idx = tid; idx < nG; idx += NT) {
+                    const int row = rown;
+                    const double4_32a vc = vcn;
+                    const double dth = dthn, dvm = dvmn;
+                    if (idx + NT < nG) fetch(idx + NT, rown, vcn, dthn, dvmn);
+                    if (row < 0) continue;
+                    const int bus = idx >> lg;
+                    // trial point (nr_klu.cpp:665-669 form_trial): committed + alpha * step
+                    const double d = active ? dth : alpha * dth;
+                    const double va = vc.y + d;
+                    const bool pq = __ldg(&P.bus_pq[bus]) != 0;
+                    const double vm = !pq ? vc.x : (active ? vc.x + dvm : fma(alpha, dvm, vc.x));
+                    double cs, sn;
+                    const unsigned ahi = (unsigned)__double2hiint(d) & 0x7fffffffu;
+                    if (ahi < 0x3FD00000u) {  // |d| < 1/4: rotate the committed phasor by d
+                        double sd, cd;
+                        sincos_small(d, ahi, &sd, &cd);
+                        cs = fma(vc.z, cd, -vc.w * sd);
+                        sn = fma(vc.w, cd, vc.z * sd);
+                    } else {
+                        sincos(va, &sn, &cs);
+                    }
+                    Vt[idx] = make_double4_32a(vm, va, cs, sn);
+                    const double e = vm * cs, f = vm * sn;
+                    Et[idx] = make_double2(e, f);
+                    if (pq) {  // PV buses keep the magnitude they were loaded with (and never read iv32)
+                        if (next_double) {
+                            const double iv = recip_nr(vm);
+                            Ei[idx] = iv;
+                            iv32[idx] = d2f_fast(iv);
+                        } else {
+                            iv32[idx] = __frcp_rn(d2f_fast(vm));
+                        }
+                    }
                 }
             }
         }
