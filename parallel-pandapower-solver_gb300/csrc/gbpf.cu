@@ -152,7 +152,7 @@ struct gbpf_solver {
     std::vector<std::unique_ptr<Shape>> shapes;
     std::vector<std::unique_ptr<ExecSlot>> slots;  // asynchronous calls (gbpf_solve_lanes_async)
     // topology on the device
-    DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos;
+    DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos, deval_order;
     gbpf::DevPlan dp{};  // topology part (schedule fields filled per shape)
     // scratch: one region per CTA (grow-only)
     DBuf scr;
@@ -173,7 +173,7 @@ struct gbpf_solver {
             if (sl->stream) cudaStreamSynchronize(sl->stream);
         slots.clear();
         shapes.clear();
-        for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row,
+        for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row, &deval_order,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
                         &btab, &bjobs, &iin, &iscr, &ibest, &iout, &dbr_f, &dbr_t, &dbr_live, &dbr_pos, &dbr_val,
                         &dslack, &dprio, &dg_ptr, &dg_src, &dshunt})
@@ -395,6 +395,7 @@ int upload_plan(gbpf_solver* s) {
     CK(upload(s->dYj, s->Yj));
     CK(upload(s->dposmap, p.posmap));
     CK(upload(s->drow_of_bus, p.row_of_bus));
+    CK(upload(s->deval_order, p.eval_order));
     CK(upload(s->dbus_pq, p.bus_pq));
     CK(upload(s->dpairs, p.pairs));
     CK(upload(s->drow_pq, p.row_pq));
@@ -416,6 +417,7 @@ int upload_plan(gbpf_solver* s) {
     d.Y32 = s->dY32.as<float2>();
     d.posmap = s->dposmap.as<int>();
     d.row_of_bus = s->drow_of_bus.as<int>();
+    d.eval_order = s->deval_order.as<int>();
     d.bus_pq = s->dbus_pq.as<uint8_t>();
     d.taskA = nullptr;
     d.ptrA = nullptr;

@@ -40,6 +40,7 @@ struct DevPlan {
     const float2* Y32;       // float copy
     const int* posmap;       // Ybus nnz -> block, -1
     const int* row_of_bus;   // bus -> block row, -1 for slack
+    const int* eval_order;   // the evaluation's bus sweep (reverse Cuthill-McKee)
     const uint8_t* bus_pq;
     const int4* taskA;
     const int* ptrA;

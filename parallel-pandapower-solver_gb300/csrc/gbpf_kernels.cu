@@ -986,16 +986,18 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         __syncthreads();
 
         // ---------------------------------------------------------------- evaluate
+        // Buses are swept in reverse Cuthill-McKee order, so the buses a CTA evaluates at the
+        // same time share their neighbours' state in cache.
         for (int idx = tid; idx < nG; idx += NT) {
             const int s = idx & (G - 1);
             const int st = s_st[s];
             if (st != SL_FRESH && st != SL_ACTIVE && st != SL_NEEDJ && st != SL_BACKTRACK) continue;
-            const int bus = idx >> lg;
+            const int bus = __ldg(&P.eval_order[idx >> lg]);
             const int row = P.row_of_bus[bus];
             if (row < 0) continue;
             const int c = s_case[s];
             const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
-            const bool pinned = spin[idx] != 0;
+            const bool pinned = spin[((size_t)bus << lg) + s] != 0;
             const bool pq = P.bus_pq[bus] != 0;
             EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;

@@ -76,6 +76,43 @@ int deal(const std::vector<long long>& weight, int W, std::vector<int>& who) {
 
 using Task = PlanTask;
 
+// Reverse Cuthill-McKee order of the bus graph (the Ybus pattern): breadth-first from a
+// least-connected unvisited bus of each component, neighbours by increasing degree, the
+// whole sequence reversed (Cuthill & McKee 1969; George's reversal).
+std::vector<int> rcm_order(int n, const int* Yp, const int* Yj) {
+    std::vector<int> deg(n, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = Yp[i]; k < Yp[i + 1]; ++k) deg[i] += Yj[k] != i;
+    auto lighter = [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; };
+    std::vector<int> starts(n);
+    for (int i = 0; i < n; ++i) starts[i] = i;
+    std::sort(starts.begin(), starts.end(), lighter);
+    std::vector<char> seen(n, 0);
+    std::vector<int> order, nb;
+    order.reserve(n);
+    for (int s0 : starts) {
+        if (seen[s0]) continue;
+        size_t head = order.size();
+        order.push_back(s0);
+        seen[s0] = 1;
+        while (head < order.size()) {
+            const int u = order[head++];
+            nb.clear();
+            for (int k = Yp[u]; k < Yp[u + 1]; ++k) {
+                const int j = Yj[k];
+                if (j != u && !seen[j]) {
+                    seen[j] = 1;
+                    nb.push_back(j);
+                }
+            }
+            std::sort(nb.begin(), nb.end(), lighter);
+            order.insert(order.end(), nb.begin(), nb.end());
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
 // Lay tasks out grouped by (level, worker); `four`: 4 ints per record (else 2). Chains
 // (a diagonal and its L column) go to one worker; a chain heavier than its level's share of a
 // worker (total weight / W) is cut into segments of at most that share (at least one L block
@@ -202,6 +239,7 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
         a.erase(std::unique(a.begin(), a.end()), a.end());
     }
     p.perm = min_degree(adj);
+    p.eval_order = rcm_order(n, Yp, Yj);
     p.pinv.assign(nv, -1);
     for (int k = 0; k < nv; ++k) p.pinv[p.perm[k]] = k;
     p.row_of_bus.assign(n, -1);

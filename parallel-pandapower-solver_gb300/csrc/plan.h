@@ -66,6 +66,8 @@ struct Plan {
     std::vector<int> row_of_bus;    // bus -> block row (pivot index) or -1
     std::vector<int> bus_of_row;    // block row -> bus
     std::vector<uint8_t> row_pq;    // block row is a PQ bus
+    std::vector<int> eval_order;    // buses in reverse Cuthill-McKee order (the evaluation's sweep:
+                                    // buses evaluated together share their neighbours' state)
     // symbolic (block level, pivot numbering)
     std::vector<int> Lp, Li;        // strict lower structure of each pivot column, ascending
     std::vector<int> parent, height, depth;
