@@ -120,7 +120,7 @@ std::vector<int> rcm_order(int n, const int* Yp, const int* Yj) {
 // TASK_NOSTORE (it recomputes the inverse from the Jacobian's diagonal, which the pass
 // leaves in place). Units are dealt longest-first onto the least-loaded worker.
 void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& out, std::vector<int>& ptr,
-            std::vector<int>* level_work, bool four) {
+            std::vector<int>* level_work, bool four, const std::vector<int>* key = nullptr) {
     std::vector<std::vector<int>> by_level(nlev);
     for (int i = 0; i < (int)tasks.size(); ++i)
         if (tasks[i].head) by_level[tasks[i].level].push_back(i);
@@ -174,12 +174,23 @@ void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& o
         }
         const int mx = deal(wts, W, who);
         if (level_work) (*level_work)[h] += mx;
+        // within a worker, units in the order of their key (the factor position they work
+        // on): at any moment the workers of a CTA are at similar positions and share the
+        // blocks they read in cache
+        std::vector<int> mine;
         for (int w = 0; w < W; ++w) {
             ptr[(size_t)h * W + w] = four ? (int)(out.size() / 4) : (int)(out.size() / 2);
-            for (size_t i = 0; i < units.size(); ++i) {
-                if (who[i] != w) continue;
+            mine.clear();
+            for (size_t i = 0; i < units.size(); ++i)
+                if (who[i] == w) mine.push_back((int)i);
+            if (key)
+                std::stable_sort(mine.begin(), mine.end(), [&](int a, int b) {
+                    const int qa = units[a][0] < 0 ? ~units[a][0] : units[a][0];
+                    const int qb = units[b][0] < 0 ? ~units[b][0] : units[b][0];
+                    return (*key)[qa] < (*key)[qb];
+                });
+            for (int i : mine)
                 for (int q : units[i]) emit(q);
-            }
         }
     }
     ptr[(size_t)nlev * W] = four ? (int)(out.size() / 4) : (int)(out.size() / 2);
@@ -424,9 +435,17 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
 void make_schedule(const Plan& p, int workers, Schedule& out) {
     const int W = out.W = std::max(1, workers);
     out.level_work.assign(std::max(p.nlev, p.nblev), 0);
-    layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true);
+    // factor-level key: the task's destination block (a forward row: its diagonal block)
+    std::vector<int> keyA(p.tasksA.size());
+    for (size_t i = 0; i < p.tasksA.size(); ++i) {
+        const Task& t = p.tasksA[i];
+        keyA[i] = (t.code & 3) == TK_FWD ? p.base[t.dst] : t.dst;
+    }
+    layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true, &keyA);
     layout(p.tasksB, p.nlev, W, out.scl, out.ptrB, nullptr, false);
-    layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true);
+    std::vector<int> keyC(p.tasksC.size());
+    for (size_t i = 0; i < p.tasksC.size(); ++i) keyC[i] = p.tasksC[i].dst;
+    layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true, &keyC);
 }
 
 // ----------------------------------------------------------------------------- host replica
