@@ -473,6 +473,7 @@ def gpu_line(args, res, rank, world):
         "case_iterations_per_launch": its_mixed,
         "factorizations_per_launch": n_fac,
         "chord_steps_per_launch": int(mixed["stats"].get("chord_steps", 0)),
+        "first_steps_per_launch": int(mixed["stats"].get("first_steps", 0)),
     }
     # fp64 pipe roofline of the double path (GB300: ~1.2 TFLOP/s)
     fp64 = {

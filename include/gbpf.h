@@ -65,6 +65,10 @@ typedef struct gbpf_stats {
     double call_ms;   /* device time of the last host-pointer call: first copy in to last copy out */
     int threads_per_cta; /* CTA shape of the last launch (with cases_per_cta) */
     unsigned long long chord_steps; /* steps solved with the previous float factors (chord_tol) */
+    unsigned long long first_steps; /* first steps solved with the shared start's factors: when every
+                                       case starts from one V0 on the base Ybus without pins, the
+                                       first mismatch's injections and J(V0) are computed and
+                                       factored once per launch */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);

@@ -494,13 +494,35 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     b.counter = reinterpret_cast<int*>(ctl + 16);
     b.stats = ctl;
     b.err = reinterpret_cast<int*>(ctl + 24);
+    // shared start: every case from the same V0 on the base Ybus without pins -- its first
+    // evaluation and factorization are computed once (start_kernel) for the whole launch
+    const bool share = b.v0_shared && b.ymode == 0 && !b.pin && !b.ref_bus && (!b.mixed || b.vote_rule == 1);
+    gbpf::StartJob sj{};
+    const size_t tab_bytes = ((size_t)s->n * 64 + 255) & ~(size_t)255;
     if (b.v0_shared) {
-        CK(R.btab->ensure((size_t)s->n * 64));
+        const size_t need = tab_bytes + (share ? gbpf::start_bytes(s->n, s->plan.nv, s->plan.nblk, G, b.mixed != 0) : 0);
+        CK(R.btab->ensure(need));
         b.v0tab = R.btab->as<double4_32a>();
     }
+    if (share) {
+        Shape* s1 = nullptr;
+        if (int rc = get_shape(s, 1024, 1, &s1)) return rc;
+        sj.P = s1->dp;
+        sj.v0tab = b.v0tab;
+        sj.mixed = b.mixed;
+        sj.log2G = ilog2(G);
+        sj.rcond_min = b.mixed ? b.rcond_min32 : b.rcond_min64;
+        gbpf::start_carve(sj, R.btab->as<char>() + tab_bytes, s->n, s->plan.nv, s->plan.nblk, G, b.mixed != 0);
+        b.R0 = sj.R0;
+        b.fac0 = sj.facG;
+        b.ok0 = sj.ok0;
+    }
     job.B = b;
-    CK(R.bjobs->ensure(sizeof(gbpf::Job)));
+    const size_t job_bytes = (sizeof(gbpf::Job) + 255) & ~(size_t)255;
+    CK(R.bjobs->ensure(job_bytes + sizeof(gbpf::StartJob)));
     CK(cudaMemcpyAsync(R.bjobs->p, &job, sizeof job, cudaMemcpyHostToDevice, R.stream));
+    if (share)
+        CK(cudaMemcpyAsync(R.bjobs->as<char>() + job_bytes, &sj, sizeof sj, cudaMemcpyHostToDevice, R.stream));
     gbpf::Launch L{};
     L.jobs = R.bjobs->as<gbpf::Job>();
     L.njobs = 1;
@@ -509,6 +531,8 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     CK(cudaEventRecord(R.e0, R.stream));
     if (b.v0_shared)
         CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, R.btab->as<double4_32a>(), b.err, R.stream));
+    if (share)
+        CK(gbpf::launch_start(reinterpret_cast<const gbpf::StartJob*>(R.bjobs->as<char>() + job_bytes), 1, R.stream));
     CK(gbpf::launch_newton(L, grid, NT, R.stream));
     CK(cudaEventRecord(R.e1, R.stream));
     CK(cudaMemcpyAsync(R.host_ctl, ctl, 32 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.stream));
@@ -529,6 +553,7 @@ int finish_launch(const LaunchRes& R, int grid, int G, int NT, const char* who, 
     st->double_rejected = host_ctl[3];
     st->macro_steps = host_ctl[4];
     st->chord_steps = host_ctl[5];
+    st->first_steps = host_ctl[6];
     st->grid = grid;
     st->cases_per_cta = G;
     st->threads_per_cta = NT;
@@ -803,6 +828,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         st.double_rejected += c[3];
         st.macro_steps += c[4];
         st.chord_steps += c[5];
+        st.first_steps += c[6];
     }
     st.grid = grid;
     st.cases_per_cta = Gmax;

@@ -102,11 +102,17 @@ struct Batch {
     int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
     double tol_polish;       // GB300 rule: float-factor cases iterate until mismatch < tol_polish
     double chord_tol;        // GB300 rule: below this mismatch a step reuses the last float factors (0: never)
+    // shared start (every case from the same V0 on the same Ybus, no pins): the injections and
+    // the factors of J(V0), computed once by start_kernel; cases starting from V0 take their
+    // first step with them (null: every case evaluates and factors its own start)
+    const double2* R0;       // -(P, Q) at V0 per block row (0 for a PV row's Q)
+    const void* fac0;        // factors of J(V0), one copy per case slot: [blk][slot], float4 / double4
+    const int* ok0;          // 1 when the shared factorization passed its pivot check
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch
     unsigned long long* stats;  // [0] fp32 factorizations [1] fp64 [2] fp32 rejected [3] fp64 rejected [4] macro steps
-                                // [5] chord steps
+                                // [5] chord steps [6] first steps with the shared start's factors
     int* err;                // [0] code [1] bus [2] case
 };
 
@@ -159,6 +165,31 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
                               double4_32a* Vt, double2* Et, double* Ei, float* iv32, double4_32a* blocks,
                               double2* R, cudaStream_t stream);
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream);
+
+// One shared start of a launch: the plan with its 1,024-thread, one-slot schedule, the start
+// table, and where the start's injections and factors go (replicated to the G slots of the
+// Newton launch that uses them).
+struct StartJob {
+    DevPlan P;
+    const double4_32a* v0tab;
+    int mixed;               // float factors (the GB300 rule's first step) or double
+    int log2G;               // slots per CTA of the Newton launch (the replication)
+    double rcond_min;        // pivot-ratio bound of the factorization
+    double2* R0;             // [row] -(P, Q) at V0
+    void* fac1;              // [blk] the factors (nblk + nv blocks)
+    void* facG;              // [blk][slot] the same, once per slot
+    double2* y0;             // [row] scratch of the factorization's forward pass
+    double2* Et0;            // [bus] scratch: the start's (e, f), 1 / Vm
+    double* Ei0;
+    float* iv0;
+    int* ok0;
+};
+// Bytes of a shared start's buffers (R0, fac1, facG, y0, Et0, Ei0, iv0, ok0), each 256-aligned.
+size_t start_bytes(int n, int nv, int nblk, int G, bool mixed);
+// Carves those buffers from `base` into `sj`.
+void start_carve(StartJob& sj, char* base, int n, int nv, int nblk, int G, bool mixed);
+// One CTA of 1,024 threads per shared start.
+cudaError_t launch_start(const StartJob* jobs, int njobs, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
 // Ybus values from stamps (postproc.cu)
 cudaError_t launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,

@@ -330,13 +330,21 @@ __device__ __forceinline__ T z4() {
     return r;
 }
 
+// Arithmetic of the factorization and substitutions with its rounding pinned: explicit fused
+// multiply-adds, so every copy of the code (a case's own factorization, the shared start's,
+// any CTA shape) rounds alike, and each 2x2 product costs two fused operations per entry.
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mulr(double a, double b) { return __dmul_rn(a, b); }
+
 // acc -= a * b (2x2 blocks, row-major)
 template <typename B4>
 __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
-    acc.x -= a.x * b.x + a.y * b.z;
-    acc.y -= a.x * b.y + a.y * b.w;
-    acc.z -= a.z * b.x + a.w * b.z;
-    acc.w -= a.z * b.y + a.w * b.w;
+    acc.x = fmadd(-a.y, b.z, fmadd(-a.x, b.x, acc.x));
+    acc.y = fmadd(-a.y, b.w, fmadd(-a.x, b.y, acc.y));
+    acc.z = fmadd(-a.w, b.z, fmadd(-a.z, b.x, acc.z));
+    acc.w = fmadd(-a.w, b.w, fmadd(-a.z, b.y, acc.w));
 }
 
 // One batched factorization + substitution pass over the slots flagged in `on` (G <= 32).
@@ -404,11 +412,11 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                             l1 = fac[((size_t)hd.z << lg) + s];
                             u1 = y[((size_t)hd.w << lg) + s];
                         }
-                        y0 -= l0.x * u0.x + l0.y * u0.y;
-                        y1 -= l0.z * u0.x + l0.w * u0.y;
+                        y0 = fmadd(-l0.y, u0.y, fmadd(-l0.x, u0.x, y0));
+                        y1 = fmadd(-l0.w, u0.y, fmadd(-l0.z, u0.x, y1));
                         if (np > 1) {
-                            y0 -= l1.x * u1.x + l1.y * u1.y;
-                            y1 -= l1.z * u1.x + l1.w * u1.y;
+                            y0 = fmadd(-l1.y, u1.y, fmadd(-l1.x, u1.x, y0));
+                            y1 = fmadd(-l1.w, u1.y, fmadd(-l1.z, u1.x, y1));
                         }
                     }
                     int p = task.z + np;
@@ -416,17 +424,17 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
                         const B4 l0 = fac[((size_t)q0.x << lg) + s], l1 = fac[((size_t)q1.x << lg) + s];
                         const B2 u0 = y[((size_t)q0.y << lg) + s], u1 = y[((size_t)q1.y << lg) + s];
-                        y0 -= l0.x * u0.x + l0.y * u0.y;
-                        y1 -= l0.z * u0.x + l0.w * u0.y;
-                        y0 -= l1.x * u1.x + l1.y * u1.y;
-                        y1 -= l1.z * u1.x + l1.w * u1.y;
+                        y0 = fmadd(-l0.y, u0.y, fmadd(-l0.x, u0.x, y0));
+                        y1 = fmadd(-l0.w, u0.y, fmadd(-l0.z, u0.x, y1));
+                        y0 = fmadd(-l1.y, u1.y, fmadd(-l1.x, u1.x, y0));
+                        y1 = fmadd(-l1.w, u1.y, fmadd(-l1.z, u1.x, y1));
                     }
                     if (p < task.w) {
                         const int2 q0 = __ldg(&P.pairs[p]);
                         const B4 l0 = fac[((size_t)q0.x << lg) + s];
                         const B2 u0 = y[((size_t)q0.y << lg) + s];
-                        y0 -= l0.x * u0.x + l0.y * u0.y;
-                        y1 -= l0.z * u0.x + l0.w * u0.y;
+                        y0 = fmadd(-l0.y, u0.y, fmadd(-l0.x, u0.x, y0));
+                        y1 = fmadd(-l0.w, u0.y, fmadd(-l0.z, u0.x, y1));
                     }
                     B2 o;
                     o.x = y0;
@@ -458,7 +466,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     mm_sub(acc, fac[((size_t)q0.x << lg) + s], fac[((size_t)q0.y << lg) + s]);
                 }
                 if (kind == 0) {  // diagonal block: its inverse, kept for the L blocks that follow
-                    const real det = acc.x * acc.w - acc.y * acc.z;
+                    const real det = fmadd(acc.x, acc.w, -mulr(acc.y, acc.z));
                     const real inv = (real)1 / det;
                     dinv.x = acc.w * inv;
                     dinv.y = -acc.y * inv;
@@ -482,10 +490,10 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                 } else if (task.y & 8) {  // L block: scaled by its column's inverse diagonal
                     B4 o;
                     const B4 dv = dinv_smem ? dinv_smem[tid] : dinv;
-                    o.x = acc.x * dv.x + acc.y * dv.z;
-                    o.y = acc.x * dv.y + acc.y * dv.w;
-                    o.z = acc.z * dv.x + acc.w * dv.z;
-                    o.w = acc.z * dv.y + acc.w * dv.w;
+                    o.x = fmadd(acc.x, dv.x, mulr(acc.y, dv.z));
+                    o.y = fmadd(acc.x, dv.y, mulr(acc.y, dv.w));
+                    o.z = fmadd(acc.z, dv.x, mulr(acc.w, dv.z));
+                    o.w = fmadd(acc.z, dv.y, mulr(acc.w, dv.w));
                     fac[((size_t)task.x << lg) + s] = o;
                 } else {
                     fac[((size_t)task.x << lg) + s] = acc;
@@ -521,11 +529,11 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         u1 = fac[((size_t)hd.z << lg) + s];
                         y1 = y[((size_t)hd.w << lg) + s];
                     }
-                    r0 -= u0.x * y0.x + u0.y * y0.y;
-                    r1 -= u0.z * y0.x + u0.w * y0.y;
+                    r0 = fmadd(-u0.y, y0.y, fmadd(-u0.x, y0.x, r0));
+                    r1 = fmadd(-u0.w, y0.y, fmadd(-u0.z, y0.x, r1));
                     if (np > 1) {
-                        r0 -= u1.x * y1.x + u1.y * y1.y;
-                        r1 -= u1.z * y1.x + u1.w * y1.y;
+                        r0 = fmadd(-u1.y, y1.y, fmadd(-u1.x, y1.x, r0));
+                        r1 = fmadd(-u1.w, y1.y, fmadd(-u1.z, y1.x, r1));
                     }
                 }
                 int p = task.z + np;
@@ -533,21 +541,21 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
                     const B4 u0 = fac[((size_t)q0.x << lg) + s], u1 = fac[((size_t)q1.x << lg) + s];
                     const B2 y0 = y[((size_t)q0.y << lg) + s], y1 = y[((size_t)q1.y << lg) + s];
-                    r0 -= u0.x * y0.x + u0.y * y0.y;
-                    r1 -= u0.z * y0.x + u0.w * y0.y;
-                    r0 -= u1.x * y1.x + u1.y * y1.y;
-                    r1 -= u1.z * y1.x + u1.w * y1.y;
+                    r0 = fmadd(-u0.y, y0.y, fmadd(-u0.x, y0.x, r0));
+                    r1 = fmadd(-u0.w, y0.y, fmadd(-u0.z, y0.x, r1));
+                    r0 = fmadd(-u1.y, y1.y, fmadd(-u1.x, y1.x, r0));
+                    r1 = fmadd(-u1.w, y1.y, fmadd(-u1.z, y1.x, r1));
                 }
                 if (p < task.w) {
                     const int2 q0 = __ldg(&P.pairs[p]);
                     const B4 u0 = fac[((size_t)q0.x << lg) + s];
                     const B2 y0 = y[((size_t)q0.y << lg) + s];
-                    r0 -= u0.x * y0.x + u0.y * y0.y;
-                    r1 -= u0.z * y0.x + u0.w * y0.y;
+                    r0 = fmadd(-u0.y, y0.y, fmadd(-u0.x, y0.x, r0));
+                    r1 = fmadd(-u0.w, y0.y, fmadd(-u0.z, y0.x, r1));
                 }
                 B2 o;
-                o.x = d.x * r0 + d.y * r1;
-                o.y = d.z * r0 + d.w * r1;
+                o.x = fmadd(d.x, r0, mulr(d.y, r1));
+                o.y = fmadd(d.z, r0, mulr(d.w, r1));
                 y[((size_t)task.x << lg) + s] = o;
             }
         }
@@ -646,9 +654,14 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ int s_nst[MAX_SLOTS];
     __shared__ int s_tb[MAX_SLOTS];
     __shared__ int s_fb[MAX_SLOTS], s_chord[MAX_SLOTS];  // float factor buffer; next step is a chord step
+    // s_first: the case started from the shared start and its first step uses the shared
+    // factors; s_nofac: this step solves with factors it does not compute (chord or first)
+    __shared__ int s_first[MAX_SLOTS], s_nofac[MAX_SLOTS];
+    __shared__ int s_share;  // the launch's shared start is usable (its factorization passed)
     __shared__ int s_stk[MAX_SLOTS][MAX_STAMPS];
     __shared__ double2 s_stv[MAX_SLOTS][MAX_STAMPS];
 
+    if (tid == 0) s_share = Bt.fac0 != nullptr && __ldg(Bt.ok0) == 1;  // written by the start kernel before this launch
     if (tid < G) {
         s_st[tid] = SL_EMPTY;
         s_lcur[tid] = s_lend[tid] = 0;
@@ -693,6 +706,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     if (!s_warm[s]) s_tb[s] = 0;
                     s_fb[s] = 0;
                     s_chord[s] = 0;
+                    s_first[s] = s_share && !s_warm[s];
                     s_it[s] = 0;
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
@@ -834,26 +848,29 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const bool f32 = act && Bt.mixed && s_vote[s] == 1 && s_jprec[s] == 1;
             s_on32[s] = f32;
             s_on64[s] = act && !f32;
-            s_reeval[s] = act && !f32 && s_jprec[s] == 1;
+            s_reeval[s] = act && !f32 && s_jprec[s] == 1 && !s_first[s];
+            s_nofac[s] = act && (s_chord[s] || s_first[s]);
             s_pmin[s] = ~0ULL;
             s_pmax[s] = 0ULL;
         }
         const int any32 = __syncthreads_or(tid < G && s_on32[tid]);
         if (any32) {
-            // chord steps are decided per slot (a result never depends on the other cases of
-            // its CTA); the factorization is left out altogether when every float slot takes one
-            const int all_chord = __syncthreads_and(!(tid < G && s_on32[tid]) || s_chord[tid]);
+            // chord and first steps are decided per slot (a result never depends on the other
+            // cases of its CTA); the factorization is left out altogether when no float slot
+            // of the CTA factors
+            const int all_chord = __syncthreads_and(!(tid < G && s_on32[tid]) || s_nofac[tid]);
             {
                 // a slot factors the Jacobian in the buffer its last factors are not in; a chord
-                // step solves with those factors
+                // step solves with those factors, a first step with the shared start's
                 const int sl = (tid & 31) & (G - 1);
                 const int buf = s_chord[sl] ? s_fb[sl] : 1 - s_fb[sl];
-                lu_pass<float>(P, buf ? fac32b : fac32, R, y32, s_on32, lg, s_pmin, s_pmax, s_chord, !all_chord, nullptr);
+                float4* const fl = s_first[sl] ? (float4*)Bt.fac0 : (buf ? fac32b : fac32);
+                lu_pass<float>(P, fl, R, y32, s_on32, lg, s_pmin, s_pmax, s_nofac, !all_chord, nullptr);
             }
             if (tid < G && s_on32[tid]) {
                 const int s = tid;
-                if (s_chord[s]) {
-                    atomicAdd(&Bt.stats[5], 1ULL);
+                if (s_nofac[s]) {
+                    atomicAdd(&Bt.stats[s_first[s] ? 6 : 5], 1ULL);
                 } else {
                     atomicAdd(&Bt.stats[0], 1ULL);
                     if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min32)) {
@@ -892,18 +909,33 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         const int any64 = __syncthreads_or(tid < G && s_on64[tid]);
         if (any64) {
-            lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true, s_dinv64);
+            if (s_share) {
+                // no double slot of the CTA factors (all take their first step): substitutions only
+                const int all_first = __syncthreads_and(!(tid < G && s_on64[tid]) || s_nofac[tid]);
+                const int sl = (tid & 31) & (G - 1);
+                double4_32a* const fd = s_first[sl] ? (double4_32a*)Bt.fac0 : fac64;
+                lu_pass<double>(P, fd, R, y64, s_on64, lg, s_pmin, s_pmax, s_nofac, !all_first, s_dinv64);
+            } else {
+                lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true, s_dinv64);
+            }
             if (tid < G && s_on64[tid]) {
                 const int s = tid;
-                atomicAdd(&Bt.stats[1], 1ULL);
-                if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min64)) {
-                    atomicAdd(&Bt.stats[3], 1ULL);
-                    s_st[s] = SL_FINISH;  // no pivoting fallback on the device: not converged
-                    s_conv[s] = 0;
+                if (s_nofac[s]) {
+                    atomicAdd(&Bt.stats[s_first[s] ? 6 : 5], 1ULL);
+                } else {
+                    atomicAdd(&Bt.stats[1], 1ULL);
+                    if (!pivots_ok(s_pmin[s], s_pmax[s], Bt.rcond_min64)) {
+                        atomicAdd(&Bt.stats[3], 1ULL);
+                        s_st[s] = SL_FINISH;  // no pivoting fallback on the device: not converged
+                        s_conv[s] = 0;
+                    }
                 }
             }
         }
-        if (tid < G && (s_on32[tid] || s_on64[tid])) s_yprec[tid] = s_on64[tid] ? 0 : 1;
+        if (tid < G && (s_on32[tid] || s_on64[tid])) {
+            s_yprec[tid] = s_on64[tid] ? 0 : 1;
+            s_first[tid] = 0;
+        }
         __syncthreads();
 
         // ---------------------------------------------------------------- step
@@ -997,8 +1029,19 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             if (row < 0) continue;
             const int c = s_case[s];
             const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
-            const bool pinned = spin[((size_t)bus << lg) + s] != 0;
             const bool pq = P.bus_pq[bus] != 0;
+            if (st == SL_FRESH && s_first[s]) {
+                // from the shared start: S - S(V0) with S(V0) computed once (the same operation
+                // eval_row does, Ssp - Pc = Ssp + (-Pc)); the Jacobian is the shared one
+                const double2 r0 = __ldg(&Bt.R0[row]);
+                const double rp = Ssp.x + r0.x;
+                const double rq = pq ? Ssp.y + r0.y : 0.0;
+                R[((size_t)row << lg) + s] = make_double2(rp, rq);
+                const unsigned long long a = abs_bits(rp), b = abs_bits(rq);
+                atomicMax(&s_res[s], b > a ? b : a);
+                continue;
+            }
+            const bool pinned = spin[((size_t)bus << lg) + s] != 0;
             EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;
             if (st == SL_BACKTRACK)
@@ -1223,6 +1266,101 @@ __global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const doubl
         piv[0] = s_min[0];
         piv[1] = s_max[0];
     }
+}
+
+// Shared start of a launch (every case from the same V0 on the same Ybus, no pins): the
+// injections S(V0) and the factors of J(V0) -- the same operations, in the same order, as
+// every case's own first evaluation and factorization would do -- computed once, the factors
+// then copied to every case slot of the Newton launch. One CTA per start; the start's plan
+// carries the 1,024-thread, one-slot schedule.
+template <int NTB>
+__global__ void __launch_bounds__(NTB, 1) start_kernel(const StartJob* jobs) {
+    __shared__ StartJob sj;
+    __shared__ int s_on[1];
+    __shared__ unsigned long long s_min[1], s_max[1];
+    const int tid = threadIdx.x;
+    {
+        const int* src = reinterpret_cast<const int*>(&jobs[blockIdx.x]);
+        int* dst = reinterpret_cast<int*>(&sj);
+        for (int w = tid; w < (int)(sizeof(StartJob) / 4); w += NTB) dst[w] = src[w];
+    }
+    if (tid == 0) {
+        s_on[0] = 1;
+        s_min[0] = ~0ULL;
+        s_max[0] = 0ULL;
+    }
+    __syncthreads();
+    const DevPlan& P = sj.P;
+    for (int i = tid; i < P.n; i += NTB) {  // as the Newton kernel loads a case from the table
+        const double4_32a t1 = sj.v0tab[2 * i + 1];
+        reinterpret_cast<double2*>(sj.Et0)[i] = make_double2(t1.x, t1.y);
+        sj.Ei0[i] = t1.z;
+        sj.iv0[i] = d2f_fast(t1.z);
+    }
+    __syncthreads();
+    for (int i = tid; i < P.n; i += NTB) {
+        const int row = P.row_of_bus[i];
+        if (row < 0) continue;
+        EvalCtx ec{&P, sj.Et0, sj.Ei0, sj.iv0, 0, 0, nullptr, 0, 0, 0, nullptr, nullptr};
+        if (sj.mixed)
+            eval_row<2>(ec, i, 0, row, false, P.bus_pq[i] != 0, make_double2(0.0, 0.0),
+                        reinterpret_cast<float4*>(sj.fac1), sj.R0, true);
+        else
+            eval_row<1>(ec, i, 0, row, false, P.bus_pq[i] != 0, make_double2(0.0, 0.0),
+                        reinterpret_cast<double4_32a*>(sj.fac1), sj.R0, true);
+    }
+    __syncthreads();
+    if (sj.mixed)
+        lu_pass<float>(P, reinterpret_cast<float4*>(sj.fac1), sj.R0, reinterpret_cast<float2*>(sj.y0), s_on, 0, s_min,
+                       s_max, nullptr, true, nullptr);
+    else
+        lu_pass<double>(P, reinterpret_cast<double4_32a*>(sj.fac1), sj.R0, sj.y0, s_on, 0, s_min, s_max, nullptr, true,
+                        nullptr);
+    // replicate to every slot: [blk] -> [blk][slot]
+    const int G = 1 << sj.log2G;
+    const long long nb = (long long)P.nblk + P.nv;
+    if (sj.mixed) {
+        const float4* a = reinterpret_cast<const float4*>(sj.fac1);
+        float4* b = reinterpret_cast<float4*>(sj.facG);
+        for (long long q = tid; q < nb * G; q += NTB) b[q] = a[q >> sj.log2G];
+    } else {
+        const double4_32a* a = reinterpret_cast<const double4_32a*>(sj.fac1);
+        double4_32a* b = reinterpret_cast<double4_32a*>(sj.facG);
+        for (long long q = tid; q < nb * G; q += NTB) b[q] = a[q >> sj.log2G];
+    }
+    if (tid == 0) *sj.ok0 = pivots_ok(s_min[0], s_max[0], sj.rcond_min) ? 1 : 0;
+}
+
+cudaError_t launch_start(const StartJob* jobs, int njobs, cudaStream_t stream) {
+    if (njobs <= 0) return cudaSuccess;
+    start_kernel<1024><<<njobs, 1024, 0, stream>>>(jobs);
+    return cudaGetLastError();
+}
+
+size_t start_bytes(int n, int nv, int nblk, int G, bool mixed) {
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t blk = mixed ? 16 : 32, nf = (size_t)nblk + nv, rows = (size_t)(nv > 0 ? nv : 1);
+    return up(rows * 16) + up(nf * blk) + up(nf * blk * G) + up(rows * 16) + up((size_t)n * 16) + up((size_t)n * 8) +
+           up((size_t)n * 4) + up(4);
+}
+
+void start_carve(StartJob& sj, char* base, int n, int nv, int nblk, int G, bool mixed) {
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t blk = mixed ? 16 : 32, nf = (size_t)nblk + nv, rows = (size_t)(nv > 0 ? nv : 1);
+    size_t at = 0;
+    auto take = [&](size_t b) {
+        char* p = base + at;
+        at += up(b);
+        return p;
+    };
+    sj.R0 = reinterpret_cast<double2*>(take(rows * 16));
+    sj.fac1 = take(nf * blk);
+    sj.facG = take(nf * blk * G);
+    sj.y0 = reinterpret_cast<double2*>(take(rows * 16));
+    sj.Et0 = reinterpret_cast<double2*>(take((size_t)n * 16));
+    sj.Ei0 = reinterpret_cast<double*>(take((size_t)n * 8));
+    sj.iv0 = reinterpret_cast<float*>(take((size_t)n * 4));
+    sj.ok0 = reinterpret_cast<int*>(take(4));
 }
 
 cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_bus, double4_32a* fac, double2* R,

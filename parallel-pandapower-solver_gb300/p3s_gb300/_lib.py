@@ -71,6 +71,7 @@ class Stats(C.Structure):
         ("call_ms", C.c_double),
         ("threads_per_cta", C.c_int),
         ("chord_steps", C.c_ulonglong),
+        ("first_steps", C.c_ulonglong),
     ]
 
 

@@ -466,12 +466,36 @@ def test_chord_polish_steps_keep_the_solution(grid2000):
         st = s.stats
         assert r["converged"].all()
         steps = int(r["iterations"].sum())
-        # every step one float factorization, chord step or double factorization (a rejected
-        # float factorization is redone in double in the same step)
-        assert (st["single_factorizations"] + st["double_factorizations"] + st["chord_steps"]
+        # every step one float factorization, chord step, first step with the shared start's
+        # factors or double factorization (a rejected float factorization is redone in double
+        # in the same step)
+        assert (st["single_factorizations"] + st["double_factorizations"] + st["chord_steps"] + st["first_steps"]
                 == steps + st["single_rejected"])
+        assert st["first_steps"] == 256  # every case starts from the shared V0
         assert (st["chord_steps"] == 0) == (ct == 0.0)
         assert np.abs(r["V"] - ref["V"]).max() < 1e-9  # tolerance: mixed path vs converged oracle
         assert (_mismatch(g, r["V"][:, :8], S[:, :8]) <= 1e-8).all()
         out[ct] = r
     assert (out[1e-8]["iterations"] <= out[0.0]["iterations"] + 1).all()
+
+
+def test_shared_start_equals_each_case_starting_on_its_own(grid2000):
+    """Cases that all start from one V0 take their first step with that start's injections and
+    factors, computed once per launch (stats["first_steps"]); the result is, bit for bit, what
+    every case gets from its own copy of V0 (its own first evaluation and factorization)."""
+    from p3s_gb300.solver import GpuSolver
+
+    g = grid2000
+    T = 64
+    S = timeseries_injections(g, T)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    own_V0 = np.ascontiguousarray(np.repeat(g.V0[:, None], T, axis=1))
+    for prec in ("mixed", "double"):
+        p = GpuSolver.params(precision=prec)
+        shared = s.solve_batch(S, g.V0, p)
+        assert s.stats["first_steps"] == T
+        own = s.solve_batch(S, own_V0, p)
+        assert s.stats["first_steps"] == 0
+        assert np.array_equal(shared["iterations"], own["iterations"])
+        assert np.array_equal(shared["V"], own["V"])
+        assert shared["converged"].all()
