@@ -45,6 +45,11 @@ typedef struct gbpf_params {
                             (1e-8 p.u.: the polish steps), the next step reuses the float factors it
                             was solved with (a chord step: substitutions only, no factorization) for
                             as long as each such step cuts the mismatch tenfold; 0: always refactor */
+    int shared_start;    /* 1: a batch of at least 16 cases that all start from one V0 on the base
+                            Ybus without pins evaluates and factors that start once (a one-CTA
+                            prologue) and every case's first step solves with it -- for bulk
+                            batches; 0: every case evaluates and factors its own start (no
+                            prologue on the launch's critical path: latency-bound serving) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */

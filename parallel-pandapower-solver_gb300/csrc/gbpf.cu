@@ -455,6 +455,7 @@ gbpf_params default_params() {
     p.polish = 1e-3;
     p.vtol = 1e-8;
     p.chord_tol = 1e-8;
+    p.shared_start = 1;
     return p;
 }
 
@@ -464,6 +465,9 @@ int check_params(const gbpf_params& p, const char* who) {
     if (p.precision != 0 && p.precision != 1) return fail(std::string(who) + ": precision must be 0 (double) or 1 (mixed)");
     return 0;
 }
+
+// A shared start pays for its one-CTA prologue only over enough cases starting from it.
+constexpr long long SHARE_MIN_CASES = 16;
 
 // The launch of `units` work items (cases, or lanes) enqueued on a stream with its own
 // scratch and control block; read back with finish_launch.
@@ -496,7 +500,8 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     b.err = reinterpret_cast<int*>(ctl + 24);
     // shared start: every case from the same V0 on the base Ybus without pins -- its first
     // evaluation and factorization are computed once (start_kernel) for the whole launch
-    const bool share = b.v0_shared && b.ymode == 0 && !b.pin && !b.ref_bus && (!b.mixed || b.vote_rule == 1);
+    const bool share = b.share_ok && units >= SHARE_MIN_CASES && b.v0_shared && b.ymode == 0 && !b.pin && !b.ref_bus &&
+                       (!b.mixed || b.vote_rule == 1);
     gbpf::StartJob sj{};
     const size_t tab_bytes = ((size_t)s->n * 64 + 255) & ~(size_t)255;
     if (b.v0_shared) {
@@ -609,6 +614,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     // chord steps belong to the GB300 rule's float cases only (the double path refactors every
     // step like nr_klu)
     b.chord_tol = b.mixed && b.vote_rule == 1 && p.chord_tol > 0.0 ? p.chord_tol : 0.0;
+    b.share_ok = p.shared_start != 0;
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
@@ -688,14 +694,28 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         return wa > wb;
     });
     std::vector<gbpf::Job> hj(nj);
+    std::vector<gbpf::StartJob> hs;  // shared starts (their pivot bound is set with the batch)
+    std::vector<int> hs_batch;
     unsigned long long cta_bytes = 0;
     long long want = 0;
     int occ = 1 << 20;
     size_t tab_bytes = 0, isl_bytes = 0;
     auto up256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    // a job whose cases all start from one V0 on the base Ybus without pins gets a shared start
+    // (its first evaluation and factorization once, start_kernel)
+    auto job_slots_of = [&](const gbpf_job& J) {
+        return J.cases_per_cta ? J.cases_per_cta : job_slots(Gmax, J.solver->plan.nv, g->slot_budget);
+    };
+    auto shares = [&](const gbpf_job& J) {
+        return p.shared_start && J.n_cases >= SHARE_MIN_CASES && !J.v0_per_col && !J.st_ptr && !J.out_ptr && !J.pin &&
+               (!mixed || p.vote_rule == 1);
+    };
     for (int j = 0; j < nj; ++j) {
         const gbpf_job& J = jobs[j];
-        tab_bytes += J.v0_per_col ? 0 : (size_t)J.solver->n * 64;
+        tab_bytes += J.v0_per_col ? 0 : up256((size_t)J.solver->n * 64);
+        if (shares(J))
+            tab_bytes += up256(gbpf::start_bytes(J.solver->n, J.solver->plan.nv, J.solver->plan.nblk, job_slots_of(J),
+                                                 mixed));
         if (J.out_ptr) {
             const size_t n = J.solver->n, L = J.n_cases, gi = std::min<size_t>(L, 4 * (size_t)g->nsm);
             isl_bytes += 3 * up256(n * L * 4) + up256(L * 4) + up256(gi * 4 * n * 4) + up256(gi * n * 8);
@@ -720,7 +740,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         const int j = order[q];
         const gbpf_job& J = jobs[j];
         gbpf_solver* s = J.solver;
-        const int G = J.cases_per_cta ? J.cases_per_cta : job_slots(Gmax, s->plan.nv, g->slot_budget);
+        const int G = job_slots_of(J);
         Shape* sh = nullptr;
         if (int rc = get_shape(s, NT, G, &sh)) return rc;
         occ = std::min(occ, sh->occ);
@@ -741,7 +761,23 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         b.sV0 = J.n_cases;
         if (b.v0_shared) {
             b.v0tab = reinterpret_cast<double4_32a*>(g->btab.as<char>() + tab_at);
-            tab_at += (size_t)s->n * 64;
+            tab_at += up256((size_t)s->n * 64);
+        }
+        if (shares(J)) {
+            Shape* s1 = nullptr;
+            if (int rc = get_shape(s, 1024, 1, &s1)) return rc;
+            gbpf::StartJob sj{};
+            sj.P = s1->dp;
+            sj.v0tab = b.v0tab;
+            sj.mixed = mixed;
+            sj.log2G = ilog2(G);
+            gbpf::start_carve(sj, g->btab.as<char>() + tab_at, s->n, s->plan.nv, s->plan.nblk, G, mixed);
+            tab_at += up256(gbpf::start_bytes(s->n, s->plan.nv, s->plan.nblk, G, mixed));
+            b.R0 = sj.R0;
+            b.fac0 = sj.facG;
+            b.ok0 = sj.ok0;
+            hs.push_back(sj);
+            hs_batch.push_back(q);
         }
         if (J.pin) {
             b.pin = J.pin;
@@ -788,10 +824,18 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         b.err = reinterpret_cast<int*>(c + 24);
         o.B = b;
     }
+    for (size_t k = 0; k < hs.size(); ++k) {
+        const gbpf::Batch& b = hj[hs_batch[k]].B;
+        hs[k].rcond_min = mixed ? b.rcond_min32 : b.rcond_min64;
+    }
     const int grid = grid_size(g->nsm, occ, want, mixed);
     CK(g->scr.ensure((size_t)grid * cta_bytes));
-    CK(g->bjobs.ensure((size_t)nj * sizeof(gbpf::Job)));
+    const size_t jobs_bytes = up256((size_t)nj * sizeof(gbpf::Job));
+    CK(g->bjobs.ensure(jobs_bytes + hs.size() * sizeof(gbpf::StartJob)));
     CK(cudaMemcpyAsync(g->bjobs.p, hj.data(), (size_t)nj * sizeof(gbpf::Job), cudaMemcpyHostToDevice, g->stream));
+    if (!hs.empty())
+        CK(cudaMemcpyAsync(g->bjobs.as<char>() + jobs_bytes, hs.data(), hs.size() * sizeof(gbpf::StartJob),
+                           cudaMemcpyHostToDevice, g->stream));
     gbpf::Launch L{};
     L.jobs = g->bjobs.as<gbpf::Job>();
     L.njobs = nj;
@@ -804,6 +848,9 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
             CK(gbpf::launch_v0_table(b.V0, hj[q].P.n, b.check_v0, const_cast<double4_32a*>(b.v0tab), b.err,
                                      g->stream));
     }
+    if (!hs.empty())
+        CK(gbpf::launch_start(reinterpret_cast<const gbpf::StartJob*>(g->bjobs.as<char>() + jobs_bytes),
+                              (int)hs.size(), g->stream));
     for (const IslLaunch& il : isl) {
         const gbpf_solver* s = il.s;
         CK(gbpf::launch_islands(s->n, s->m, s->dbr_f.as<int>(), s->dbr_t.as<int>(), s->dbr_live.as<uint8_t>(),

@@ -108,6 +108,7 @@ struct Batch {
     const double2* R0;       // -(P, Q) at V0 per block row (0 for a PV row's Q)
     const void* fac0;        // factors of J(V0), one copy per case slot: [blk][slot], float4 / double4
     const int* ok0;          // 1 when the shared factorization passed its pivot check
+    int share_ok;            // the caller allows a shared start (gbpf_params.shared_start)
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch

@@ -36,6 +36,7 @@ class Params(C.Structure):
         ("polish", C.c_double),
         ("vtol", C.c_double),
         ("chord_tol", C.c_double),
+        ("shared_start", C.c_int),
     ]
 
 

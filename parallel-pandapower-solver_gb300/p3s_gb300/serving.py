@@ -124,6 +124,8 @@ class Server:
                  max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
                  **solver_params):
         self.topos = topologies
+        # no shared-start prologue ahead of a request's launch: latency first
+        solver_params.setdefault("shared_start", False)
         self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
         self.mixed = precision == "mixed"
         self.groups = [GpuGroup() for _ in range(max(1, contexts))]
