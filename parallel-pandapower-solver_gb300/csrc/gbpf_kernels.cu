@@ -1316,24 +1316,30 @@ __global__ void __launch_bounds__(NTB, 1) start_kernel(const StartJob* jobs) {
     else
         lu_pass<double>(P, reinterpret_cast<double4_32a*>(sj.fac1), sj.R0, sj.y0, s_on, 0, s_min, s_max, nullptr, true,
                         nullptr);
-    // replicate to every slot: [blk] -> [blk][slot]
-    const int G = 1 << sj.log2G;
-    const long long nb = (long long)P.nblk + P.nv;
-    if (sj.mixed) {
-        const float4* a = reinterpret_cast<const float4*>(sj.fac1);
-        float4* b = reinterpret_cast<float4*>(sj.facG);
-        for (long long q = tid; q < nb * G; q += NTB) b[q] = a[q >> sj.log2G];
-    } else {
-        const double4_32a* a = reinterpret_cast<const double4_32a*>(sj.fac1);
-        double4_32a* b = reinterpret_cast<double4_32a*>(sj.facG);
-        for (long long q = tid; q < nb * G; q += NTB) b[q] = a[q >> sj.log2G];
-    }
     if (tid == 0) *sj.ok0 = pivots_ok(s_min[0], s_max[0], sj.rcond_min) ? 1 : 0;
+}
+
+// The start's factors copied to every case slot ([blk] -> [blk][slot]) by the whole device:
+// blockIdx.y is the start, x and threads stride over its 16-byte words.
+__global__ void replicate_kernel(const StartJob* jobs) {
+    const StartJob& sj = jobs[blockIdx.y];
+    const long long nb = (long long)sj.P.nblk + sj.P.nv;
+    const int wpb = sj.mixed ? 1 : 2;  // 16-byte words per block
+    const long long words = nb * wpb << sj.log2G;
+    const float4* a = reinterpret_cast<const float4*>(sj.fac1);
+    float4* b = reinterpret_cast<float4*>(sj.facG);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < words; q += (long long)gridDim.x * blockDim.x) {
+        const long long blk = (q / wpb) >> sj.log2G, part = q % wpb;
+        b[q] = a[blk * wpb + part];
+    }
 }
 
 cudaError_t launch_start(const StartJob* jobs, int njobs, cudaStream_t stream) {
     if (njobs <= 0) return cudaSuccess;
     start_kernel<1024><<<njobs, 1024, 0, stream>>>(jobs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    replicate_kernel<<<dim3(256, njobs), 256, 0, stream>>>(jobs);
     return cudaGetLastError();
 }
 
