@@ -419,7 +419,8 @@ def run_serving(args):
         srv = Server(topos, precision=prec, contexts=4)
         srv.warmup(cases=64)
         sweep = []
-        for rate in (25, 50, 100, 200, 400, 800, 1600):
+        # rates in steps of sqrt(2) from 200 req/s, where the 50 ms bound starts to bind
+        for rate in (25, 50, 100, 200, 280, 400, 560, 800, 1130, 1600):
             reqs = poisson_stream(topos, rate=float(rate), duration=args.serve_seconds, seed=rate)
             s = latency_summary(srv.run(reqs))
             sweep.append({"rate_per_s": rate, **{k: (round(v, 3) if isinstance(v, float) else v) for k, v in s.items()}})
