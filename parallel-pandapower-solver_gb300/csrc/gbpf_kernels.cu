@@ -764,10 +764,14 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         if (!alive) break;
 
         // ---------------------------------------------------------------- load
+        // The start goes to buffer 0 (a fresh case's committed point); buffer 1 gets it only at
+        // slack buses, which no step rewrites -- every other bus's first trial is written to
+        // buffer 1 before anything reads it.
         for (int idx = tid; idx < nG; idx += NT) {
             const int s = idx & (G - 1);
             if (s_st[s] != SL_FRESH) continue;
             const int bus = idx >> lg;
+            const bool fixed = P.row_of_bus[bus] < 0;
             const int c = s_case[s];
             if (s_warm[s]) {
                 // previous hour of the lane converged here: its evaluated state is the start point
@@ -775,7 +779,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 // shared start: the state table built once per launch (v0_table_kernel)
                 const double4_32a t0 = Bt.v0tab[2 * bus], t1 = Bt.v0tab[2 * bus + 1];
                 Vb0[idx] = t0;
-                Vb1[idx] = t0;
+                if (fixed) Vb1[idx] = t0;
                 Et[idx] = make_double2(t1.x, t1.y);
                 Ei[idx] = t1.z;
                 iv32[idx] = d2f_fast(t1.z);
@@ -799,7 +803,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 sincos(va, &sn, &cs);
                 const double4_32a v = make_double4_32a(vm, va, cs, sn);
                 Vb0[idx] = v;
-                Vb1[idx] = v;
+                if (fixed) Vb1[idx] = v;
                 const double e = vm * cs, f = vm * sn, iv = 1.0 / vm;
                 Et[idx] = make_double2(e, f);
                 Ei[idx] = iv;
@@ -831,7 +835,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                         }
                     }
                     Vb0[idx] = v;
-                    Vb1[idx] = v;
+                    if (fixed) Vb1[idx] = v;
                     const double e = v.x * v.z, f = v.x * v.w;
                     Et[idx] = make_double2(e, f);
                     Ei[idx] = iv;
