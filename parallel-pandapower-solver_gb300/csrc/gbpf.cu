@@ -109,10 +109,10 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
 // and the factorization schedule dealt to its NT / G workers (built on first use).
 struct Shape {
     int NT = 0, G = 0, lg = 0, occ = 1;
-    DBuf dtaskA, dptrA, dscl, dptrB, dtaskC, dptrC, dheadA, dheadC, dtaskF, dheadF, dptrF;
+    DBuf dtaskA, dptrA, dtaskC, dptrC, dheadA, dheadC, dtaskF, dheadF, dptrF;
     gbpf::DevPlan dp{};
     ~Shape() {
-        for (DBuf* b : {&dtaskA, &dptrA, &dscl, &dptrB, &dtaskC, &dptrC, &dheadA, &dheadC, &dtaskF, &dheadF, &dptrF})
+        for (DBuf* b : {&dtaskA, &dptrA, &dtaskC, &dptrC, &dheadA, &dheadC, &dtaskF, &dheadF, &dptrF})
             b->release();
     }
 };
@@ -367,16 +367,12 @@ int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     CK(upload(sh->dptrF, ptrF));
     CK(upload(sh->dtaskA, sc.taskA));
     CK(upload(sh->dptrA, sc.ptrA));
-    CK(upload(sh->dscl, sc.scl));
-    CK(upload(sh->dptrB, sc.ptrB));
     CK(upload(sh->dtaskC, sc.taskC));
     CK(upload(sh->dptrC, sc.ptrC));
     sh->dp = s->dp;
     sh->dp.W = sc.W;
     sh->dp.taskA = sh->dtaskA.as<int4>();
     sh->dp.ptrA = sh->dptrA.as<int>();
-    sh->dp.scl = sh->dscl.as<int2>();
-    sh->dp.ptrB = sh->dptrB.as<int>();
     sh->dp.taskC = sh->dtaskC.as<int4>();
     sh->dp.ptrC = sh->dptrC.as<int>();
     sh->dp.headA = sh->dheadA.as<int4>();
@@ -421,8 +417,6 @@ int upload_plan(gbpf_solver* s) {
     d.bus_pq = s->dbus_pq.as<uint8_t>();
     d.taskA = nullptr;
     d.ptrA = nullptr;
-    d.scl = nullptr;
-    d.ptrB = nullptr;
     d.taskC = nullptr;
     d.ptrC = nullptr;
     d.headA = nullptr;

@@ -44,8 +44,6 @@ struct DevPlan {
     const uint8_t* bus_pq;
     const int4* taskA;
     const int* ptrA;
-    const int2* scl;
-    const int* ptrB;
     const int4* taskC;
     const int* ptrC;
     const int4* headA;       // per taskA entry: its first two pairs inline (x0, y0, x1, y1; -1 = none)

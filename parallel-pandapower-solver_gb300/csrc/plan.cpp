@@ -361,7 +361,7 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
 
     // tasks
     const int W = p.W = std::max(1, workers);
-    std::vector<Task> A, B, C;
+    std::vector<Task> A, C;
     p.pairs.clear();
     auto add_pairs_factor = [&](int q, int& p0, int& p1) {
         p0 = (int)(p.pairs.size() / 2);
@@ -418,14 +418,11 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
     }
     if (p.pairs.size() / 2 >= (size_t)1 << 31) return "too many pairs";
     p.tasksA = std::move(A);
-    p.tasksB = std::move(B);
     p.tasksC = std::move(C);
     Schedule sc;
     make_schedule(p, W, sc);
     p.taskA = std::move(sc.taskA);
     p.ptrA = std::move(sc.ptrA);
-    p.scl = std::move(sc.scl);
-    p.ptrB = std::move(sc.ptrB);
     p.taskC = std::move(sc.taskC);
     p.ptrC = std::move(sc.ptrC);
     p.level_work = std::move(sc.level_work);
@@ -442,7 +439,6 @@ void make_schedule(const Plan& p, int workers, Schedule& out) {
         keyA[i] = (t.code & 3) == TK_FWD ? p.base[t.dst] : t.dst;
     }
     layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true, &keyA);
-    layout(p.tasksB, p.nlev, W, out.scl, out.ptrB, nullptr, false);
     std::vector<int> keyC(p.tasksC.size());
     for (size_t i = 0; i < p.tasksC.size(); ++i) keyC[i] = p.tasksC[i].dst;
     layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true, &keyC);
@@ -565,16 +561,6 @@ bool host_factor(const Plan& p, double* blk, double* pmin, double* pmax) {
                 }
             }
         }
-        for (int w = 0; w < W; ++w)
-            for (int t = p.ptrB[(size_t)h * W + w]; t < p.ptrB[(size_t)h * W + w + 1]; ++t) {
-                double* l = blk + 4 * (size_t)p.scl[2 * t];
-                const double* d = blk + 4 * (size_t)p.scl[2 * t + 1];
-                const double a0 = l[0], a1 = l[1], a2 = l[2], a3 = l[3];
-                l[0] = a0 * d[0] + a1 * d[2];
-                l[1] = a0 * d[1] + a1 * d[3];
-                l[2] = a2 * d[0] + a3 * d[2];
-                l[3] = a2 * d[1] + a3 * d[3];
-            }
     }
     *pmin = mn;
     *pmax = mx;
@@ -611,13 +597,13 @@ void host_solve(const Plan& p, const double* blk, double* y) {
 namespace gbpf {
 
 // Serial execution of the device schedule (factor levels with the forward substitution in
-// the entry phase, scale phase, backward levels) in double precision, and a structural
+// the factor levels, backward levels) in double precision, and a structural
 // check that no task of a level reads what another task of the same phase writes.
 std::string schedule_selftest(const Plan& p, double* blk, const double* R, double* y) {
     const int W = p.W;
     std::vector<int> wstamp((size_t)p.nblk + p.nv, -1), ystamp(std::max(p.nv, 1), -1);
     for (int h = 0; h < p.nlev; ++h) {
-        // structural: writes of the entry phase
+        // structural: writes of the factor level
         for (int w = 0; w < W; ++w)
             for (int t = p.ptrA[(size_t)h * W + w]; t < p.ptrA[(size_t)h * W + w + 1]; ++t) {
                 const int* T = &p.taskA[4 * (size_t)t];
@@ -641,7 +627,7 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                     if (fwd && ystamp[b] == h) return "level " + std::to_string(h) + ": forward row reads a row of its level";
                 }
             }
-        // execute the entry phase in reverse worker order (any order must give the same result)
+        // execute the level in reverse worker order (any order must give the same result)
         for (int w = W - 1; w >= 0; --w) {
             double dinv[4] = {0, 0, 0, 0};
             int dinv_level = -1;
@@ -694,16 +680,6 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
                 }
             }
         }
-        for (int w = W - 1; w >= 0; --w)
-            for (int t = p.ptrB[(size_t)h * W + w]; t < p.ptrB[(size_t)h * W + w + 1]; ++t) {
-                double* l = blk + 4 * (size_t)p.scl[2 * t];
-                const double* d = blk + 4 * (size_t)p.scl[2 * t + 1];
-                const double a0 = l[0], a1 = l[1], a2 = l[2], a3 = l[3];
-                l[0] = a0 * d[0] + a1 * d[2];
-                l[1] = a0 * d[1] + a1 * d[3];
-                l[2] = a2 * d[0] + a3 * d[2];
-                l[3] = a2 * d[1] + a3 * d[3];
-            }
     }
     std::vector<int> bst(std::max(p.nv, 1), -1);
     for (int h = 0; h < p.nblev; ++h) {

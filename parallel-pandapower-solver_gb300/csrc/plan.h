@@ -50,7 +50,6 @@ struct PlanTask {
 struct Schedule {
     int W = 0;
     std::vector<int> taskA, ptrA;   // entry tasks (4 ints) and per-(level, worker) ranges
-    std::vector<int> scl, ptrB;     // L scalings (2 ints; empty: L blocks are scaled in their column chain)
     std::vector<int> taskC, ptrC;   // backward substitution tasks (4 ints)
     std::vector<int> level_work;    // per level: max worker load
 };
@@ -81,13 +80,11 @@ struct Plan {
     int nlev = 0, nblev = 0;
     std::vector<int> taskA;         // 4 ints per task: dst, kind|flags, p0, p1
     std::vector<int> ptrA;          // nlev*W + 1
-    std::vector<int> scl;           // 2 ints: L block, diagonal block
-    std::vector<int> ptrB;          // nlev*W + 1
     std::vector<int> taskC;         // backward: 4 ints: row, inverse-diagonal block, p0, p1
     std::vector<int> ptrC;          // nblev*W + 1
     std::vector<int> pairs;         // 2 ints per pair
-    // undealt tasks (entry, scale, backward), kept so other worker counts can be scheduled
-    std::vector<PlanTask> tasksA, tasksB, tasksC;
+    // undealt tasks (factor levels, backward), kept so other worker counts can be scheduled
+    std::vector<PlanTask> tasksA, tasksC;
     // statistics
     long long n_factor_pairs = 0, n_fwd_pairs = 0, n_bwd_pairs = 0;
     double rcond0 = 0.0;            // pivot ratio of the flat-start factorization
