@@ -229,7 +229,7 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
 /* Device arrays (every pointer of every job on the device). */
 int gbpf_group_solve_device(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_params* p);
 /* Launch shape of later group launches: threads per CTA (0: by the batch-size rule) and the
- * budget of variable buses x case slots a CTA holds per job (0: 8,192). */
+ * budget of variable buses x case slots a CTA holds per job (0: 16,384). */
 int gbpf_group_set_shape(gbpf_group* g, int threads_per_cta, int slot_budget);
 /* Counters of the last group launch (summed over its jobs). */
 int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);

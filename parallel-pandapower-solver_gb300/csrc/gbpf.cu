@@ -616,7 +616,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
 
 // Shape rule for a launch over several topologies: threads per CTA by the batch-size rule of
 // choose_shape on the total work; case slots per CTA per job: the batch-size rule's count,
-// reduced for large topologies so that a job's CTA holds at most `slot_budget` (8,192)
+// reduced for large topologies so that a job's CTA holds at most `slot_budget` (16,384)
 // variable buses' worth of cases -- a large grid's cases then get many workers each, and
 // they set the launch's critical path (measured on GB300, 256 grids of 30..19,423 buses x 16
 // scenarios: one slot per CTA for the largest grids halves the launch).
@@ -646,7 +646,8 @@ struct gbpf_group {
     DBuf scr, bjobs, bctl, btab, bin, bout, bisl;
     gbpf_stats last{};
     int fixed_NT = 0;              // threads per CTA (0: by the group rule)
-    int slot_budget = 8192;        // variable buses x case slots a CTA may hold per job
+    int slot_budget = 16384;       // variable buses x case slots a CTA may hold per job (measured best on the
+                                   // 256-grid batch: 8,192 +5 %, 32,768 +8 % time)
     ~gbpf_group() {
         for (DBuf* b : {&scr, &bjobs, &bctl, &btab, &bin, &bout, &bisl}) b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
@@ -1663,7 +1664,7 @@ int gbpf_group_set_shape(gbpf_group* g, int threads_per_cta, int slot_budget) {
         return fail("group_set_shape: threads_per_cta must be 0, 256, 512 or 1024");
     if (slot_budget < 0) return fail("group_set_shape: slot_budget must be >= 0");
     g->fixed_NT = threads_per_cta;
-    g->slot_budget = slot_budget ? slot_budget : 8192;
+    g->slot_budget = slot_budget ? slot_budget : 16384;
     return 0;
 }
 

@@ -56,7 +56,7 @@ class GpuGroup:
 
     def set_shape(self, threads_per_cta: int = 0, slot_budget: int = 0):
         """Threads per CTA of later launches (0: by batch size) and the variable buses x case
-        slots a CTA may hold per job (0: 8,192)."""
+        slots a CTA may hold per job (0: 16,384)."""
         _lib.check(_lib.load().gbpf_group_set_shape(self._h, int(threads_per_cta), int(slot_budget)),
                    "gbpf_group_set_shape")
 

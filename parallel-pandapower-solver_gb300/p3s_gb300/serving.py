@@ -62,10 +62,13 @@ class Response:
 
 
 def _slot_bytes(n: int, nv: int, nblk: int, mixed: bool) -> int:
-    """Device bytes of one case slot (the kernel's per-slot scratch)."""
-    b = nblk * 32 + nv * 32 + n * (32 + 32 + 16 + 8 + 16 + 1)
+    """Device bytes of one case slot (the kernel's per-slot scratch, gbpf::scratch_offsets):
+    double factors and inverse diagonals, residual and step, two state buffers, (e, f), 1/Vm in
+    double and float, pins; mixed: two float factor buffers and the float step."""
+    nf = nblk + nv
+    b = nf * 32 + nv * 32 + n * (32 + 32 + 16 + 8 + 4 + 1)
     if mixed:
-        b += nblk * 16 + nv * 8
+        b += 2 * nf * 16 + nv * 8
     return b
 
 
