@@ -482,6 +482,11 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     const int grid = grid_size(s->nsm, sh->occ, (units + G - 1) / G, b.mixed != 0);
     gbpf::Job job{};
     job.P = sh->dp;
+    // the one-slot schedule for a CTA's last case (solo passes)
+    Shape* sh1 = sh;
+    if (G > 1)
+        if (int rc = get_shape(s, NT, 1, &sh1)) return rc;
+    job.P1 = sh1->dp;
     job.off = solver_offsets(s, G, b.mixed != 0);
     job.G = G;
     job.log2G = ilog2(G);
@@ -741,6 +746,10 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         occ = std::min(occ, sh->occ);
         gbpf::Job& o = hj[q];
         o.P = sh->dp;
+        Shape* sh1 = sh;
+        if (G > 1)
+            if (int rc = get_shape(s, NT, 1, &sh1)) return rc;
+        o.P1 = sh1->dp;
         o.off = solver_offsets(s, G, mixed);
         o.G = G;
         o.log2G = ilog2(G);

@@ -138,6 +138,7 @@ struct ScratchOffsets {
 // batch of its cases, and where its scratch sits in a CTA's region.
 struct Job {
     DevPlan P;
+    DevPlan P1;              // the same topology with the one-slot schedule of the launch's CTA size
     Batch B;
     ScratchOffsets off;
     int G, log2G;            // case slots per CTA for this job (the schedule has NT / G workers)

@@ -350,19 +350,22 @@ __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
 // One batched factorization + substitution pass over the slots flagged in `on` (G <= 32).
 // Worker w = (warp, lane / G) runs its task list of every level for its G slot lanes;
 // the CTA meets at a barrier after each level, forward and backward. Pivot statistics per
-// slot go to smin / smax (as ordered bits). Slots flagged in `chord` keep the factors already
+// slot go to smin / smax (as ordered bits). With `solo` a slot index, P is the one-slot
+// schedule and all threads work on that slot. Slots flagged in `chord` keep the factors already
 // in `fac` and run the substitutions only; when every slot of the CTA does (factor_any false),
 // the workers walk the substitution-only lists instead of skipping factor tasks one by one.
 template <typename real>
 __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
                         const int* on, int lg, unsigned long long* smin, unsigned long long* smax,
-                        const int* chord, bool factor_any, typename V4<real>::t* dinv_smem) {
+                        const int* chord, bool factor_any, typename V4<real>::t* dinv_smem, int solo = -1) {
     using B4 = typename V4<real>::t;
     using B2 = typename V4<real>::t2;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const int s = lane & ((1 << lg) - 1);
-    const int w = (tid >> 5) * (32 >> lg) + (lane >> lg);
+    // solo >= 0: one slot left in the CTA; P then carries the one-slot schedule (a worker per
+    // thread) and every thread works on that slot
+    const int s = solo >= 0 ? solo : lane & ((1 << lg) - 1);
+    const int w = solo >= 0 ? tid : (tid >> 5) * (32 >> lg) + (lane >> lg);
     const int W = P.W;
     const bool act = on[s] != 0;
     const bool factor = !(chord && chord[s]);
@@ -592,7 +595,9 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     const int NT = blockDim.x;
     char* const region = L.scratch + (size_t)blockIdx.x * L.cta_bytes;
     __shared__ DevPlan s_plan;
+    __shared__ DevPlan s_plan1;  // the same topology with the one-slot schedule (solo passes)
     __shared__ Batch s_batch;
+    __shared__ int s_solo;
     __shared__ double4_32a s_dinv64[NTB];  // double passes: each worker's inverse diagonal (off the registers)
     __shared__ int s_job;
     int next_job = 0;  // thread 0: first job this CTA has not finished yet
@@ -621,6 +626,9 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         src = reinterpret_cast<const int*>(&L.jobs[job].B);
         dst = reinterpret_cast<int*>(&s_batch);
         for (int w = tid; w < (int)(sizeof(Batch) / 4); w += NT) dst[w] = src[w];
+        src = reinterpret_cast<const int*>(&L.jobs[job].P1);
+        dst = reinterpret_cast<int*>(&s_plan1);
+        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = src[w];
     }
     const ScratchOffsets& off = L.jobs[job].off;
     const int G = L.jobs[job].G, lg = L.jobs[job].log2G;  // case slots of this job's CTAs
@@ -760,14 +768,22 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             }
             if (s_st[s] == SL_ACTIVE) s_it[s] += 1;
         }
-        const int alive = __syncthreads_or(tid < G && s_st[tid] != SL_RETIRED);
+        if (tid == 0) s_solo = -1;
+        const int alive = __syncthreads_count(tid < G && s_st[tid] != SL_RETIRED);
         if (!alive) break;
+        // one case left in the CTA (its tail): every thread works on that slot this pass
+        if (alive == 1 && G > 1 && tid < G && s_st[tid] != SL_RETIRED) s_solo = tid;
+        __syncthreads();
+        // (read from shared memory where used: no register held across the pass)
+        const int& solo = s_solo;
+        auto nloop = [&]() { return s_solo >= 0 ? n : nG; };  // loop items of the per-bus phases
 
         // ---------------------------------------------------------------- load
         // The start goes to buffer 0 (a fresh case's committed point); buffer 1 gets it only at
         // slack buses, which no step rewrites -- every other bus's first trial is written to
         // buffer 1 before anything reads it.
-        for (int idx = tid; idx < nG; idx += NT) {
+        for (int k = tid; k < nloop(); k += NT) {
+            const int idx = solo >= 0 ? (k << lg) + solo : k;
             const int s = idx & (G - 1);
             if (s_st[s] != SL_FRESH) continue;
             const int bus = idx >> lg;
@@ -866,10 +882,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             {
                 // a slot factors the Jacobian in the buffer its last factors are not in; a chord
                 // step solves with those factors, a first step with the shared start's
-                const int sl = (tid & 31) & (G - 1);
+                const int sl = solo >= 0 ? solo : (tid & 31) & (G - 1);
                 const int buf = s_chord[sl] ? s_fb[sl] : 1 - s_fb[sl];
                 float4* const fl = s_first[sl] ? (float4*)Bt.fac0 : (buf ? fac32b : fac32);
-                lu_pass<float>(P, fl, R, y32, s_on32, lg, s_pmin, s_pmax, s_nofac, !all_chord, nullptr);
+                lu_pass<float>(solo >= 0 ? s_plan1 : P, fl, R, y32, s_on32, lg, s_pmin, s_pmax, s_nofac, !all_chord,
+                               nullptr, solo);
             }
             if (tid < G && s_on32[tid]) {
                 const int s = tid;
@@ -916,11 +933,13 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             if (s_share) {
                 // no double slot of the CTA factors (all take their first step): substitutions only
                 const int all_first = __syncthreads_and(!(tid < G && s_on64[tid]) || s_nofac[tid]);
-                const int sl = (tid & 31) & (G - 1);
+                const int sl = solo >= 0 ? solo : (tid & 31) & (G - 1);
                 double4_32a* const fd = s_first[sl] ? (double4_32a*)Bt.fac0 : fac64;
-                lu_pass<double>(P, fd, R, y64, s_on64, lg, s_pmin, s_pmax, s_nofac, !all_first, s_dinv64);
+                lu_pass<double>(solo >= 0 ? s_plan1 : P, fd, R, y64, s_on64, lg, s_pmin, s_pmax, s_nofac, !all_first,
+                                s_dinv64, solo);
             } else {
-                lu_pass<double>(P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true, s_dinv64);
+                lu_pass<double>(solo >= 0 ? s_plan1 : P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true,
+                                s_dinv64, solo);
             }
             if (tid < G && s_on64[tid]) {
                 const int s = tid;
@@ -944,10 +963,10 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
 
         // ---------------------------------------------------------------- step
         // A thread's elements idx = tid + k NT all belong to slot tid & (G - 1) (NT is a
-        // multiple of G), so the slot's state is read once and the next element's committed
-        // point and step are loaded while the current one is worked on.
+        // multiple of G) -- or all to the solo slot -- so the slot's state is read once and the
+        // next element's committed point and step are loaded while the current one is worked on.
         {
-            const int s = tid & (G - 1);
+            const int s = solo >= 0 ? solo : tid & (G - 1);
             const int st = s_st[s];
             if (st == SL_ACTIVE || st == SL_BACKTRACK || st == SL_NEEDJ) {
                 const bool active = st == SL_ACTIVE;
@@ -973,15 +992,18 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                         dvm = dd.y;
                     }
                 };
+                const int ksh = solo >= 0 ? lg : 0;  // element k -> idx = (k << ksh) + koff
+                const int koff = solo >= 0 ? solo : 0;
                 int rown = -1;
                 double4_32a vcn = make_double4_32a(0.0, 0.0, 0.0, 0.0);
                 double dthn = 0.0, dvmn = 0.0;
-                if (tid < nG) fetch(tid, rown, vcn, dthn, dvmn);
-                for (int idx = tid; idx < nG; idx += NT) {
+                if (tid < nloop()) fetch((tid << ksh) + koff, rown, vcn, dthn, dvmn);
+                for (int k = tid; k < nloop(); k += NT) {
+                    const int idx = (k << ksh) + koff;
                     const int row = rown;
                     const double4_32a vc = vcn;
                     const double dth = dthn, dvm = dvmn;
-                    if (idx + NT < nG) fetch(idx + NT, rown, vcn, dthn, dvmn);
+                    if (k + NT < nloop()) fetch(((k + NT) << ksh) + koff, rown, vcn, dthn, dvmn);
                     if (row < 0) continue;
                     const int bus = idx >> lg;
                     // trial point (nr_klu.cpp:665-669 form_trial): committed + alpha * step
@@ -1024,11 +1046,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         // ---------------------------------------------------------------- evaluate
         // Buses are swept in reverse Cuthill-McKee order, so the buses a CTA evaluates at the
         // same time share their neighbours' state in cache.
-        for (int idx = tid; idx < nG; idx += NT) {
-            const int s = idx & (G - 1);
+        for (int k = tid; k < nloop(); k += NT) {
+            const int s = solo >= 0 ? solo : k & (G - 1);
             const int st = s_st[s];
             if (st != SL_FRESH && st != SL_ACTIVE && st != SL_NEEDJ && st != SL_BACKTRACK) continue;
-            const int bus = __ldg(&P.eval_order[idx >> lg]);
+            const int bus = __ldg(&P.eval_order[solo >= 0 ? k : k >> lg]);
             const int row = P.row_of_bus[bus];
             if (row < 0) continue;
             const int c = s_case[s];
@@ -1156,7 +1178,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         __syncthreads();
 
         // ---------------------------------------------------------------- write back
-        for (int idx = tid; idx < nG; idx += NT) {
+        for (int k = tid; k < nloop(); k += NT) {
+            const int idx = solo >= 0 ? (k << lg) + solo : k;
             const int s = idx & (G - 1);
             if (s_st[s] != SL_FINISH) continue;
             const int bus = idx >> lg;
