@@ -24,6 +24,7 @@ all host cores) on the same workload.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -422,7 +423,14 @@ def run_serving(args):
         # rates in steps of sqrt(2) from 200 req/s, where the 50 ms bound starts to bind
         for rate in (25, 50, 100, 200, 280, 400, 560, 800, 1130, 1600):
             reqs = poisson_stream(topos, rate=float(rate), duration=args.serve_seconds, seed=rate)
-            s = latency_summary(srv.run(reqs))
+            # the host's garbage collector paused during the stream (a collection over the
+            # bench's large arrays would stall the serving loop for 100s of ms)
+            gc.collect()
+            gc.disable()
+            try:
+                s = latency_summary(srv.run(reqs))
+            finally:
+                gc.enable()
             sweep.append({"rate_per_s": rate, **{k: (round(v, 3) if isinstance(v, float) else v) for k, v in s.items()}})
             if s["p99_ms"] > 50.0:
                 break

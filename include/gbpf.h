@@ -110,6 +110,11 @@ int gbpf_get_stats(gbpf_solver* s, gbpf_stats* out);
  * nr_polar_solver.py:285-300). */
 int gbpf_get_shape(gbpf_solver* s, long long units, int* threads_per_cta, int* cases_per_cta);
 int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cases_per_cta);
+/* Builds, ahead of use, the schedules of every CTA shape a launch of this topology may take
+ * with up to max_cases_per_cta slots (512 threads: 1, 2, 4, ... slots; 1,024: up to 4), so that
+ * no later launch builds one on its critical path (a serving loop's warm-up). No reference
+ * counterpart. */
+int gbpf_prepare_shapes(gbpf_solver* s, int max_cases_per_cta);
 
 /* The solver's current Ybus values (nnz complex), e.g. after gbpf_update_Y_from_branches. */
 int gbpf_get_Y(gbpf_solver* s, double* Yx);

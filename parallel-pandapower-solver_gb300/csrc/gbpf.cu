@@ -985,6 +985,17 @@ int gbpf_get_info(gbpf_solver* s, gbpf_info* o) {
     return 0;
 }
 
+int gbpf_prepare_shapes(gbpf_solver* s, int max_cases_per_cta) {
+    if (!s) return fail("null solver");
+    const int cap = std::max(1, std::min(gbpf::MAX_SLOTS, max_cases_per_cta));
+    for (int NT : {1024, 512})
+        for (int G = 1; G <= (NT == 1024 ? std::min(cap, 4) : cap); G *= 2) {  // 1,024 threads: <= 4 slots
+            Shape* sh = nullptr;
+            if (int rc = get_shape(s, NT, G, &sh)) return rc;
+        }
+    return 0;
+}
+
 int gbpf_get_shape(gbpf_solver* s, long long units, int* threads_per_cta, int* cases_per_cta) {
     if (!s || !threads_per_cta || !cases_per_cta) return fail("null argument");
     if (units <= 0) return fail("get_shape: units must be > 0");

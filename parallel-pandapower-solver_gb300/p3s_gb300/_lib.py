@@ -115,6 +115,7 @@ SIGNATURES = {
     "gbpf_get_Y": (C.c_int, [_vp, _dp]),
     "gbpf_get_shape": (C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gbpf_set_shape": (C.c_int, [_vp, C.c_longlong, C.c_int, C.c_int]),
+    "gbpf_prepare_shapes": (C.c_int, [_vp, C.c_int]),
     "gbpf_get_row_of_bus": (C.c_int, [_vp, _ip]),
     "gbpf_solve_batch": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.POINTER(Params), _dp, _ip, _bp]),
     "gbpf_solve_batch_device": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int, C.POINTER(Params), _vp, _vp,

@@ -120,18 +120,23 @@ class Server:
     """Continuous batching over resident topologies (see the module docstring).
 
     precision: "mixed" or "double"; contexts: launches that may overlap on the device;
-    max_cases: cases per launch; hbm_budget: bytes of case-slot scratch all contexts may hold.
+    max_cases: cases per launch; hbm_budget: bytes of case-slot scratch all contexts may hold;
+    slot_budget: variable buses x case slots a CTA holds per job (smaller than bulk launches':
+    a request's cases spread over more CTAs, which keeps its latency down).
     """
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", contexts: int = 2,
                  max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
-                 **solver_params):
+                 slot_budget: int = 8192, **solver_params):
         self.topos = topologies
         # no shared-start prologue ahead of a request's launch: latency first
         solver_params.setdefault("shared_start", False)
         self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
         self.mixed = precision == "mixed"
         self.groups = [GpuGroup() for _ in range(max(1, contexts))]
+        self.slot_budget = slot_budget
+        for grp in self.groups:  # fewer case slots per CTA than bulk launches: more CTAs per request
+            grp.set_shape(0, slot_budget)
         self.max_cases = max_cases
         self.hbm_budget = hbm_budget
         self._cv = threading.Condition()
@@ -141,6 +146,11 @@ class Server:
         launch before serving, so that no launch allocates device memory (an allocation or
         release synchronises the device and would stall the launches in flight)."""
         big = max(self.topos, key=lambda tp: tp.nblk)
+        for tp in self.topos:  # every shape a request's launch may take (its group's slot rule)
+            g = 1
+            while g * 2 <= 32 and g * 2 * max(1, tp.nv) <= self.slot_budget:
+                g *= 2
+            tp.solver.prepare_shapes(g)
         for grp in self.groups:
             jobs = [GroupJob(tp.solver, tp.grid.Sbus, tp.V_warm, n_cases=1) for tp in self.topos]
             jobs.append(GroupJob(big.solver, big.grid.Sbus, big.V_warm, n_cases=max(cases, 1)))

@@ -101,6 +101,11 @@ class GpuSolver:
         _lib.check(_lib.load().gbpf_get_shape(self._h, int(units), C.byref(nt), C.byref(g)), "gbpf_get_shape")
         return nt.value, g.value
 
+    def prepare_shapes(self, max_cases_per_cta: int = 32):
+        """Build the schedules of every CTA shape a launch may take (512 / 1,024 threads, up to
+        ``max_cases_per_cta`` slots) now rather than on a later launch's critical path."""
+        _lib.check(_lib.load().gbpf_prepare_shapes(self._h, int(max_cases_per_cta)), "gbpf_prepare_shapes")
+
     def set_shape(self, units: int, threads_per_cta: int, cases_per_cta: int):
         """Pin the CTA shape for batches of `units`' size class (0, 0 restores the rule)."""
         _lib.check(_lib.load().gbpf_set_shape(self._h, int(units), int(threads_per_cta), int(cases_per_cta)),
