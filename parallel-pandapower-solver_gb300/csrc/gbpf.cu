@@ -40,13 +40,26 @@ int fail(const std::string& m) {
 struct DBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    // Grows to at least b bytes; a buffer that had to grow takes half as much again (1 MiB
+    // granules), so that a stream of slowly growing requests reallocates -- and synchronises
+    // the device in cudaFree -- only a few times.
     cudaError_t ensure(size_t b) {
         if (b <= bytes && p) return cudaSuccess;
-        if (p) cudaFree(p);
+        size_t want = std::max<size_t>(b, 16);
+        if (p) {
+            want = std::max(want, bytes + bytes / 2);
+            want = (want + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
+            cudaFree(p);
+        }
         p = nullptr;
         bytes = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(b, 16));
-        if (e == cudaSuccess) bytes = std::max<size_t>(b, 16);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess && want > b) {  // no room for the headroom: exactly what is asked
+            (void)cudaGetLastError();
+            want = std::max<size_t>(b, 16);
+            e = cudaMalloc(&p, want);
+        }
+        if (e == cudaSuccess) bytes = want;
         return e;
     }
     void release() {
