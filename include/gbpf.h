@@ -225,6 +225,8 @@ typedef struct gbpf_job {
     const int32_t* out_ptr;
     const int32_t* out_idx;
     int reslack;
+    uint8_t* served;         /* out, outage jobs: (n, n_cases) 1 where the bus's island is served
+                                (the device islanding's mask, gbpf_islands semantics), or NULL */
 } gbpf_job;
 
 gbpf_group* gbpf_group_create(void);

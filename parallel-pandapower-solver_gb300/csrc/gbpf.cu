@@ -14,6 +14,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -163,6 +164,7 @@ struct gbpf_solver {
     int fixed_NT = 0, fixed_G = 0;               // CTA shape requested at creation (0: by batch size)
     int table_NT[N_SIZE_CLASSES] = {}, table_G[N_SIZE_CLASSES] = {};  // shapes set per size class
     std::vector<std::unique_ptr<Shape>> shapes;
+    std::mutex shapes_mu;  // launches of several groups on this topology may look up shapes at once
     std::vector<std::unique_ptr<ExecSlot>> slots;  // asynchronous calls (gbpf_solve_lanes_async)
     // topology on the device
     DBuf dYp, dYj, dY, dY32, dposmap, drow_of_bus, dbus_pq, dpairs, drow_pq, dbus_of_row, ddpos, deval_order;
@@ -325,6 +327,7 @@ void choose_shape(const gbpf_solver* s, long long units, int* NT, int* G) {
 // The schedule of one CTA shape: tasks dealt to NT / G workers, uploaded next to the
 // shared topology arrays.
 int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
+    std::lock_guard<std::mutex> lock(s->shapes_mu);
     for (auto& sh : s->shapes)
         if (sh->NT == NT && sh->G == G) {
             *out = sh.get();
@@ -691,6 +694,8 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
             if (!J.solver->m) return fail(std::string(who) + ": job " + std::to_string(j) + ": outage cases need the solver's branch table (gbpf_set_branches)");
             if (J.s_per_col || J.v0_per_col || !J.out_idx)
                 return fail(std::string(who) + ": job " + std::to_string(j) + ": outage cases take one S and one V0 (n,) and out_ptr / out_idx");
+        } else if (J.served) {
+            return fail(std::string(who) + ": job " + std::to_string(j) + ": a served mask belongs to outage cases");
         }
         units += J.n_cases;
     }
@@ -875,6 +880,9 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
                                 s->dprio.as<double>(), il.J->reslack, il.scr, il.best, il.labels,
                                 reinterpret_cast<uint8_t*>(il.served_i), il.ref_bus, il.nis, il.err, il.grid,
                                 g->stream));
+        if (il.J->served)
+            CK(cudaMemcpyAsync(il.J->served, il.served_i, (size_t)s->n * il.J->n_cases, cudaMemcpyDeviceToDevice,
+                               g->stream));
     }
     CK(gbpf::launch_newton(L, grid, NT, g->stream));
     CK(cudaEventRecord(g->e1, g->stream));
@@ -1461,6 +1469,7 @@ int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t,
         d.is_slack = s->dslack.as<uint8_t>();
     };
     fill(s->dp);
+    std::lock_guard<std::mutex> lock(s->shapes_mu);
     for (auto& sh : s->shapes) fill(sh->dp);
     return 0;
 }
@@ -1632,7 +1641,7 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
             in_bytes += up((T + 1) * 4) + up((size_t)std::max(J.out_ptr[T], 1) * 4);
         }
         out_at[j] = out_bytes;
-        out_bytes += up(n * T * 16) + up(T * 4) + up(T);
+        out_bytes += up(n * T * 16) + up(T * 4) + up(T) + (J.served ? up(n * T) : 0);
     }
     CK(g->bin.ensure(in_bytes));
     CK(g->bout.ensure(out_bytes));
@@ -1674,6 +1683,7 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
         D.V = reinterpret_cast<double*>(o);
         D.iterations = reinterpret_cast<int32_t*>(o + up(n * T * 16));
         D.converged = reinterpret_cast<uint8_t*>(o + up(n * T * 16) + up(T * 4));
+        if (J.served) D.served = reinterpret_cast<uint8_t*>(o + up(n * T * 16) + up(T * 4) + up(T));
     }
     if (int rc = group_run(g, njobs, dj.data(), p, "group_solve")) return rc;
     for (int j = 0; j < njobs; ++j) {
@@ -1682,6 +1692,7 @@ int gbpf_group_solve(gbpf_group* g, int njobs, const gbpf_job* jobs, const gbpf_
         CK(cudaMemcpyAsync(J.V, dj[j].V, n * T * 16, cudaMemcpyDeviceToHost, g->stream));
         CK(cudaMemcpyAsync(J.iterations, dj[j].iterations, T * 4, cudaMemcpyDeviceToHost, g->stream));
         CK(cudaMemcpyAsync(J.converged, dj[j].converged, T, cudaMemcpyDeviceToHost, g->stream));
+        if (J.served) CK(cudaMemcpyAsync(J.served, dj[j].served, n * T, cudaMemcpyDeviceToHost, g->stream));
     }
     CK(cudaEventRecord(g->c1, g->stream));
     CK(cudaStreamSynchronize(g->stream));

@@ -423,8 +423,13 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         }
                     }
                     int p = task.z + np;
+                    int2 n0 = make_int2(0, 0), n1 = make_int2(0, 0);
+                    if (p < task.w) n0 = __ldg(&P.pairs[p]);
+                    if (p + 1 < task.w) n1 = __ldg(&P.pairs[p + 1]);
                     for (; p + 1 < task.w; p += 2) {
-                        const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                        const int2 q0 = n0, q1 = n1;
+                        if (p + 2 < task.w) n0 = __ldg(&P.pairs[p + 2]);
+                        if (p + 3 < task.w) n1 = __ldg(&P.pairs[p + 3]);
                         const B4 l0 = fac[((size_t)q0.x << lg) + s], l1 = fac[((size_t)q1.x << lg) + s];
                         const B2 u0 = y[((size_t)q0.y << lg) + s], u1 = y[((size_t)q1.y << lg) + s];
                         y0 = fmadd(-l0.y, u0.y, fmadd(-l0.x, u0.x, y0));
@@ -433,7 +438,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         y1 = fmadd(-l1.w, u1.y, fmadd(-l1.z, u1.x, y1));
                     }
                     if (p < task.w) {
-                        const int2 q0 = __ldg(&P.pairs[p]);
+                        const int2 q0 = n0;
                         const B4 l0 = fac[((size_t)q0.x << lg) + s];
                         const B2 u0 = y[((size_t)q0.y << lg) + s];
                         y0 = fmadd(-l0.y, u0.y, fmadd(-l0.x, u0.x, y0));
@@ -456,16 +461,22 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                         mm_sub(acc, a0, b0);
                     }
                 }
+                // the next two pairs' indices are fetched while this iteration's blocks load
                 int p = task.z + np;
+                int2 n0 = make_int2(0, 0), n1 = make_int2(0, 0);
+                if (p < task.w) n0 = __ldg(&P.pairs[p]);
+                if (p + 1 < task.w) n1 = __ldg(&P.pairs[p + 1]);
                 for (; p + 1 < task.w; p += 2) {
-                    const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                    const int2 q0 = n0, q1 = n1;
+                    if (p + 2 < task.w) n0 = __ldg(&P.pairs[p + 2]);
+                    if (p + 3 < task.w) n1 = __ldg(&P.pairs[p + 3]);
                     const B4 a0 = fac[((size_t)q0.x << lg) + s], b0 = fac[((size_t)q0.y << lg) + s];
                     const B4 a1 = fac[((size_t)q1.x << lg) + s], b1 = fac[((size_t)q1.y << lg) + s];
                     mm_sub(acc, a0, b0);
                     mm_sub(acc, a1, b1);
                 }
                 if (p < task.w) {
-                    const int2 q0 = __ldg(&P.pairs[p]);
+                    const int2 q0 = n0;
                     mm_sub(acc, fac[((size_t)q0.x << lg) + s], fac[((size_t)q0.y << lg) + s]);
                 }
                 if (kind == 0) {  // diagonal block: its inverse, kept for the L blocks that follow
@@ -540,8 +551,13 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     }
                 }
                 int p = task.z + np;
+                int2 n0 = make_int2(0, 0), n1 = make_int2(0, 0);
+                if (p < task.w) n0 = __ldg(&P.pairs[p]);
+                if (p + 1 < task.w) n1 = __ldg(&P.pairs[p + 1]);
                 for (; p + 1 < task.w; p += 2) {
-                    const int2 q0 = __ldg(&P.pairs[p]), q1 = __ldg(&P.pairs[p + 1]);
+                    const int2 q0 = n0, q1 = n1;
+                    if (p + 2 < task.w) n0 = __ldg(&P.pairs[p + 2]);
+                    if (p + 3 < task.w) n1 = __ldg(&P.pairs[p + 3]);
                     const B4 u0 = fac[((size_t)q0.x << lg) + s], u1 = fac[((size_t)q1.x << lg) + s];
                     const B2 y0 = y[((size_t)q0.y << lg) + s], y1 = y[((size_t)q1.y << lg) + s];
                     r0 = fmadd(-u0.y, y0.y, fmadd(-u0.x, y0.x, r0));
@@ -550,7 +566,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
                     r1 = fmadd(-u1.w, y1.y, fmadd(-u1.z, y1.x, r1));
                 }
                 if (p < task.w) {
-                    const int2 q0 = __ldg(&P.pairs[p]);
+                    const int2 q0 = n0;
                     const B4 u0 = fac[((size_t)q0.x << lg) + s];
                     const B2 y0 = y[((size_t)q0.y << lg) + s];
                     r0 = fmadd(-u0.y, y0.y, fmadd(-u0.x, y0.x, r0));

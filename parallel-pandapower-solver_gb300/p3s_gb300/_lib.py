@@ -97,6 +97,7 @@ class Job(C.Structure):
         ("out_ptr", _vp),
         ("out_idx", _vp),
         ("reslack", C.c_int),
+        ("served", _vp),
     ]
 
 

@@ -20,6 +20,7 @@ pandapower nets, which this package does not depend on):
 
 from __future__ import annotations
 
+import itertools
 from dataclasses import dataclass
 
 import numpy as np
@@ -149,8 +150,8 @@ def outage_lists(groups):
     """(ptr (L+1,), idx) int32 outage lists of case groups (branch index lists)."""
     ptr = np.zeros(len(groups) + 1, dtype=np.int32)
     ptr[1:] = np.cumsum([len(g) for g in groups])
-    idx = np.concatenate([np.asarray(g, dtype=np.int32) for g in groups]) if ptr[-1] else np.zeros(0, np.int32)
-    return ptr, idx.astype(np.int32)
+    idx = np.fromiter(itertools.chain.from_iterable(groups), dtype=np.int32, count=int(ptr[-1]))
+    return ptr, idx
 
 
 def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, max_iter: int = 30,
@@ -162,8 +163,8 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
     The grid's branch table stays resident with the solver; every case is an outage list, so
     islanding, the re-slack start and the outage-patched Ybus are all made on the device in the
     solve's launch (no per-case arrays cross the bus but the results). Unserved buses come back
-    as NaN. ``return_islands`` adds the island labels and reference buses (one more islanding
-    call); without it ``served`` is read off the NaNs."""
+    as NaN; ``served`` is the launch's own islanding mask. ``return_islands`` adds the island
+    labels and reference buses (one more islanding call)."""
     from .group import GpuGroup, GroupJob
 
     n = grid.n
@@ -195,14 +196,13 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
     ptr, idx = outage_lists(groups)
     job = GroupJob(gs, np.asarray(grid.Sbus), np.asarray(v_start), n_cases=len(groups), outages=(ptr, idx),
                    reslack=reslack_islands)
-    res = solver._group.solve([job], solver._params(max_iter, tol))[0]
+    res = solver._group.solve([job], solver._params(max_iter, tol), pinned_out=True)[0]
     solver._record(len(groups), res, solver._group.stats)
     V = res["V"]
+    served = res["served"]
     labels = ref_bus = None
     if return_islands:
         batch = build_batch(grid, groups)
-        labels, served, ref_bus, _ = islands(batch, reslack_islands, gen_prio)
-    else:
-        served = ~np.isnan(V)
+        labels, _, ref_bus, _ = islands(batch, reslack_islands, gen_prio)
     return ContingencyResultTable(groups, V, served, np.asarray(res["converged"], bool),
                                   np.asarray(res["iterations"], int), labels, ref_bus)

@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from .solver import GpuSolver, c128
+from .solver import GpuSolver, c128, pooled_empty
 
 
 @dataclass
@@ -66,7 +66,11 @@ class GpuGroup:
         _lib.check(_lib.load().gbpf_group_stats(self._h, C.byref(o)), "gbpf_group_stats")
         return {f: getattr(o, f) for f, _ in o._fields_}
 
-    def solve(self, jobs: list[GroupJob], params: _lib.Params) -> list[dict]:
+    def solve(self, jobs: list[GroupJob], params: _lib.Params, pinned_out: bool = False) -> list[dict]:
+        """One launch over `jobs`; per job a dict of V (n, T), iterations, converged and, for
+        outage jobs, served (n, T). pinned_out: V and served in pooled page-locked host memory
+        (a direct copy from the device; the block is reused once the arrays are dropped)."""
+        empty = pooled_empty if pinned_out else np.empty
         arr = (_lib.Job * len(jobs))()
         keep = []
         outs = []
@@ -77,7 +81,7 @@ class GpuGroup:
             T = jb.n_cases or (S.shape[1] if S.ndim == 2 else (V0.shape[1] if V0.ndim == 2 else 1))
             if S.shape not in ((n, T), (n,)) or V0.shape not in ((n, T), (n,)):
                 raise ValueError(f"job {i}: S / V0 must be (n_bus, T) or (n_bus,)")
-            V = np.empty((n, T), dtype=np.complex128)
+            V = empty((n, T), dtype=np.complex128)
             it = np.empty(T, dtype=np.int32)
             cv = np.empty(T, dtype=np.uint8)
             J = arr[i]
@@ -113,7 +117,17 @@ class GpuGroup:
                     raise ValueError(f"job {i}: outage pointers must be (T + 1,)")
                 J.out_ptr, J.out_idx, J.reslack = optr.ctypes.data, oidx.ctypes.data, int(bool(jb.reslack))
                 keep += [optr, oidx]
-            outs.append((V, it, cv))
+                sv = empty((n, T), dtype=np.uint8)  # the device islanding's served mask
+                J.served = sv.ctypes.data
+            else:
+                sv = None
+            outs.append((V, it, cv, sv))
         rc = _lib.load().gbpf_group_solve(self._h, len(jobs), arr, C.byref(params))
         _lib.check(rc, "group_solve")
-        return [{"V": V, "iterations": it, "converged": cv.astype(bool)} for V, it, cv in outs]
+        res = []
+        for V, it, cv, sv in outs:
+            r = {"V": V, "iterations": it, "converged": cv.view(bool)}
+            if sv is not None:
+                r["served"] = sv.view(bool)
+            res.append(r)
+        return res

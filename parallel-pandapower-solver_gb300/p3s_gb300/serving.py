@@ -9,12 +9,15 @@ data -- and serves a stream of requests:
 * ``n1``: an N-1 sweep over a list of branch outages (islands, re-slack, stamp-patched Ybus).
 
 Requests are admitted as they arrive. Whenever one of the server's launch contexts
-(``GpuGroup``: its own stream and scratch) is free, every admitted request waiting for a
-topology that no other launch is using joins ONE persistent-kernel launch over all those
-topologies (largest job first), within the device-memory budget; requests that arrive while
-launches run wait at most until the next context frees, and the launches of different
-contexts overlap on the device. Every case runs the same arithmetic alone and in any mix,
-so a request's result does not depend on what it was batched with.
+(``GpuGroup``: its own stream and scratch) is free, every admitted request joins ONE
+persistent-kernel launch (largest job first), within the launch's case limit and the
+device-memory budget; requests that arrive while launches run wait at most until the next
+context frees, and the launches of different contexts overlap on the device, on one topology
+or on several (a topology's plan and schedules are read-only while it serves). A time-series
+chunk or an N-1 sweep is a job of its own, solved straight from the caller's array into its
+own result array; the single solves of one topology share a job. Every case runs the same
+arithmetic alone and in any mix, so a request's result does not depend on what it was
+batched with.
 
 No reference counterpart: the reference solves one call at a time
 (p3s/cuda/nr_polar_solver.py:466-596, p3s/contingency/solver_cuda.py:30-119); its N-1
@@ -168,54 +171,47 @@ class Server:
     def _footprint(self, r: Request) -> float:
         return self._cases(r) * self.topos[r.topo].slot_bytes(self.mixed)
 
-    def _form(self, pending: deque, busy_topos: set, budget_left: float):
-        """Take every pending request whose topology is idle, oldest first, within the
-        launch's case and memory limits."""
-        take, cases, mem, topos = [], 0, 0.0, set()
+    def _form(self, pending: deque, budget_left: float):
+        """Take pending requests, oldest first, within the launch's case and memory limits
+        (the oldest is taken even when it alone exceeds them)."""
+        take, cases, mem = [], 0, 0.0
         keep = deque()
         while pending:
             r = pending.popleft()
             c, fp = self._cases(r), self._footprint(r)
-            if r.topo in busy_topos or (take and (cases + c > self.max_cases or mem + fp > budget_left)):
+            if take and (cases + c > self.max_cases or mem + fp > budget_left):
                 keep.append(r)
                 continue
             take.append(r)
             cases += c
             mem += fp
-            topos.add(r.topo)
         pending.extend(keep)
-        return take, topos, mem
+        return take, mem
 
     def _jobs(self, reqs: list):
-        """One job per topology for its steady-state cases (single + chunk columns, all
-        starting from the warm-start voltage) and one per topology for its N-1 cases."""
-        ts, n1 = {}, {}
-        for r in reqs:
-            (n1 if r.kind == "n1" else ts).setdefault(r.topo, []).append(r)
+        """Jobs of one launch: the single solves of a topology together (columns of one
+        (n, k) array), every chunk and every N-1 sweep alone -- a job of its own reads the
+        request's array in place and its result array is the response's, so a large request
+        is not copied on the host. layout[j]: (request, first column, end column) per job."""
+        singles = {}
         jobs, layout, served = [], [], {}
-        for k, rs in ts.items():
-            tp = self.topos[k]
-            cols = [r.S[:, None] if r.S.ndim == 1 else r.S for r in rs]
-            S = np.ascontiguousarray(np.concatenate(cols, axis=1), dtype=np.complex128)
-            jobs.append(GroupJob(tp.solver, S, tp.V_warm))
-            at = 0
-            spans = []
-            for r, c in zip(rs, cols):
-                spans.append((r, at, at + c.shape[1]))
-                at += c.shape[1]
-            layout.append(spans)
-        for k, rs in n1.items():
-            tp = self.topos[k]
-            out = np.concatenate([r.outages for r in rs])
-            jobs.append(tp.n1_job(out, rs[0].S))
-            at = 0
-            spans = []
-            for r in rs:
-                L = len(r.outages)
-                spans.append((r, at, at + L))
+        for r in reqs:
+            tp = self.topos[r.topo]
+            if r.kind == "single":
+                singles.setdefault(r.topo, []).append(r)
+            elif r.kind == "n1":
+                jobs.append(tp.n1_job(r.outages, r.S))
+                layout.append([(r, 0, len(r.outages))])
                 served[r.rid] = True
-                at += L
-            layout.append(spans)
+            else:
+                S = r.S if r.S.ndim == 2 else r.S[:, None]
+                jobs.append(GroupJob(tp.solver, S, tp.V_warm))
+                layout.append([(r, 0, S.shape[1])])
+        for k, rs in singles.items():
+            tp = self.topos[k]
+            S = rs[0].S[:, None] if len(rs) == 1 else np.stack([r.S for r in rs], axis=1)
+            jobs.append(GroupJob(tp.solver, S, tp.V_warm))
+            layout.append([(r, c, c + 1) for c, r in enumerate(rs)])
         return jobs, layout, served
 
     # ------------------------------------------------------------------ serving
@@ -226,7 +222,6 @@ class Server:
         pending: deque = deque()
         responses: dict[int, Response] = {}
         free = list(range(len(self.groups)))
-        busy_topos: set = set()
         mem_in_use = [0.0]
         inflight = [0]
         errors: list = []
@@ -236,18 +231,19 @@ class Server:
         def now():
             return time.perf_counter() - t0
 
-        def worker(gi: int, launch: _Launch, topos: set, mem: float, layout):
+        def worker(gi: int, launch: _Launch, mem: float, layout):
             try:
                 res = self.groups[gi].solve(launch.jobs, self.params)
                 done = now()
                 out = []
                 for job_res, spans in zip(res, layout):
+                    whole = len(spans) == 1  # the job's result arrays are the response's
                     for r, a, b in spans:
-                        V = job_res["V"][:, a:b].copy()
-                        sv = ~np.isnan(V) if r.rid in launch.served else None  # unserved buses are NaN
-                        out.append(Response(r.rid, V, job_res["iterations"][a:b].copy(),
-                                            job_res["converged"][a:b].copy(), r.arrival, launch.start, done,
-                                            launch.seq, sv))
+                        V = job_res["V"] if whole else job_res["V"][:, a:b].copy()
+                        it = job_res["iterations"] if whole else job_res["iterations"][a:b].copy()
+                        cv = job_res["converged"] if whole else job_res["converged"][a:b].copy()
+                        sv = job_res["served"] if r.rid in launch.served else None  # an N-1 job is one request
+                        out.append(Response(r.rid, V, it, cv, r.arrival, launch.start, done, launch.seq, sv))
             except Exception as e:  # reported to the caller after the stream
                 out = []
                 errors.append(e)
@@ -255,7 +251,6 @@ class Server:
                 for resp in out:
                     responses[resp.rid] = resp
                 free.append(gi)
-                busy_topos.difference_update(topos)
                 mem_in_use[0] -= mem
                 inflight[0] -= 1
                 self._cv.notify_all()
@@ -270,16 +265,15 @@ class Server:
                 if errors:
                     break
                 if pending and free:
-                    take, topos, mem = self._form(pending, busy_topos, self.hbm_budget - mem_in_use[0])
+                    take, mem = self._form(pending, self.hbm_budget - mem_in_use[0])
                     if take:
                         gi = free.pop()
                         jobs, layout, served = self._jobs(take)
                         launch = _Launch(seq[0], take, jobs, served, now())
                         seq[0] += 1
-                        busy_topos.update(topos)
                         mem_in_use[0] += mem
                         inflight[0] += 1
-                        threading.Thread(target=worker, args=(gi, launch, topos, mem, layout), daemon=True).start()
+                        threading.Thread(target=worker, args=(gi, launch, mem, layout), daemon=True).start()
                         continue
                 wait = None
                 if i < len(reqs) and realtime:

@@ -8,6 +8,7 @@ arrays out, every solve one launch of the persistent sm_103a Newton kernel.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 
 import numpy as np
 
@@ -49,6 +50,65 @@ def pinned_empty(shape, dtype) -> np.ndarray:
     a = np.frombuffer(buf, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape).view(PinnedArray)
     a._owner = _PinnedOwner(ptr)
     return a
+
+
+class _HostPool:
+    """Page-locked blocks of dropped result arrays, kept for the next result of about the same
+    size: a page-locked allocation costs milliseconds, and a fresh pageable array has its pages
+    faulted in during the device-to-host copy. Holds at most `keep` bytes; the rest is freed."""
+
+    def __init__(self, keep: int = 4 << 30):
+        self.keep = keep
+        self._free: list[tuple[int, int]] = []  # (bytes, address)
+        self._held = 0
+        self._lock = threading.Lock()
+
+    def take(self, nbytes: int) -> tuple[int, int]:
+        with self._lock:
+            fit = [i for i, (nb, _) in enumerate(self._free) if nbytes <= nb <= 2 * nbytes]
+            if fit:
+                i = min(fit, key=lambda k: self._free[k][0])
+                nb, ptr = self._free.pop(i)
+                self._held -= nb
+                return nb, ptr
+        ptr = _lib.load().gbpf_host_alloc(nbytes)
+        if not ptr:
+            raise MemoryError(_lib.last_error())
+        return nbytes, ptr
+
+    def give(self, nbytes: int, ptr: int) -> None:
+        with self._lock:
+            if self._held + nbytes <= self.keep:
+                self._free.append((nbytes, ptr))
+                self._held += nbytes
+                return
+        _lib.load().gbpf_host_free(ptr)
+
+
+_HOST_POOL = _HostPool()
+
+
+class _PooledBlock:
+    def __init__(self, nbytes, ptr):
+        self.nbytes, self.ptr = nbytes, ptr
+
+    def __del__(self):
+        try:
+            _HOST_POOL.give(self.nbytes, self.ptr)
+        except Exception:
+            pass
+
+
+def pooled_empty(shape, dtype) -> np.ndarray:
+    """An uninitialised plain numpy array in page-locked host memory from a pool: the block
+    goes back to the pool when the array and every view of it are gone (copies do not hold
+    it)."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    nb, ptr = _HOST_POOL.take(max(nbytes, 16))
+    buf = (C.c_char * nb).from_address(ptr)
+    buf._block = _PooledBlock(nb, ptr)
+    return np.frombuffer(buf, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape)
 
 
 class GpuSolver:

@@ -357,6 +357,11 @@ def test_n1_sweep_of_the_2000_bus_grid(grid2000):
     assert ok.all()
     res = contingency.solve_contingencies(g, reslack_islands=True, groups=groups)
     assert np.array_equal(res.served, s_sv) and np.array_equal(res.converged, ok)
+    assert np.array_equal(res.labels, s_lab) and np.array_equal(res.ref_bus, s_rb)
+    # the served mask comes from the launch's own islanding (no separate islanding call)
+    res2 = contingency.solve_contingencies(g, reslack_islands=True, groups=groups, return_islands=False)
+    assert res2.labels is None and res2.served.dtype == bool and np.array_equal(res2.served, s_sv)
+    assert np.array_equal(np.isnan(res2.V), ~s_sv) and np.array_equal(res2.iterations, res.iterations)
     assert np.array_equal(res.iterations, ref["iterations"])
     Vs = np.where(s_sv, ref["V"], np.nan)
     assert np.nanmax(np.abs(res.V - Vs)) < 1e-10  # the oracle rebuilds each Ybus from |Y| and angle

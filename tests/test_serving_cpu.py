@@ -41,7 +41,7 @@ def _server(topos, max_cases, budget):
     return s
 
 
-def test_batch_formation_respects_busy_topologies_and_limits():
+def test_batch_formation_respects_case_and_memory_limits():
     topos = [_topo(grid_118()), _topo(make_grid(300, seed=3))]
     S0, S1 = np.zeros(118, complex), np.zeros(300, complex)
     reqs = [Request(0, 0, "single", 0.0, S0), Request(1, 1, "chunk", 0.1, np.zeros((300, 50), complex)),
@@ -49,15 +49,35 @@ def test_batch_formation_respects_busy_topologies_and_limits():
             Request(4, 0, "n1", 0.4, S0, np.arange(20))]
     s = _server(topos, max_cases=60, budget=1e12)
     pending = deque(reqs)
-    take, tp, mem = s._form(pending, busy_topos={1}, budget_left=1e12)
-    # topology 1 is busy: its requests wait; topology 0 fills up to 60 cases in arrival order
-    assert [r.rid for r in take] == [0, 2] and tp == {0}
-    assert [r.rid for r in pending] == [1, 3, 4]
-    assert mem == (1 + 40) * 1000 * 118
+    take, mem = s._form(pending, budget_left=1e12)
+    # up to 60 cases in arrival order; a request that does not fit waits, later ones may fit
+    assert [r.rid for r in take] == [0, 1, 3]
+    assert [r.rid for r in pending] == [2, 4]
+    assert mem == 1 * 1000 * 118 + 51 * 1000 * 300
     # the memory budget admits the oldest request even when it alone exceeds the budget
     pending = deque(reqs)
-    take, _, _ = _server(topos, 10_000, 1.0)._form(pending, set(), 1.0)
+    take, _ = _server(topos, 10_000, 1.0)._form(pending, 1.0)
     assert [r.rid for r in take] == [0]
+
+
+def test_jobs_keep_large_requests_in_place():
+    topos = [_topo(grid_118()), _topo(make_grid(300, seed=3))]
+    for tp in topos:
+        tp.solver, tp.V_warm = None, np.ones(tp.n, complex)
+        tp.n1_job = lambda outages, S, tp=tp: SimpleNamespace(solver=None, S=S, outages=outages)
+    rng = np.random.default_rng(1)
+    a, b, c = (rng.standard_normal(118) + 0j for _ in range(3))
+    chunk = np.ascontiguousarray(rng.standard_normal((300, 7)) + 0j)
+    reqs = [Request(0, 0, "single", 0.0, a), Request(1, 1, "chunk", 0.1, chunk),
+            Request(2, 0, "single", 0.2, b), Request(3, 0, "n1", 0.3, c, np.arange(5)),
+            Request(4, 1, "single", 0.4, np.zeros(300, complex))]
+    s = _server(topos, max_cases=10_000, budget=1e12)
+    jobs, layout, served = s._jobs(reqs)
+    spans = [[(r.rid, lo, hi) for r, lo, hi in lay] for lay in layout]
+    # chunk and N-1 alone (their arrays in place), the single solves of a topology together
+    assert spans == [[(1, 0, 7)], [(3, 0, 5)], [(0, 0, 1), (2, 1, 2)], [(4, 0, 1)]]
+    assert jobs[0].S is chunk and jobs[1].S is c and served == {3: True}
+    assert np.array_equal(jobs[2].S, np.stack([a, b], axis=1))
 
 
 def test_latency_summary():
