@@ -418,7 +418,7 @@ def run_serving(args):
     out = {"topologies": len(topos), "bus_range": [int(sizes[0]), int(sizes[-1])], "stream_s": args.serve_seconds}
     for prec in ("mixed", "double"):
         srv = Server(topos, precision=prec, contexts=4)
-        srv.warmup(cases=64)
+        srv.warmup(cases=96, n1_outages=200)  # the stream's largest chunk and N-1 sweep
         sweep = []
         # rates in steps of sqrt(2) from 200 req/s, where the 50 ms bound starts to bind
         for rate in (25, 50, 100, 200, 280, 400, 560, 800, 1130, 1600):
@@ -428,9 +428,17 @@ def run_serving(args):
             gc.collect()
             gc.disable()
             try:
-                s = latency_summary(srv.run(reqs))
+                resp = srv.run(reqs)
             finally:
                 gc.enable()
+            s = latency_summary(resp)
+            # the slowest request: what it was, how long it waited for a launch and ran in one
+            w = max(resp, key=lambda r: r.latency)
+            q = reqs[w.rid]
+            s["slowest"] = {"kind": q.kind, "n_bus": int(topos[q.topo].n), "cases": int(len(w.iterations)),
+                            "wait_ms": round((w.start - w.arrival) * 1e3, 2), "run_ms": round((w.done - w.start) * 1e3, 2),
+                            "arrival_s": round(w.arrival, 3),
+                            "launch_requests": int(sum(1 for r in resp if r.launch == w.launch))}
             sweep.append({"rate_per_s": rate, **{k: (round(v, 3) if isinstance(v, float) else v) for k, v in s.items()}})
             if s["p99_ms"] > 50.0:
                 break

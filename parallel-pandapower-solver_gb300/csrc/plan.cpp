@@ -596,9 +596,9 @@ void host_solve(const Plan& p, const double* blk, double* y) {
 // ------------------------------------------------------------------ schedule self-test
 namespace gbpf {
 
-// Serial execution of the device schedule (factor levels with the forward substitution in
-// the factor levels, backward levels) in double precision, and a structural
-// check that no task of a level reads what another task of the same phase writes.
+// Serial execution of the device schedule in double precision (the factor levels, which carry
+// the forward substitution, then the backward levels), and a structural check that no task of
+// a level reads what another task of the same level writes.
 std::string schedule_selftest(const Plan& p, double* blk, const double* R, double* y) {
     const int W = p.W;
     std::vector<int> wstamp((size_t)p.nblk + p.nv, -1), ystamp(std::max(p.nv, 1), -1);

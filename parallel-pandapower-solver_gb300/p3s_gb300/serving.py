@@ -13,7 +13,9 @@ Requests are admitted as they arrive. Whenever one of the server's launch contex
 persistent-kernel launch (largest job first), within the launch's case limit and the
 device-memory budget; requests that arrive while launches run wait at most until the next
 context frees, and the launches of different contexts overlap on the device, on one topology
-or on several (a topology's plan and schedules are read-only while it serves). A time-series
+or on several (a topology's plan and schedules are read-only while it serves). Some contexts
+take small requests only (at most ``small_work`` bus-cases), so a burst of large requests
+holding the other contexts does not queue the small ones behind it. A time-series
 chunk or an N-1 sweep is a job of its own, solved straight from the caller's array into its
 own result array; the single solves of one topology share a job. Every case runs the same
 arithmetic alone and in any mix, so a request's result does not depend on what it was
@@ -122,7 +124,8 @@ class _Launch:
 class Server:
     """Continuous batching over resident topologies (see the module docstring).
 
-    precision: "mixed" or "double"; contexts: launches that may overlap on the device;
+    precision: "mixed" or "double"; contexts: launches that may overlap on the device, of
+    which small_contexts take only requests of at most small_work bus-cases (buses x cases);
     max_cases: cases per launch; hbm_budget: bytes of case-slot scratch all contexts may hold;
     slot_budget: variable buses x case slots a CTA holds per job (smaller than bulk launches':
     a request's cases spread over more CTAs, which keeps its latency down).
@@ -130,13 +133,17 @@ class Server:
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", contexts: int = 2,
                  max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
-                 slot_budget: int = 8192, **solver_params):
+                 slot_budget: int = 8192, small_contexts: int = 0, small_work: int = 1 << 18, **solver_params):
         self.topos = topologies
         # no shared-start prologue ahead of a request's launch: latency first
         solver_params.setdefault("shared_start", False)
         self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
         self.mixed = precision == "mixed"
         self.groups = [GpuGroup() for _ in range(max(1, contexts))]
+        # the last small_contexts contexts serve small requests only (never all of them)
+        self.small = set(range(len(self.groups) - min(max(0, small_contexts), len(self.groups) - 1),
+                               len(self.groups)))
+        self.small_work = small_work
         self.slot_budget = slot_budget
         for grp in self.groups:  # fewer case slots per CTA than bulk launches: more CTAs per request
             grp.set_shape(0, slot_budget)
@@ -144,10 +151,13 @@ class Server:
         self.hbm_budget = hbm_budget
         self._cv = threading.Condition()
 
-    def warmup(self, cases: int = 64):
-        """Build every topology's schedules and grow every context's scratch to its largest
-        launch before serving, so that no launch allocates device memory (an allocation or
-        release synchronises the device and would stall the launches in flight)."""
+    def warmup(self, cases: int = 64, n1_outages: int = 64):
+        """Build every topology's schedules and grow every context's scratch and staging
+        buffers before serving, so that no launch allocates device memory (an allocation or
+        release synchronises the device and would stall the launches in flight). cases: the
+        largest time-series chunk expected; n1_outages: the largest N-1 sweep expected (each
+        context runs one launch with that many cases on every topology, which sizes its buffers
+        for any mix of smaller requests)."""
         big = max(self.topos, key=lambda tp: tp.nblk)
         for tp in self.topos:  # every shape a request's launch may take (its group's slot rule)
             g = 1
@@ -159,8 +169,8 @@ class Server:
             jobs.append(GroupJob(big.solver, big.grid.Sbus, big.V_warm, n_cases=max(cases, 1)))
             jobs += [GroupJob(tp.solver, tp.grid.Sbus, tp.V_warm, n_cases=cases) for tp in self.topos]
             grp.solve(jobs, self.params)
-            grp.solve([tp.n1_job(np.arange(min(64, len(tp.f)), dtype=np.int32), tp.grid.Sbus) for tp in self.topos],
-                      self.params)
+            grp.solve([tp.n1_job(np.arange(min(n1_outages, len(tp.f)), dtype=np.int32), tp.grid.Sbus)
+                       for tp in self.topos], self.params)
 
     # ------------------------------------------------------------------ batching
     def _cases(self, r: Request) -> int:
@@ -171,15 +181,18 @@ class Server:
     def _footprint(self, r: Request) -> float:
         return self._cases(r) * self.topos[r.topo].slot_bytes(self.mixed)
 
-    def _form(self, pending: deque, budget_left: float):
+    def _is_small(self, r: Request) -> bool:
+        return self._cases(r) * self.topos[r.topo].n <= self.small_work
+
+    def _form(self, pending: deque, budget_left: float, small_only: bool = False):
         """Take pending requests, oldest first, within the launch's case and memory limits
-        (the oldest is taken even when it alone exceeds them)."""
+        (the oldest is taken even when it alone exceeds them); small_only: small requests only."""
         take, cases, mem = [], 0, 0.0
         keep = deque()
         while pending:
             r = pending.popleft()
             c, fp = self._cases(r), self._footprint(r)
-            if take and (cases + c > self.max_cases or mem + fp > budget_left):
+            if (small_only and not self._is_small(r)) or (take and (cases + c > self.max_cases or mem + fp > budget_left)):
                 keep.append(r)
                 continue
             take.append(r)
@@ -265,9 +278,11 @@ class Server:
                 if errors:
                     break
                 if pending and free:
-                    take, mem = self._form(pending, self.hbm_budget - mem_in_use[0])
+                    # a general context if one is free, else a small-request one
+                    gi = next((g for g in free if g not in self.small), free[0])
+                    take, mem = self._form(pending, self.hbm_budget - mem_in_use[0], gi in self.small)
                     if take:
-                        gi = free.pop()
+                        free.remove(gi)
                         jobs, layout, served = self._jobs(take)
                         launch = _Launch(seq[0], take, jobs, served, now())
                         seq[0] += 1

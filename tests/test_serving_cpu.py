@@ -58,6 +58,11 @@ def test_batch_formation_respects_case_and_memory_limits():
     pending = deque(reqs)
     take, _ = _server(topos, 10_000, 1.0)._form(pending, 1.0)
     assert [r.rid for r in take] == [0]
+    # a small-request context takes requests of at most small_work bus-cases only
+    s.small_work = 40 * 118
+    pending = deque(reqs)
+    take, _ = s._form(pending, 1e12, small_only=True)
+    assert [r.rid for r in take] == [0, 2, 3] and [r.rid for r in pending] == [1, 4]
 
 
 def test_jobs_keep_large_requests_in_place():
