@@ -416,8 +416,11 @@ def run_serving(args):
     sizes = np.sort(np.exp(rng.uniform(np.log(100), np.log(50000), 32)).astype(int))
     topos = [Topology(make_grid(int(n), seed=500 + i, max_drop_pu=0.05)) for i, n in enumerate(sizes)]
     out = {"topologies": len(topos), "bus_range": [int(sizes[0]), int(sizes[-1])], "stream_s": args.serve_seconds}
+    from p3s_gb300.group import GpuGroup
+
+    groups = [GpuGroup() for _ in range(4)]  # both servers run on the same 4 launch contexts
     for prec in ("mixed", "double"):
-        srv = Server(topos, precision=prec, contexts=4)
+        srv = Server(topos, precision=prec, groups=groups)
         srv.warmup(cases=96, n1_outages=200)  # the stream's largest chunk and N-1 sweep
         sweep = []
         # rates in steps of sqrt(2) from 200 req/s, where the 50 ms bound starts to bind

@@ -128,18 +128,21 @@ class Server:
     which small_contexts take only requests of at most small_work bus-cases (buses x cases);
     max_cases: cases per launch; hbm_budget: bytes of case-slot scratch all contexts may hold;
     slot_budget: variable buses x case slots a CTA holds per job (smaller than bulk launches':
-    a request's cases spread over more CTAs, which keeps its latency down).
+    a request's cases spread over more CTAs, which keeps its latency down); groups: launch
+    contexts to serve on (e.g. another server's, whose grown buffers are then reused instead of
+    released and allocated again), else `contexts` new ones.
     """
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", contexts: int = 2,
                  max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
-                 slot_budget: int = 8192, small_contexts: int = 0, small_work: int = 1 << 18, **solver_params):
+                 slot_budget: int = 8192, small_contexts: int = 0, small_work: int = 1 << 18,
+                 groups: list[GpuGroup] | None = None, **solver_params):
         self.topos = topologies
         # no shared-start prologue ahead of a request's launch: latency first
         solver_params.setdefault("shared_start", False)
         self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
         self.mixed = precision == "mixed"
-        self.groups = [GpuGroup() for _ in range(max(1, contexts))]
+        self.groups = list(groups) if groups else [GpuGroup() for _ in range(max(1, contexts))]
         # the last small_contexts contexts serve small requests only (never all of them)
         self.small = set(range(len(self.groups) - min(max(0, small_contexts), len(self.groups) - 1),
                                len(self.groups)))
