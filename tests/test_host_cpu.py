@@ -101,3 +101,84 @@ def test_case_sharding_covers_every_case_once():
     for B, W in ((8760, 1), (8760, 2), (3001, 4), (5, 8)):
         seen = np.concatenate([np.arange(*shard(B, r, W)) for r in range(W)])
         assert np.array_equal(np.sort(seen), np.arange(B))
+
+
+def _header_structs():
+    """Field names of every `typedef struct NAME { ... } NAME;` in include/gbpf.h, in order."""
+    hdr = open(os.path.join(ROOT, "include", "gbpf.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    out = {}
+    for name, body in re.findall(r"typedef struct (\w+) \{(.*?)\} \1;", hdr, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            for piece in decl.split(","):
+                ids = re.findall(r"[A-Za-z_]\w*", piece)
+                if ids:
+                    fields.append(ids[-1])
+        out[name] = fields
+    return out
+
+
+@pytest.mark.parametrize("cname, py", [("gbpf_params", "Params"), ("gbpf_info", "Info"), ("gbpf_stats", "Stats"),
+                                       ("gbpf_job", "Job")])
+def test_ctypes_structs_follow_the_header(cname, py, tmp_path):
+    """The ctypes mirrors of the C ABI's structs: same fields in the same order, and the same
+    offsets and size as the C compiler lays them out."""
+    import shutil
+    import subprocess
+
+    fields = _header_structs()[cname]
+    S = getattr(_lib, py)
+    assert [f for f, _ in S._fields_] == fields
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "gbpf.h"\nint main(void) {\n'
+                   + "".join(f'    printf("%zu\\n", offsetof({cname}, {f}));\n' for f in fields)
+                   + f'    printf("%zu\\n", sizeof({cname}));\n    return 0;\n}}\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == [getattr(S, f).offset for f in fields] + [C.sizeof(S)]
+
+
+def test_pooled_result_blocks_are_reused_once_dropped(monkeypatch):
+    """Page-locked result blocks (faked here by plain host buffers): a dropped array's block
+    serves the next request of about its size; views keep it, copies do not; blocks beyond
+    the pool's limit are released."""
+    from p3s_gb300 import solver
+
+    live, freed = {}, []
+
+    class FakeLib:
+        def gbpf_host_alloc(self, nbytes):
+            buf = (C.c_char * nbytes)()
+            live[C.addressof(buf)] = buf
+            return C.addressof(buf)
+
+        def gbpf_host_free(self, ptr):
+            freed.append(ptr)
+
+    fake = FakeLib()
+    monkeypatch.setattr(_lib, "load", lambda: fake)
+    pool = solver._HostPool(keep=40_000)
+    monkeypatch.setattr(solver, "_HOST_POOL", pool)
+    a = solver.pooled_empty((100, 10), np.complex128)  # 16,000 bytes
+    assert type(a) is np.ndarray and a.flags.c_contiguous and len(live) == 1
+    a[:] = 1.0
+    pa = a.ctypes.data
+    del a
+    assert pool._held == 16_000
+    b = solver.pooled_empty((90, 10), np.complex128)  # fits the dropped block: reused
+    assert b.ctypes.data == pa and len(live) == 1 and pool._held == 0
+    c = solver.pooled_empty((10, 10), np.complex128)  # far smaller than any free block: a new one
+    assert len(live) == 2
+    d = b[:, :3].copy()
+    v = c[:, 1:]
+    del b, c
+    assert pool._held == 16_000  # b's block is back; c's is held by its view
+    del v
+    assert pool._held == 17_600 and d.base is None
+    e = solver.pooled_empty((200, 10), np.complex128)  # 32,000 bytes: new
+    del e  # 49,600 would exceed the 40,000-byte limit: released
+    assert freed == [list(live)[2]] and pool._held == 17_600
