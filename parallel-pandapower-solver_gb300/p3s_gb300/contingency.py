@@ -154,6 +154,14 @@ def outage_lists(groups):
     return ptr, idx
 
 
+def single_outage_lists(n_branch: int):
+    """outage_lists of the base case and every single-branch outage ([[], [0], ..., [m-1]]),
+    made directly."""
+    ptr = np.arange(-1, n_branch + 1, dtype=np.int32)
+    ptr[0] = 0
+    return ptr, np.arange(n_branch, dtype=np.int32)
+
+
 def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, max_iter: int = 30,
                         precision: str = "double", groups=None, gen_prio=None, v_start=None, solver=None,
                         return_islands: bool = True):
@@ -170,7 +178,10 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
     n = grid.n
     if groups is None:
         groups = [[]] + [[b] for b in range(grid.n_branch)]
-    groups = [list(map(int, g)) for g in groups]
+        outages = single_outage_lists(grid.n_branch)
+    else:
+        groups = [list(map(int, g)) for g in groups]
+        outages = outage_lists(groups)
     if len(groups) == 0:
         e = np.empty((n, 0))
         return ContingencyResultTable([], e.astype(np.complex128), e.astype(bool), np.empty(0, bool),
@@ -193,8 +204,7 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
     if getattr(solver, "_group", None) is None:
         solver._group = GpuGroup()
     solver.precision = precision
-    ptr, idx = outage_lists(groups)
-    job = GroupJob(gs, np.asarray(grid.Sbus), np.asarray(v_start), n_cases=len(groups), outages=(ptr, idx),
+    job = GroupJob(gs, np.asarray(grid.Sbus), np.asarray(v_start), n_cases=len(groups), outages=outages,
                    reslack=reslack_islands)
     res = solver._group.solve([job], solver._params(max_iter, tol), pinned_out=True)[0]
     solver._record(len(groups), res, solver._group.stats)

@@ -182,3 +182,17 @@ def test_pooled_result_blocks_are_reused_once_dropped(monkeypatch):
     e = solver.pooled_empty((200, 10), np.complex128)  # 32,000 bytes: new
     del e  # 49,600 would exceed the 40,000-byte limit: released
     assert freed == [list(live)[2]] and pool._held == 17_600
+
+
+def test_outage_lists():
+    """Case-group outage lists (ptr, idx) as the outage jobs take them; the full N-1 sweep's
+    lists made directly equal the generic ones."""
+    from p3s_gb300 import contingency
+
+    ptr, idx = contingency.outage_lists([[], [3], [1, 2], []])
+    assert ptr.tolist() == [0, 0, 1, 3, 3] and idx.tolist() == [3, 1, 2]
+    assert ptr.dtype == np.int32 and idx.dtype == np.int32
+    for m in (0, 1, 7, 3000):
+        a = contingency.single_outage_lists(m)
+        b = contingency.outage_lists([[]] + [[e] for e in range(m)])
+        assert all(np.array_equal(x, y) and x.dtype == y.dtype for x, y in zip(a, b))
