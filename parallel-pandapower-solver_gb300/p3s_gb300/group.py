@@ -68,9 +68,14 @@ class GpuGroup:
 
     def solve(self, jobs: list[GroupJob], params: _lib.Params, pinned_out: bool = False) -> list[dict]:
         """One launch over `jobs`; per job a dict of V (n, T), iterations, converged and, for
-        outage jobs, served (n, T). pinned_out: V and served in pooled page-locked host memory
-        (a direct copy from the device; the block is reused once the arrays are dropped)."""
-        empty = pooled_empty if pinned_out else np.empty
+        outage jobs, served (n, T). pinned_out: V and served of 1 MB or more in pooled
+        page-locked host memory (a direct copy from the device; the block is reused once the
+        arrays are dropped)."""
+
+        def empty(shape, dtype):
+            big = pinned_out and shape[0] * shape[1] * np.dtype(dtype).itemsize >= 1 << 20
+            return pooled_empty(shape, dtype) if big else np.empty(shape, dtype=dtype)
+
         arr = (_lib.Job * len(jobs))()
         keep = []
         outs = []

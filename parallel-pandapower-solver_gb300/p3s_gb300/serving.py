@@ -130,13 +130,15 @@ class Server:
     slot_budget: variable buses x case slots a CTA holds per job (smaller than bulk launches':
     a request's cases spread over more CTAs, which keeps its latency down); groups: launch
     contexts to serve on (e.g. another server's, whose grown buffers are then reused instead of
-    released and allocated again), else `contexts` new ones.
+    released and allocated again), else `contexts` new ones; pinned_results: results of 1 MB or
+    more land in pooled page-locked host memory (no page faults in the copy; a block returns to
+    the pool when its response is dropped), and `warmup` fills the pool for the largest requests.
     """
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", contexts: int = 2,
                  max_cases: int = 8192, hbm_budget: float = 64e9, tol: float = 1e-8, max_iter: int = 30,
                  slot_budget: int = 8192, small_contexts: int = 0, small_work: int = 1 << 18,
-                 groups: list[GpuGroup] | None = None, **solver_params):
+                 groups: list[GpuGroup] | None = None, pinned_results: bool = False, **solver_params):
         self.topos = topologies
         # no shared-start prologue ahead of a request's launch: latency first
         solver_params.setdefault("shared_start", False)
@@ -147,6 +149,7 @@ class Server:
         self.small = set(range(len(self.groups) - min(max(0, small_contexts), len(self.groups) - 1),
                                len(self.groups)))
         self.small_work = small_work
+        self.pinned_results = pinned_results
         self.slot_budget = slot_budget
         for grp in self.groups:  # fewer case slots per CTA than bulk launches: more CTAs per request
             grp.set_shape(0, slot_budget)
@@ -174,6 +177,18 @@ class Server:
             grp.solve(jobs, self.params)
             grp.solve([tp.n1_job(np.arange(min(n1_outages, len(tp.f)), dtype=np.int32), tp.grid.Sbus)
                        for tp in self.topos], self.params)
+        if self.pinned_results:  # page-locked blocks for every context's largest results
+            from . import solver as _solver
+
+            held = []
+            for tp in self.topos:
+                for _ in self.groups:
+                    for shape, dt in (((tp.n, cases), np.complex128), ((tp.n, n1_outages), np.complex128),
+                                      ((tp.n, n1_outages), np.uint8)):
+                        if shape[0] * shape[1] * np.dtype(dt).itemsize >= 1 << 20:
+                            held.append(_solver.pooled_empty(shape, dt))
+            _solver._HOST_POOL.keep = max(_solver._HOST_POOL.keep, 2 * sum(a.nbytes for a in held))
+            del held
 
     # ------------------------------------------------------------------ batching
     def _cases(self, r: Request) -> int:
@@ -231,9 +246,11 @@ class Server:
         return jobs, layout, served
 
     # ------------------------------------------------------------------ serving
-    def run(self, requests: list[Request], realtime: bool = True) -> list[Response]:
+    def run(self, requests: list[Request], realtime: bool = True, keep_results: bool = True) -> list[Response]:
         """Serve a request stream. realtime: each request is admitted at its arrival time
-        (wall clock from the call); otherwise all are admitted at once."""
+        (wall clock from the call); otherwise all are admitted at once. keep_results False:
+        each voltage result is dropped once it is on the host (its response keeps the
+        iterations, flags and times), as a server does once it has sent it."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         pending: deque = deque()
         responses: dict[int, Response] = {}
@@ -249,7 +266,7 @@ class Server:
 
         def worker(gi: int, launch: _Launch, mem: float, layout):
             try:
-                res = self.groups[gi].solve(launch.jobs, self.params)
+                res = self.groups[gi].solve(launch.jobs, self.params, pinned_out=self.pinned_results)
                 done = now()
                 out = []
                 for job_res, spans in zip(res, layout):
@@ -259,6 +276,9 @@ class Server:
                         it = job_res["iterations"] if whole else job_res["iterations"][a:b].copy()
                         cv = job_res["converged"] if whole else job_res["converged"][a:b].copy()
                         sv = job_res["served"] if r.rid in launch.served else None  # an N-1 job is one request
+                        if not keep_results:
+                            V = sv = None
+                            it, cv = it.copy(), cv.copy()
                         out.append(Response(r.rid, V, it, cv, r.arrival, launch.start, done, launch.seq, sv))
             except Exception as e:  # reported to the caller after the stream
                 out = []

@@ -4,6 +4,7 @@ from collections import deque
 from types import SimpleNamespace
 
 import numpy as np
+import pytest
 
 from p3s_gb300.serving import Request, Response, Server, latency_summary, poisson_stream
 from p3s_gb300.synthetic import grid_118, make_grid
@@ -91,3 +92,50 @@ def test_latency_summary():
     s = latency_summary(rs)
     assert s["requests"] == 100 and s["cases"] == 100 and s["converged_fraction"] == 1.0
     assert abs(s["p50_ms"] - 50.5) < 1e-6 and abs(s["p99_ms"] - 99.01) < 1e-6 and abs(s["max_ms"] - 100.0) < 1e-6
+
+
+class _FakeGroup:
+    """Stands in for a launch context: results are the job's S columns (n1: the base S per
+    outage), one iteration each."""
+
+    def __init__(self):
+        self.calls = []
+
+    def solve(self, jobs, params, pinned_out=False):
+        self.calls.append(len(jobs))
+        out = []
+        for j in jobs:
+            T = j.n_cases or (j.S.shape[1] if j.S.ndim == 2 else 1)
+            V = np.repeat(j.S[:, None], T, axis=1) if j.S.ndim == 1 else j.S.copy()
+            r = {"V": V, "iterations": np.ones(T, np.int32), "converged": np.ones(T, bool)}
+            if j.outages is not None:
+                r["served"] = np.ones(V.shape, bool)
+            out.append(r)
+        return out
+
+
+@pytest.mark.parametrize("keep", [True, False])
+def test_serving_loop_delivers_every_request(keep):
+    import threading
+
+    topos = [_topo(grid_118()), _topo(make_grid(300, seed=3))]
+    for tp in topos:
+        tp.solver, tp.V_warm = SimpleNamespace(n=tp.n), np.ones(tp.n, complex)
+        tp.n1_job = lambda outages, S, tp=tp: SimpleNamespace(solver=tp.solver, S=S, n_cases=len(outages),
+                                                              outages=(None, outages))
+    reqs = poisson_stream(topos, rate=4000.0, duration=0.05, seed=2, chunk=5, n1_outages=4)
+    s = _server(topos, max_cases=64, budget=1e12)
+    s.groups = [_FakeGroup(), _FakeGroup()]
+    s.small, s.small_work, s.params, s.pinned_results = {1}, 10_000, None, False
+    s._cv = threading.Condition()
+    resp = s.run(reqs, realtime=False, keep_results=keep)
+    assert [r.rid for r in resp] == [q.rid for q in reqs]
+    for q, r in zip(reqs, resp):
+        T = len(q.outages) if q.kind == "n1" else (1 if q.S.ndim == 1 else q.S.shape[1])
+        assert len(r.iterations) == T and r.converged.all() and r.done >= r.start >= 0.0
+        if keep:
+            want = np.repeat(q.S[:, None], T, axis=1) if q.kind != "chunk" else q.S
+            assert np.array_equal(r.V, want) and (r.served is not None) == (q.kind == "n1")
+        else:
+            assert r.V is None and r.served is None
+    assert sum(sum(g.calls) for g in s.groups) >= len({r.launch for r in resp})
