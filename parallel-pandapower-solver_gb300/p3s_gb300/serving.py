@@ -36,7 +36,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .group import GpuGroup, GroupJob
-from .solver import GpuSolver, c128
+from .solver import GpuSolver, c128, pool_keep_at_least, pooled_empty
 
 
 @dataclass
@@ -178,17 +178,15 @@ class Server:
             grp.solve([tp.n1_job(np.arange(min(n1_outages, len(tp.f)), dtype=np.int32), tp.grid.Sbus)
                        for tp in self.topos], self.params)
         if self.pinned_results:  # page-locked blocks for every context's largest results
-            from . import solver as _solver
-
             held = []
             for tp in self.topos:
                 for _ in self.groups:
                     for shape, dt in (((tp.n, cases), np.complex128), ((tp.n, n1_outages), np.complex128),
                                       ((tp.n, n1_outages), np.uint8)):
                         if shape[0] * shape[1] * np.dtype(dt).itemsize >= 1 << 20:
-                            held.append(_solver.pooled_empty(shape, dt))
-            _solver._HOST_POOL.keep = max(_solver._HOST_POOL.keep, 2 * sum(a.nbytes for a in held))
-            del held
+                            held.append(pooled_empty(shape, dt))
+            pool_keep_at_least(2 * sum(a.nbytes for a in held))
+            del held  # the blocks go back to the pool
 
     # ------------------------------------------------------------------ batching
     def _cases(self, r: Request) -> int:

@@ -99,6 +99,12 @@ class _PooledBlock:
             pass
 
 
+def pool_keep_at_least(nbytes: int) -> None:
+    """Let the pool of page-locked result blocks hold at least `nbytes` of dropped blocks."""
+    with _HOST_POOL._lock:
+        _HOST_POOL.keep = max(_HOST_POOL.keep, int(nbytes))
+
+
 def pooled_empty(shape, dtype) -> np.ndarray:
     """An uninitialised plain numpy array in page-locked host memory from a pool: the block
     goes back to the pool when the array and every view of it are gone (copies do not hold
