@@ -196,3 +196,43 @@ def test_outage_lists():
         a = contingency.single_outage_lists(m)
         b = contingency.outage_lists([[]] + [[e] for e in range(m)])
         assert all(np.array_equal(x, y) and x.dtype == y.dtype for x, y in zip(a, b))
+
+
+def _shaped_grid(kind: str, n: int, all_pv: bool = False):
+    """A small grid of a given shape (bus 0 the slack): 'chain' (a deep elimination tree),
+    'star' (one hub column as long as the grid), 'mesh' (a square lattice: fill), with series
+    impedance 0.01 + 0.1j per line and alternating PV / PQ buses (or PV only)."""
+    from types import SimpleNamespace
+
+    from p3s_gb300.synthetic import build_ybus
+
+    if kind == "chain":
+        f, t = np.arange(n - 1), np.arange(1, n)
+    elif kind == "star":
+        f, t = np.zeros(n - 1, int), np.arange(1, n)
+    else:
+        k = int(round(np.sqrt(n)))
+        n = k * k
+        idx = np.arange(n).reshape(k, k)
+        f = np.concatenate([idx[:, :-1].ravel(), idx[:-1, :].ravel()])
+        t = np.concatenate([idx[:, 1:].ravel(), idx[1:, :].ravel()])
+    y = 1.0 / (0.01 + 0.1j)
+    stamp = np.tile(np.array([y + 0.01j, -y, -y, y + 0.01j]), (len(f), 1))
+    Yp, Yj, Yx, _ = build_ybus(n, f.astype(np.int32), t.astype(np.int32), stamp)
+    rest = np.arange(1, n, dtype=np.int32)
+    pv = rest if all_pv else np.ascontiguousarray(rest[::2])
+    pq = np.zeros(0, np.int32) if all_pv else np.ascontiguousarray(rest[1::2])
+    rng = np.random.default_rng(n)
+    S = np.zeros(n, complex)
+    S[1:] = -0.01 * (1 + rng.random(n - 1)) - 0.005j
+    return SimpleNamespace(n=n, Yp=Yp, Yj=Yj, Yx=Yx, nnz=len(Yj), pv=pv, pq=pq, V0=np.ones(n, complex), Sbus=S)
+
+
+@pytest.mark.parametrize("kind", ["chain", "star", "mesh"])
+@pytest.mark.parametrize("workers", [1, 16, 1024])
+def test_block_schedule_on_shaped_grids(kind, workers):
+    """Deep elimination trees, one long hub column (split into chain segments) and lattice
+    fill: the schedule, executed serially with its race check, solves what scipy solves."""
+    for n, all_pv in ((2, False), (3, True), (400, False), (400, True)):
+        err, shape = _selftest(_shaped_grid(kind, n, all_pv), workers)
+        assert err < 1e-9, (kind, n, all_pv, err)
