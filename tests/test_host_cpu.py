@@ -236,3 +236,20 @@ def test_block_schedule_on_shaped_grids(kind, workers):
     for n, all_pv in ((2, False), (3, True), (400, False), (400, True)):
         err, shape = _selftest(_shaped_grid(kind, n, all_pv), workers)
         assert err < 1e-9, (kind, n, all_pv, err)
+
+
+def test_no_cpu_fallback_without_a_device(grid118):
+    """Without a visible CUDA device every product entry point raises (no silent CPU path)."""
+    if _lib.load().gbpf_device_count() > 0:
+        pytest.skip("a CUDA device is visible")
+    from p3s_gb300 import nr_klu
+    from p3s_gb300.cuda.nr_polar_solver import PolarNewtonSolverCUDA
+    from p3s_gb300.group import GpuGroup
+    from p3s_gb300.solver import GpuSolver
+
+    g = grid118
+    args = (g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    for make in (lambda: GpuSolver(*args), lambda: nr_klu.Solver(*args), lambda: PolarNewtonSolverCUDA(*args),
+                 lambda: nr_klu.solve_single(g.Yp, g.Yj, g.Yx, g.Sbus, g.V0, g.pv, g.pq), lambda: GpuGroup()):
+        with pytest.raises(RuntimeError):
+            make()
