@@ -188,6 +188,11 @@ int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
  * Jacobian applies to voltage components (equal to d2f[i] for finite |in[i]| < 2^128). No
  * reference counterpart (a GB300-specific helper). */
 int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
+/* Self-test of the kernels' own double-precision numerics (no reference counterpart): per
+ * element, recip = the Newton-refined reciprocal (x > 0, else 0), s_small / c_small = the
+ * small-angle series sine / cosine (|x| < 1/4, else CUDA's), s_ref / c_ref = CUDA's sincos. */
+int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
+                       double* c_ref);
 
 /* Page-locked host memory for fast transfers. */
 void* gbpf_host_alloc(size_t bytes);
@@ -291,9 +296,10 @@ int gbpf_solver_islands(gbpf_solver* s, int m, const int32_t* f, const int32_t* 
 /* gbpf_islands on caller-owned DEVICE buffers (same layouts; out_idx holds n_out entries),
  * allocating nothing: the kernel's scratch is a statically allocated 16 MiB device array,
  * so n may not exceed GBPF_ISLANDS_STATIC_MAX_BUS (larger n is rejected with an error).
- * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and returns after it
- * has finished. The first call on each device looks up the scratch address (make it before
- * any stream capture). The scratch is shared by every call on a device: calls that overlap
+ * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and is synchronous:
+ * it waits for `stream` and reads the validation and error words back to the host before it
+ * returns. The first call on each device looks up the scratch address; make that first call
+ * before any stream capture. The scratch is shared by every call on a device: calls that overlap
  * in time there (other streams or host threads) race. No reference counterpart: for callers
  * that must not allocate device memory (cudaMalloc / cudaFree synchronise the whole device,
  * stalling the solves a serving loop overlaps, and can fail under a memory budget). */

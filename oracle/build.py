@@ -7,8 +7,9 @@
   ``finite.hpp``), compiled where it lies under the read-only reference checkout with the
   flags of its ``p3s/cpp/CMakeLists.txt:32-35`` (``-O3 -funroll-loops -ffast-math``,
   OpenMP), pybind11, and the project's KLU-API shim (klu_shim/) standing in for
-  SuiteSparse KLU. Output goes to ``oracle/_ref/`` only. Needs the reference checkout and
-  pybind11, so it is built only where both exist.
+  SuiteSparse KLU. Output goes to ``oracle/_ref/`` only. Needs the reference checkout
+  (``$P3S_REFERENCE``, default ``../reference`` beside the repository) and pybind11, so it is
+  built only where both exist.
 """
 
 from __future__ import annotations
@@ -19,7 +20,8 @@ import sys
 import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# the reference checkout: P3S_REFERENCE, else the checkout beside this repository's parent
+REFERENCE = os.environ.get("P3S_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_CPP = os.path.join(REFERENCE, "p3s", "cpp")
 
 

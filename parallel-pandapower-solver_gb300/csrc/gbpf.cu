@@ -1419,6 +1419,23 @@ int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, 
     return 0;
 }
 
+int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
+                       double* c_ref) {
+    if (n <= 0) return 0;
+    DBuf a, b;
+    CK(a.ensure((size_t)n * 8));
+    CK(b.ensure((size_t)n * 8 * 5));
+    double* o = b.as<double>();
+    CK(cudaMemcpy(a.p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
+    CK(gbpf::launch_math(a.as<double>(), n, o, o + n, o + 2 * (size_t)n, o + 3 * (size_t)n, o + 4 * (size_t)n));
+    CK(cudaDeviceSynchronize());
+    double* outs[5] = {recip, s_small, c_small, s_ref, c_ref};
+    for (int k = 0; k < 5; ++k) CK(cudaMemcpy(outs[k], o + k * (size_t)n, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    a.release();
+    b.release();
+    return 0;
+}
+
 void* gbpf_host_alloc(size_t bytes) {
     void* p = nullptr;
     if (cudaMallocHost(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {

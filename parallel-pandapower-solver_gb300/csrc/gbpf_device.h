@@ -191,6 +191,8 @@ void start_carve(StartJob& sj, char* base, int n, int nv, int nblk, int G, bool 
 // One CTA of 1,024 threads per shared start.
 cudaError_t launch_start(const StartJob* jobs, int njobs, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
+cudaError_t launch_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
+                        double* c_ref);
 // Ybus values from stamps (postproc.cu)
 cudaError_t launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,
                                const double2* shunt, double2* Y, float2* Y32, cudaStream_t stream);

@@ -1253,6 +1253,37 @@ __global__ void conversions_kernel(const double* in, int n, float* d2f, double* 
     }
 }
 
+// The project's own double-precision numerics applied elementwise (tests bound them against
+// IEEE division and CUDA's sincos): recip_nr(x) for x > 0, and sincos_small(d) with CUDA's
+// sincos(d) beside it for |d| < 1/4 (elements outside that range get sincos only).
+__global__ void math_kernel(const double* in, int n, double* recip, double* s_small, double* c_small,
+                            double* s_ref, double* c_ref) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = in[i];
+        recip[i] = x > 0.0 ? recip_nr(x) : 0.0;
+        double sr, cr;
+        sincos(x, &sr, &cr);
+        s_ref[i] = sr;
+        c_ref[i] = cr;
+        const unsigned ahi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+        if (ahi < 0x3FD00000u) {
+            double sd, cd;
+            sincos_small(x, ahi, &sd, &cd);
+            s_small[i] = sd;
+            c_small[i] = cd;
+        } else {
+            s_small[i] = sr;
+            c_small[i] = cr;
+        }
+    }
+}
+
+cudaError_t launch_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
+                        double* c_ref) {
+    math_kernel<<<(n + 255) / 256, 256>>>(in, n, recip, s_small, c_small, s_ref, c_ref);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small) {
     conversions_kernel<<<(n + 255) / 256, 256>>>(in, n, d2f, f2d, d2f_small);
     return cudaGetLastError();

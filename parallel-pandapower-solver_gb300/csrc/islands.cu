@@ -39,12 +39,14 @@ __global__ void __launch_bounds__(NT) islands_kernel(int n, int m, const int* f,
     int* cgen = cslack + n;
     unsigned long long* cbest = best + (size_t)blockIdx.x * n;
     __shared__ int s_changed;
+    __shared__ int s_unsettled;
     __shared__ int s_total;
     __shared__ int s_warp[NT / 32];
     const int tid = threadIdx.x;
     for (int c = blockIdx.x; c < L; c += gridDim.x) {
         const int o0 = out_ptr[c], o1 = out_ptr[c + 1];
         for (int v = tid; v < n; v += NT) lab[v] = v;
+        if (tid == 0) s_unsettled = 0;
         __syncthreads();
         for (int pass = 0;; ++pass) {
             if (tid == 0) s_changed = 0;
@@ -78,9 +80,26 @@ __global__ void __launch_bounds__(NT) islands_kernel(int n, int m, const int* f,
             __syncthreads();
             if (!ch) break;
             if (pass > 2 * n + 64) {
-                if (tid == 0) atomicCAS(err, 0, 1);
+                if (tid == 0) {
+                    atomicCAS(err, 0, 1);
+                    s_unsettled = 1;
+                }
+                __syncthreads();
                 break;
             }
+        }
+        if (s_unsettled) {
+            // labels that are not all roots would index the per-island words past this case's
+            // islands: the case gets no islands (label -1, unserved, no reference bus) and the
+            // error word, already set, is the call's only other effect
+            for (int v = tid; v < n; v += NT) {
+                labels[(size_t)v * L + c] = -1;
+                served[(size_t)v * L + c] = 0;
+                ref_bus[(size_t)v * L + c] = -1;
+            }
+            if (tid == 0) n_islands[c] = -1;
+            __syncthreads();
+            continue;
         }
         // component ids: exclusive prefix count of the roots (lab[v] == v), in bus order
         if (tid == 0) s_total = 0;
@@ -161,6 +180,9 @@ extern "C" int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, co
     if (n <= 0 || m < 0 || L <= 0) return ifail("gbpf_islands: invalid sizes");
     for (int e = 0; e < m; ++e)
         if (f[e] < 0 || f[e] >= n || t[e] < 0 || t[e] >= n) return ifail("gbpf_islands: branch end out of range");
+    if (out_ptr[0] != 0) return ifail("gbpf_islands: outage pointers must start at 0");
+    for (int c = 0; c < L; ++c)
+        if (out_ptr[c + 1] < out_ptr[c]) return ifail("gbpf_islands: outage pointers must not decrease");
     const int nout = out_ptr[L];
     for (int q = 0; q < nout; ++q)
         if (out_idx[q] < 0 || out_idx[q] >= m) return ifail("gbpf_islands: outage index out of range");

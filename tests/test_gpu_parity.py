@@ -326,6 +326,34 @@ def test_integer_pipe_conversions_match_ieee():
     assert np.array_equal(small[inr].view(np.uint32), d2f[inr].view(np.uint32))
 
 
+def test_own_double_numerics_within_an_ulp():
+    """The kernels' own double-precision helpers against exact references: the Newton-refined
+    reciprocal (a float seed and two Newton-Raphson steps) within 2 ulp of IEEE 1/x over the
+    voltage-magnitude range and beyond, and the small-angle Maclaurin sine / cosine used to
+    rotate phasors within 1 ulp of numpy's (and of CUDA's sincos) over |d| < 1/4."""
+    from p3s_gb300 import _lib
+
+    rng = np.random.default_rng(3)
+    x = np.concatenate([10.0 ** rng.uniform(-6, 6, 20000), rng.uniform(0.5, 1.5, 20000),
+                        [1e-6, 0.9, 1.0, 1.04, 10.0, 1e6]])
+    d = np.concatenate([rng.uniform(-0.25, 0.25, 20000) * 2.0 ** -rng.integers(0, 40, 20000),
+                        [0.0, -0.0, 2.0 ** -14, -(2.0 ** -6), 0.2499999]])
+    inp = np.ascontiguousarray(np.concatenate([x, d]))
+    outs = [np.empty(len(inp)) for _ in range(5)]
+    rc = _lib.load().gbpf_selftest_math(_lib.d(inp), len(inp), *[_lib.d(o) for o in outs])
+    assert rc == 0, _lib.last_error()
+    recip, s_small, c_small, s_ref, c_ref = outs
+    nx = len(x)
+    want = 1.0 / x
+    assert (np.abs(recip[:nx] - want) <= 2 * np.spacing(want)).all()
+    dd = inp[nx:]
+    for got, cuda, exact in ((s_small[nx:], s_ref[nx:], np.sin(dd)), (c_small[nx:], c_ref[nx:], np.cos(dd))):
+        ulp = np.spacing(np.abs(exact))
+        assert (np.abs(got - exact) <= ulp).all()
+        assert (np.abs(got - cuda) <= 2 * ulp).all()
+    assert s_small[nx + 20000] == 0.0 and c_small[nx + 20000] == 1.0
+
+
 def test_n1_sweep_of_the_2000_bus_grid(grid2000):
     """The full N-1 sweep (base case + every single-branch outage): islands, served masks and
     references bit-exact against the restated reference islanding for all 3,001 cases; the

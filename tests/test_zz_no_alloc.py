@@ -80,6 +80,45 @@ def test_static_scratch_islands_match_allocating_entry_two_calls():
         assert np.array_equal(w, x)
 
 
+def test_static_scratch_call_allocates_no_device_memory():
+    """The property the entry point exists for: with its inputs and outputs already on the
+    device, a call leaves the device's free memory where it was (a cudaMalloc of the
+    driver's 2 MiB granularity or more would show) and the caching allocator untouched."""
+    import torch
+
+    from p3s_gb300 import _lib
+    from p3s_gb300.synthetic import grid_2000
+
+    L_ = _lib.require_device()
+    g = grid_2000()
+    batch, a = _inputs(g, [[]] + [[b] for b in range(400)])
+    L = len(batch.groups)
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in a.items()}
+    lab = torch.empty((g.n, L), dtype=torch.int32, device=dev)
+    sv = torch.empty((g.n, L), dtype=torch.uint8, device=dev)
+    rb = torch.empty((g.n, L), dtype=torch.int32, device=dev)
+    ni = torch.empty((L,), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def call():
+        return L_.gbpf_islands_device_static(
+            g.n, len(a["f"]), d["f"].data_ptr(), d["t"].data_ptr(), d["live"].data_ptr(), L, d["ptr"].data_ptr(),
+            d["idx"].data_ptr(), int(a["ptr"][-1]), d["is_slack"].data_ptr(), d["prio"].data_ptr(), 1,
+            lab.data_ptr(), sv.data_ptr(), rb.data_ptr(), ni.data_ptr(), stream)
+
+    assert call() == 0, _lib.last_error()  # warmed up: scratch address looked up, module loaded
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    reserved0 = torch.cuda.memory_reserved(dev)
+    for _ in range(3):
+        assert call() == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, (free0, free1)
+    assert torch.cuda.memory_reserved(dev) == reserved0
+
+
 def test_static_scratch_rejects_oversize_and_bad_outages():
     from p3s_gb300 import _lib
     from p3s_gb300.synthetic import grid_118
