@@ -67,3 +67,31 @@ def islands(n, f, t, live, groups, ref, reslack, prio):
         s, r = resolve_references(lab, nc, ref, reslack, prio)
         labels[:, c], served[:, c], ref_bus[:, c], nis[c] = lab, s, r, nc
     return labels, served, ref_bus, nis
+
+
+def start_and_pins(v_start, served, ref_bus, ref):
+    """Per-case start voltages and pins of outage cases (n, L), for any start voltage.
+
+    solver_cpp.py:119-134 pins a re-slack reference at |v0| + 0j and an unserved bus at
+    1 + 0j, from a flat start where every other bus of a re-slacked island already has angle
+    0. From a warm start (a converged base case) the whole re-slacked island is rotated by its
+    new reference's angle, so that the reference sits at |v0| + 0j and the island's angle
+    differences are kept; islands that hold a slack bus keep the start as it is. For a flat
+    start this is exactly the reference's rule."""
+    v_start = np.asarray(v_start, dtype=np.complex128)
+    n, L = served.shape
+    is_slack = np.zeros(n, dtype=bool)
+    is_slack[np.asarray(ref, dtype=np.int64)] = True
+    V0 = np.repeat(v_start[:, None], L, axis=1)
+    pin = np.zeros((n, L), dtype=np.uint8)
+    rb = np.asarray(ref_bus, dtype=np.int64)
+    resl = served & ~is_slack[np.where(rb >= 0, rb, 0)]
+    rot = np.exp(-1j * np.angle(v_start))  # e^{-j angle(v_r)} per candidate reference r
+    V0[resl] = V0[resl] * rot[rb[resl]]
+    bus = np.arange(n)[:, None]
+    is_ref = resl & (rb == bus)
+    V0[is_ref] = np.abs(np.broadcast_to(v_start[:, None], V0.shape)[is_ref]) + 0j
+    pin[is_ref] = 1
+    V0[~served] = 1.0 + 0.0j
+    pin[~served] = 1
+    return np.ascontiguousarray(V0), np.ascontiguousarray(pin)
