@@ -179,6 +179,16 @@ int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const u
  * bus keeps its magnitude from V0 (n complex) with the DC angle, slack buses keep V0. Returns 0,
  * or 1 when the DC system is singular or gives non-finite angles (Vout = V0, the flat start). */
 int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* Vout);
+/* Batched DC start: T injection columns Pinj (n, T) [bus][case] (e.g. Sbus.real + the phase-shift
+ * injection per time step or scenario), one shared V0 (n complex), B factored ONCE and every case
+ * substituted on the device. dc_stamps (m x 4 complex, the DC branch stamps (Yff, Yft, Ytf, Ytt)
+ * of the reference's models, TwoPort.py:169-189 create_y_dc_matrix, summed onto the Ybus pattern
+ * at the positions of gbpf_set_branches; their imaginary parts are the reference's Bbus) or NULL
+ * (B from the Ybus as gbpf_dc_start). Vout (n, T) complex; used (T, or NULL): 1 where the DC angles
+ * were taken, 0 where the case keeps V0 (singular B or non-finite angles). Returns 0 when every case
+ * took its DC angles, 1 otherwise, -1 on error. */
+int gbpf_dc_start_batch(gbpf_solver* s, int T, const double* Pinj, const double* V0, const double* dc_stamps,
+                        double* Vout, uint8_t* used);
 /* Block row of each bus (-1 for slack), length n. */
 int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
 
@@ -327,7 +337,8 @@ int gbpf_build_sbus_device(int n, int T, const double* s0, const int64_t* ptr, c
  * i_end = |S_end| / (vn_end |V_end| sqrt 3) (kA); i_max = max; loading = i_max / rating x 100
  * (kind 0, line: rating in kA) or max(i_from vn_from, i_to vn_to) sqrt 3 / rating x 100 (kind
  * 1, trafo: rating in MVA). Case c's outaged branches out_idx[out_ptr[c] ..] (out_ptr NULL:
- * none) report 0, non-converged cases NaN, NaN voltages propagate. V (n, L) complex; outputs
+ * none) report 0, non-converged cases NaN (end powers NaN + 0j, as the reference stores them), NaN
+ * voltages propagate. V (n, L) complex; outputs
  * (nbr, L). */
 int gbpf_branch_flows(int n, int nbr, int L, const int32_t* f, const int32_t* t, const double* y,
                       const double* vn_from, const double* vn_to, const double* rating, const uint8_t* kind,

@@ -1311,54 +1311,87 @@ int gbpf_solve_contingency(gbpf_solver* s, int L, const double* S, const double*
     return 0;
 }
 
-int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* Vout) {
+static int ensure_gather(gbpf_solver* s);
+
+int gbpf_dc_start_batch(gbpf_solver* s, int T, const double* Pinj, const double* V0, const double* dc_stamps,
+                        double* Vout, uint8_t* used) {
     if (!s || !Pinj || !V0 || !Vout) return fail("dc_start: null argument");
-    const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv);
+    if (T <= 0) return fail("dc_start: T must be > 0");
+    if (dc_stamps && !s->m) return fail("dc_start: DC branch stamps need the branch table (gbpf_set_branches)");
+    const size_t n = s->n, nb = s->plan.nblk, nv = std::max(1, s->plan.nv), nnz = s->nnz;
     Shape* sh = nullptr;
     if (int rc = get_shape(s, 1024, 1, &sh)) return rc;
-    std::vector<double> th(n);
-    for (size_t i = 0; i < n; ++i) th[i] = std::atan2(V0[2 * i + 1], V0[2 * i]);
-    DBuf dP, dth, dfac, dR, dy, dout, dpiv;
+    int dev = 0, nsm = 1;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::max(1, std::min(T - 1, 2 * nsm));
+    std::vector<double> th(n * (size_t)T);
+    std::vector<double> th0(n);
+    for (size_t i = 0; i < n; ++i) th0[i] = std::atan2(V0[2 * i + 1], V0[2 * i]);
+    DBuf dP, dth, dfac, dR, dy, dout, dpiv, dB, dst, dsh;
     auto cleanup = [&]() {
-        for (DBuf* b : {&dP, &dth, &dfac, &dR, &dy, &dout, &dpiv}) b->release();
+        for (DBuf* b : {&dP, &dth, &dfac, &dR, &dy, &dout, &dpiv, &dB, &dst, &dsh}) b->release();
     };
     struct Guard {
         std::function<void()> f;
         ~Guard() { f(); }
     } guard{cleanup};
-    CK(dP.ensure(n * 8));
+    const double2* Bx = nullptr;
+    if (dc_stamps) {  // the DC stamps summed onto the Ybus pattern like the AC ones (COO order)
+        if (int rc = ensure_gather(s)) return rc;
+        CK(dst.ensure(64 * (size_t)s->m));
+        CK(dsh.ensure(16 * n));
+        CK(dB.ensure(16 * nnz));
+        CK(cudaMemcpyAsync(dst.p, dc_stamps, 64 * (size_t)s->m, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemsetAsync(dsh.p, 0, 16 * n, s->stream));
+        CK(gbpf::launch_ybus_gather((int)nnz, 4 * s->m, s->dg_ptr.as<int>(), s->dg_src.as<int>(), dst.as<double2>(),
+                                    dsh.as<double2>(), dB.as<double2>(), nullptr, s->stream));
+        Bx = dB.as<double2>();
+    }
+    CK(dP.ensure(n * 8 * T));
     CK(dth.ensure(n * 8));
     CK(dfac.ensure((nb + nv) * 32));
-    CK(dR.ensure(nv * 16));
-    CK(dy.ensure(nv * 16));
-    CK(dout.ensure(n * 8));
+    CK(dR.ensure(nv * 16 * grid));
+    CK(dy.ensure(nv * 16 * grid));
+    CK(dout.ensure(n * 8 * T));
     CK(dpiv.ensure(16));
-    CK(cudaMemcpyAsync(dP.p, Pinj, n * 8, cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(dth.p, th.data(), n * 8, cudaMemcpyHostToDevice, s->stream));
-    CK(gbpf::launch_dc(sh->dp, dP.as<double>(), dth.as<double>(), dfac.as<double4_32a>(), dR.as<double2>(),
-                       dy.as<double2>(), dout.as<double>(), dpiv.as<unsigned long long>(), s->stream));
+    CK(cudaMemcpyAsync(dP.p, Pinj, n * 8 * T, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dth.p, th0.data(), n * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(gbpf::launch_dc(sh->dp, Bx, dP.as<double>(), T, dth.as<double>(), dfac.as<double4_32a>(), dR.as<double2>(),
+                       dy.as<double2>(), dout.as<double>(), dpiv.as<unsigned long long>(), grid, s->stream));
     unsigned long long piv[2];
-    CK(cudaMemcpyAsync(th.data(), dout.p, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(th.data(), dout.p, n * 8 * T, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(piv, dpiv.p, 16, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     // a zero or non-finite pivot (a DC island without a reference) or non-finite angles:
-    // the reference keeps the flat start then (timeseries.py:244-247)
+    // the case keeps the flat start (timeseries.py:244-247)
     double mn, mx;
     std::memcpy(&mn, &piv[0], 8);
     std::memcpy(&mx, &piv[1], 8);
-    bool ok = std::isfinite(mx) && mn > 0.0;
-    for (size_t i = 0; i < n && ok; ++i) ok = std::isfinite(th[i]);
-    for (size_t i = 0; i < n; ++i) {
-        const double vm = std::hypot(V0[2 * i], V0[2 * i + 1]);
-        if (!ok || s->plan.row_of_bus[i] < 0) {
-            Vout[2 * i] = V0[2 * i];
-            Vout[2 * i + 1] = V0[2 * i + 1];
-        } else {
-            Vout[2 * i] = vm * std::cos(th[i]);
-            Vout[2 * i + 1] = vm * std::sin(th[i]);
+    const bool piv_ok = std::isfinite(mx) && mn > 0.0;
+    bool all = true;
+    for (int c = 0; c < T; ++c) {
+        bool ok = piv_ok;
+        for (size_t i = 0; i < n && ok; ++i) ok = std::isfinite(th[i * T + c]);
+        all = all && ok;
+        if (used) used[c] = ok ? 1 : 0;
+        for (size_t i = 0; i < n; ++i) {
+            const size_t o = 2 * (i * T + c);
+            if (!ok || s->plan.row_of_bus[i] < 0) {
+                Vout[o] = V0[2 * i];
+                Vout[o + 1] = V0[2 * i + 1];
+            } else {
+                const double vm = std::hypot(V0[2 * i], V0[2 * i + 1]);
+                Vout[o] = vm * std::cos(th[i * T + c]);
+                Vout[o + 1] = vm * std::sin(th[i * T + c]);
+            }
         }
     }
-    return ok ? 0 : 1;
+    return all ? 0 : 1;
+}
+
+int gbpf_dc_start(gbpf_solver* s, const double* Pinj, const double* V0, double* Vout) {
+    return gbpf_dc_start_batch(s, 1, Pinj, V0, nullptr, Vout, nullptr);
 }
 
 int gbpf_eval_jacobian(gbpf_solver* s, const double* S, const double* V, const uint8_t* pin, double* blocks,
@@ -1491,28 +1524,33 @@ int gbpf_set_branches(gbpf_solver* s, int m, const int32_t* f, const int32_t* t,
     return 0;
 }
 
+// Gather lists of the Ybus sum: the contributions of every CSR entry in the order a COO sum of
+// the stamps meets them (all Yff, then Yft, Ytf, Ytt, each in branch order; TwoPort.py:133-149),
+// the bus shunt last. Built once per branch table.
+static int ensure_gather(gbpf_solver* s) {
+    if (s->gather_ready) return 0;
+    const int m = s->m, n = s->n, nnz = s->nnz;
+    std::vector<std::vector<int>> lists(nnz);
+    for (int q = 0; q < 4; ++q)
+        for (int e = 0; e < m; ++e) lists[s->br_pos[4 * (size_t)e + q]].push_back(4 * e + q);
+    for (int i = 0; i < n; ++i)
+        if (s->plan.ydiag[i] >= 0) lists[s->plan.ydiag[i]].push_back(4 * m + i);
+    std::vector<int> ptr(nnz + 1, 0), src;
+    for (int k = 0; k < nnz; ++k) {
+        ptr[k + 1] = ptr[k] + (int)lists[k].size();
+        src.insert(src.end(), lists[k].begin(), lists[k].end());
+    }
+    CK(upload(s->dg_ptr, ptr));
+    CK(upload(s->dg_src, src));
+    s->gather_ready = true;
+    return 0;
+}
+
 int gbpf_update_Y_from_branches(gbpf_solver* s, const double* stamps, const double* bus_shunt) {
     if (!s || !stamps) return fail("update_Y_from_branches: null argument");
     if (!s->m) return fail("update_Y_from_branches: the branch table is not set (gbpf_set_branches)");
     const int m = s->m, n = s->n, nnz = s->nnz;
-    if (!s->gather_ready) {
-        // contributions of every CSR entry in the order a COO sum of the stamps meets them
-        // (all Yff, then Yft, Ytf, Ytt, each in branch order; TwoPort.py:133-149), the bus
-        // shunt last
-        std::vector<std::vector<int>> lists(nnz);
-        for (int q = 0; q < 4; ++q)
-            for (int e = 0; e < m; ++e) lists[s->br_pos[4 * (size_t)e + q]].push_back(4 * e + q);
-        for (int i = 0; i < n; ++i)
-            if (s->plan.ydiag[i] >= 0) lists[s->plan.ydiag[i]].push_back(4 * m + i);
-        std::vector<int> ptr(nnz + 1, 0), src;
-        for (int k = 0; k < nnz; ++k) {
-            ptr[k + 1] = ptr[k] + (int)lists[k].size();
-            src.insert(src.end(), lists[k].begin(), lists[k].end());
-        }
-        CK(upload(s->dg_ptr, ptr));
-        CK(upload(s->dg_src, src));
-        s->gather_ready = true;
-    }
+    if (int rc = ensure_gather(s)) return rc;
     std::vector<double> sh(2 * (size_t)n, 0.0);
     if (bus_shunt) sh.assign(bus_shunt, bus_shunt + 2 * (size_t)n);
     CK(upload(s->dshunt, sh));

@@ -158,9 +158,12 @@ ScratchOffsets scratch_offsets(int n, int nv, int nblk, int G, bool mixed);
 
 // host-side launchers (gbpf_kernels.cu)
 cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream);
-// DC start with the block LU of a (1024 threads, 1 slot) schedule; piv = (min, max) pivot bits
-cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_bus, double4_32a* fac, double2* R,
-                      double2* y, double* theta, unsigned long long* piv, cudaStream_t stream);
+// DC start of T cases ([bus][case] injections and angles) with the block LU of a (1024 threads,
+// 1 slot) schedule: B factored once (Bx: caller's susceptances on the Ybus pattern, or null:
+// from the Ybus), every case substituted; R / y hold `grid` rows of nv; piv = (min, max) pivot bits
+cudaError_t launch_dc(const DevPlan& P, const double2* Bx, const double* Pinj, int T, const double* theta_bus,
+                      double4_32a* fac, double2* R, double2* y, double* theta, unsigned long long* piv, int grid,
+                      cudaStream_t stream);
 cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2* Sbus, const uint8_t* pin,
                               double4_32a* Vt, double2* Et, double* Ei, float* iv32, double4_32a* blocks,
                               double2* R, cudaStream_t stream);

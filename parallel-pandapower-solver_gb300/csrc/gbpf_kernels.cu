@@ -1294,16 +1294,46 @@ cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* ta
     return cudaGetLastError();
 }
 
-// DC start (NewtonPowerflowCpp.py:422-440 _pre_dc_solve): B[pvpq, pvpq] theta = Pinj[pvpq] -
-// B[pvpq, ref] theta_ref with B the branch susceptance Laplacian (B_ij = -Im Y_ij off the
-// diagonal, B_ii = -sum of the row's off-diagonal B_ij: no shunts, no tap asymmetry -- the DC
-// model), factored and solved by the Newton kernel's block LU (one case: every 2x2 block
-// carries B in its angle / P entry and the identity in its magnitude / Q entry). One CTA of
-// NTB threads; the plan's schedule has NTB workers.
+// DC start (NewtonPowerflowCpp.py:422-440 _pre_dc_solve, timeseries.py:200-247
+// dc_initial_voltage): B[pvpq, pvpq] theta = Pinj[pvpq] - B[pvpq, ref] theta_ref, factored and
+// solved by the Newton kernel's block LU (every 2x2 block carries B in its angle / P entry and
+// the identity in its magnitude / Q entry). B is either the caller's DC susceptance matrix on
+// the Ybus pattern (Bx: the imaginary parts of the summed DC branch stamps, diagonal included,
+// as the reference's make_ybus builds its Bbus, NewtonPowerflowCpp.py:64-161) or, with Bx null,
+// derived from the Ybus (-Im Y off the diagonal, the negated row sum on it). The plan's
+// schedule has NTB workers and one slot.
+template <bool BLOCKS>
+__device__ void dc_assemble(const DevPlan& P, const double2* Bx, const double* Pinj, long long sP,
+                            const double* theta_bus, double4_32a* fac, double2* R) {
+    for (int i = threadIdx.x; i < P.n; i += blockDim.x) {
+        const int row = P.row_of_bus[i];
+        if (row < 0) continue;
+        double rhs = Pinj[(size_t)i * sP], diag = 0.0;
+        for (int k = P.Yp[i]; k < P.Yp[i + 1]; ++k) {
+            const int j = P.Yj[k];
+            if (j == i) {
+                if (Bx) diag = Bx[k].y;
+                continue;
+            }
+            const double b = Bx ? Bx[k].y : -P.Y[k].y;
+            if (!Bx) diag -= b;
+            const int q = P.posmap[k];
+            if (q >= 0) {
+                if (BLOCKS) fac[q] = make_double4_32a(b, 0.0, 0.0, 0.0);
+            } else if (P.row_of_bus[j] < 0) {
+                rhs -= b * theta_bus[j];  // coupling to a reference bus at its angle
+            }
+        }
+        if (BLOCKS) fac[P.dpos[row]] = make_double4_32a(diag, 0.0, 0.0, 1.0);
+        R[row] = make_double2(rhs, 0.0);
+    }
+}
+
+// Case 0: factors B (one CTA) and solves its right-hand side; theta column 0.
 template <int NTB>
-__global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const double* Pinj, const double* theta_bus,
-                                                    double4_32a* fac, double2* R, double2* y, double* theta,
-                                                    unsigned long long* piv) {
+__global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const double2* Bx, const double* Pinj, long long sP,
+                                                    const double* theta_bus, double4_32a* fac, double2* R, double2* y,
+                                                    double* theta, long long sT, unsigned long long* piv) {
     __shared__ int s_on[1];
     __shared__ unsigned long long s_min[1], s_max[1];
     const int tid = threadIdx.x;
@@ -1312,33 +1342,49 @@ __global__ void __launch_bounds__(NTB, 1) dc_kernel(const DevPlan P, const doubl
         s_min[0] = ~0ULL;
         s_max[0] = 0ULL;
     }
-    for (int i = tid; i < P.n; i += NTB) {
-        const int row = P.row_of_bus[i];
-        if (row < 0) continue;
-        double rhs = Pinj[i], diag = 0.0;
-        for (int k = P.Yp[i]; k < P.Yp[i + 1]; ++k) {
-            const int j = P.Yj[k];
-            if (j == i) continue;
-            const double b = -P.Y[k].y;
-            diag -= b;
-            const int q = P.posmap[k];
-            if (q >= 0)
-                fac[q] = make_double4_32a(b, 0.0, 0.0, 0.0);
-            else if (P.row_of_bus[j] < 0)
-                rhs -= b * theta_bus[j];  // coupling to a reference bus at its angle
-        }
-        fac[P.dpos[row]] = make_double4_32a(diag, 0.0, 0.0, 1.0);
-        R[row] = make_double2(rhs, 0.0);
-    }
+    dc_assemble<true>(P, Bx, Pinj, sP, theta_bus, fac, R);
     __syncthreads();
     lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max, nullptr, true, nullptr);
     for (int i = tid; i < P.n; i += NTB) {
         const int row = P.row_of_bus[i];
-        theta[i] = row < 0 ? theta_bus[i] : y[row].x;
+        theta[(size_t)i * sT] = row < 0 ? theta_bus[i] : y[row].x;
     }
     if (tid == 0) {
         piv[0] = s_min[0];
         piv[1] = s_max[0];
+    }
+}
+
+// Cases 1 .. T-1: the factors of case 0 reused (B is the same for every case), substitutions
+// only; each CTA takes cases blockIdx.x + 1, + gridDim.x, ... with its own R / y rows.
+template <int NTB>
+__global__ void __launch_bounds__(NTB, 1) dc_solve_kernel(const DevPlan P, const double2* Bx, const double* Pinj,
+                                                          long long sP, int T, const double* theta_bus,
+                                                          double4_32a* fac, double2* Rs, double2* ys, double* theta,
+                                                          long long sT) {
+    __shared__ int s_on[1], s_chord[1];
+    __shared__ unsigned long long s_min[1], s_max[1];
+    const int tid = threadIdx.x;
+    const int nv = P.nv > 0 ? P.nv : 1;
+    double2* R = Rs + (size_t)blockIdx.x * nv;
+    double2* y = ys + (size_t)blockIdx.x * nv;
+    if (tid == 0) {
+        s_on[0] = 1;
+        s_chord[0] = 1;
+    }
+    for (int c = blockIdx.x + 1; c < T; c += gridDim.x) {
+        if (tid == 0) {
+            s_min[0] = ~0ULL;
+            s_max[0] = 0ULL;
+        }
+        dc_assemble<false>(P, Bx, Pinj + c, sP, theta_bus, fac, R);
+        __syncthreads();
+        lu_pass<double>(P, fac, R, y, s_on, 0, s_min, s_max, s_chord, false, nullptr);
+        for (int i = tid; i < P.n; i += NTB) {
+            const int row = P.row_of_bus[i];
+            theta[(size_t)i * sT + c] = row < 0 ? theta_bus[i] : y[row].x;
+        }
+        __syncthreads();
     }
 }
 
@@ -1443,9 +1489,13 @@ void start_carve(StartJob& sj, char* base, int n, int nv, int nblk, int G, bool 
     sj.ok0 = reinterpret_cast<int*>(take(4));
 }
 
-cudaError_t launch_dc(const DevPlan& P, const double* Pinj, const double* theta_bus, double4_32a* fac, double2* R,
-                      double2* y, double* theta, unsigned long long* piv, cudaStream_t stream) {
-    dc_kernel<1024><<<1, 1024, 0, stream>>>(P, Pinj, theta_bus, fac, R, y, theta, piv);
+cudaError_t launch_dc(const DevPlan& P, const double2* Bx, const double* Pinj, int T, const double* theta_bus,
+                      double4_32a* fac, double2* R, double2* y, double* theta, unsigned long long* piv, int grid,
+                      cudaStream_t stream) {
+    dc_kernel<1024><<<1, 1024, 0, stream>>>(P, Bx, Pinj, T, theta_bus, fac, R, y, theta, T, piv);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || T <= 1) return e;
+    dc_solve_kernel<1024><<<grid, 1024, 0, stream>>>(P, Bx, Pinj, T, T, theta_bus, fac, R, y, theta, T);
     return cudaGetLastError();
 }
 

@@ -80,8 +80,10 @@ __global__ void __launch_bounds__(TB) flow_kernel(int nbr, int L, const int* __r
             for (int q = out_ptr[c]; q < out_ptr[c + 1]; ++q) out |= out_idx[q] == b;
         if (out || !conv[c]) {  // a non-converged case wins over an outage (NaN, not 0)
             const double z = conv[c] ? 0.0 : nan;
-            Sf[o] = make_double2(z, z);
-            St[o] = make_double2(z, z);
+            // the reference stores a real NaN into its complex end powers (find_overloads.py:
+            // 246-250), i.e. NaN + 0j: the reactive powers of a non-converged case read 0
+            Sf[o] = make_double2(z, 0.0);
+            St[o] = make_double2(z, 0.0);
             If[o] = It[o] = Imax[o] = load[o] = z;
             continue;
         }

@@ -129,6 +129,7 @@ SIGNATURES = {
     "gbpf_solve_contingency": (C.c_int, [_vp, C.c_int, _dp, _dp, _bp, _dp, _ip, _ip, _dp, C.POINTER(Params), _dp,
                                          _ip, _bp]),
     "gbpf_dc_start": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "gbpf_dc_start_batch": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _bp]),
     "gbpf_eval_jacobian": (C.c_int, [_vp, _dp, _dp, _bp, _dp, _dp]),
     "gbpf_selftest_conversions": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
     "gbpf_selftest_math": (C.c_int, [_dp, C.c_int, _dp, _dp, _dp, _dp, _dp]),

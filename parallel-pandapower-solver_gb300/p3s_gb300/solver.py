@@ -326,18 +326,34 @@ class GpuSolver:
         _lib.check(rc, "solve_batch_contingency")
         return {"V": V, "iterations": it, "converged": cv.astype(bool)}
 
-    def dc_start(self, Pinj, V0):
+    def dc_start(self, Pinj, V0, dc_stamps=None):
         """DC start voltage (``dc_initial_voltage``): DC angles at every non-slack bus with V0's
-        magnitudes; V0 itself when the DC system is singular. Returns (V, used_dc)."""
-        P = np.ascontiguousarray(np.asarray(Pinj, dtype=np.float64).ravel())
+        magnitudes; V0 itself when the DC system is singular. Pinj (n,) or (n, T): one or T cases
+        (time steps, scenarios) solved with ONE factorization of B. dc_stamps: (m, 4) complex DC
+        branch stamps of the reference's models (``ybus.branch_stamps`` of the ``ys_dc`` two-ports,
+        at the positions of ``set_branches``) -- B is then the reference's Bbus; None: B from the
+        Ybus. Returns (V, used) -- V and used shaped like Pinj's cases (used: DC angles taken)."""
+        P = np.asarray(Pinj, dtype=np.float64)
+        one = P.ndim == 1
+        P = np.ascontiguousarray(P.reshape(self.n, -1) if P.size else P)
         V0 = c128(np.asarray(V0).ravel())
-        if P.shape != (self.n,) or V0.shape != (self.n,):
-            raise ValueError("dc_start: Pinj and V0 must be (n_bus,)")
-        out = np.empty(self.n, dtype=np.complex128)
-        rc = _lib.load().gbpf_dc_start(self._h, _lib.d(P), _lib.cview(V0), _lib.cview(out))
+        if P.ndim != 2 or P.shape[0] != self.n or P.shape[1] < 1 or V0.shape != (self.n,):
+            raise ValueError("dc_start: Pinj must be (n_bus,) or (n_bus, T) and V0 (n_bus,)")
+        T = P.shape[1]
+        st = None
+        if dc_stamps is not None:
+            st = c128(dc_stamps)
+            if st.shape != (getattr(self, "branches", -1), 4):
+                raise ValueError("dc_start: dc_stamps must be (n_branch, 4) complex (after set_branches)")
+        out = np.empty((self.n, T), dtype=np.complex128)
+        used = np.empty(T, dtype=np.uint8)
+        rc = _lib.load().gbpf_dc_start_batch(self._h, T, _lib.d(P), _lib.cview(V0),
+                                             None if st is None else _lib.cview(st), _lib.cview(out), _lib.u8(used))
         if rc < 0:
             raise RuntimeError(_lib.last_error())
-        return out, rc == 0
+        if one:
+            return out[:, 0], bool(used[0])
+        return out, used.astype(bool)
 
     # -------------------------------------------------------------- Jacobian
     def eval_blocks(self, S, V, pin=None):

@@ -57,7 +57,7 @@ def test_branch_loading_of_an_n1_sweep_matches_the_restated_reference():
     assert np.isnan(tab.i_ka[touch, c]).all()
 
 
-def test_dc_start_matches_the_restated_reference_and_starts_newton():
+def test_dc_start_from_the_ybus_matches_the_restated_reference_and_starts_newton():
     from oracle import cpu
     from oracle.postproc import dc_initial_voltage
     from p3s_gb300.solver import GpuSolver
@@ -121,3 +121,92 @@ def test_ybus_from_branch_stamps_on_the_device():
     S = g.Sbus[:, None] * np.ones((1, 4))
     r1, r2 = s.solve_batch(S, g.V0, p), host.solve_batch(S, g.V0, p)
     assert np.array_equal(r1["V"], r2["V"]) and np.array_equal(r1["iterations"], r2["iterations"])
+
+
+def _device_element_stamps():
+    """Device stamps (AC and DC) of the golden element tables, and the solver holding the
+    118-bus grid's branch table with the element Ybus summed on the device."""
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.ybus import branch_stamps
+    from test_postproc_cpu import golden_two_ports
+
+    d, tp = golden_two_ports()
+    g = grid_118()
+    flags = (tp["in_service"], tp["open_from"], tp["open_to"])
+    st = branch_stamps(tp["ys"], tp["y_from"], tp["y_to"], tp["a"], tp["b"], *flags)
+    dc = branch_stamps(tp["ys_dc"], 0.0, 0.0, 1.0, 1.0, *flags)
+    s = GpuSolver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    is_slack = np.zeros(g.n, np.uint8)
+    is_slack[g.ref] = 1
+    s.set_branches(g.f, g.t, g.stamp_pos, g.stamp, is_slack)
+    s.update_Y_from_branches(st, d["shunt"])
+    return d, tp, g, st, dc, s
+
+
+def test_ybus_from_element_tables_matches_the_reference_models():
+    """Element tables -> two-ports (host) -> stamps with out-of-service masks and open-end Kron
+    elimination -> Ybus summed, both on the device, against the Ybus the reference's own
+    TransmissionLineModel / TwoWindingTransformerModel / create_y_matrix built (golden_post.npz);
+    1e-13 of the largest entry (the device divides complex numbers by another formula)."""
+    d, tp, g, st, dc, s = _device_element_stamps()
+    assert np.abs(s.Yx - d["Ybus"]).max() <= 1e-13 * np.abs(d["Ybus"]).max()
+    assert (st[~tp["in_service"]] == 0).all() and (st[tp["open_from"] | tp["open_to"]][:, 1:3] == 0).all()
+
+
+def test_branch_loading_matches_the_reference_compute_branch_loading():
+    """Branch flows of the reference's own compute_branch_loading (line and transformer tables,
+    outaged branches 0, non-converged cases NaN, NaN voltages propagating) from the device
+    stamps of the same element tables (values 1e-11 relative / 1e-10 absolute)."""
+    from p3s_gb300.flows import branch_flows
+
+    d, tp, g, st, dc, s = _device_element_stamps()
+    V, conv = d["V_flows"], d["converged_flows"]
+    L = V.shape[1]
+    vn = d["bus_vn_kv"]
+    for el, rows in (("line", d["line_branches"]), ("trafo", d["trafo_branches"])):
+        local = -np.ones(g.n_branch, np.int64)
+        local[rows] = np.arange(len(rows))
+        # case c > 0 of the N-1 voltages has branch c - 1 out (its outage group)
+        hit = [local[c - 1] if c > 0 and local[c - 1] >= 0 else -1 for c in range(L)]
+        ptr = np.zeros(L + 1, np.int32)
+        ptr[1:] = np.cumsum([h >= 0 for h in hit])
+        idx = np.array([h for h in hit if h >= 0], np.int32)
+        if el == "line":
+            vf = vt = vn[d["line__from_bus"]]
+            rating, kind = d["line__max_i_ka"], 0
+        else:
+            vf, vt = vn[d["trafo__hv_bus"]], vn[d["trafo__lv_bus"]]
+            rating, kind = d["trafo__sn_mva"], 1
+        got = branch_flows(g.f[rows], g.t[rows], st[rows], V, conv, vf, vt, rating, kind, float(d["sn_mva"]),
+                           (ptr, idx))
+        pairs = ((got["S_from"].real, "p_from_mw"), (got["S_from"].imag, "q_from_mvar"),
+                 (got["S_to"].real, "p_to_mw"), (got["S_to"].imag, "q_to_mvar"), (got["i_from"], "i_from_ka"),
+                 (got["i_to"], "i_to_ka"), (got["i_max"], "i_ka"), (got["loading"], "loading_percent"))
+        out = d[f"{el}__res__outaged"]
+        assert out.any()
+        for a, k in pairs:
+            b = d[f"{el}__res__{k}"]
+            assert np.array_equal(np.isnan(a), np.isnan(b)), k
+            assert np.array_equal(a[out & conv[None, :]], b[out & conv[None, :]]), k  # zeros
+            m = ~np.isnan(b)
+            assert np.allclose(a[m], b[m], rtol=1e-11, atol=1e-10), k
+
+
+def test_batched_dc_start_matches_the_reference_dc_initial_voltage():
+    """The reference's dc_initial_voltage (its own Bbus of DC branch stamps, phase-shift
+    injection, _pre_dc_solve) for the base injections and four scenarios, against the device's
+    batched DC start (B factored once from the device DC stamps, five substitutions): angles
+    within 1e-10 rad, magnitudes kept; one column alone gives the same bits as in the batch."""
+    d, tp, g, st, dc, s = _device_element_stamps()
+    Pinj = np.ascontiguousarray(d["S_dc"].real + d["p_shift"][:, None])
+    V, used = s.dc_start(Pinj, g.V0, dc_stamps=dc)
+    assert used.all()
+    ref = d["V_dc"]
+    assert np.abs(np.angle(V * np.conj(ref))).max() < 1e-10
+    assert np.allclose(np.abs(V), np.abs(ref), rtol=1e-15, atol=0)
+    assert np.abs(np.angle(ref)).max() > 0.3  # phase shifters: the shift injection matters
+    one, ok = s.dc_start(Pinj[:, 2], g.V0, dc_stamps=dc)
+    assert ok and np.array_equal(one, V[:, 2])
+    # the Ybus-derived B (the DC start without element data) still starts Newton
+    V2, used2 = s.dc_start(np.ascontiguousarray(g.Sbus.real[:, None] * np.ones((1, 3))), g.V0)
+    assert used2.all() and np.array_equal(V2[:, 0], V2[:, 2])
