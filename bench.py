@@ -1,8 +1,11 @@
 """Benchmark: batched AC power flow solves/s on one GB300 (the 2,000-bus x 8,760-hour series).
 
 One step = one pass of the Newton path over the whole workload: the 2,000-bus grid's
-8,760 hourly cases, chained hour to hour in warm-start lanes, solved to <= 1e-8 p.u.
-mismatch by ONE launch of the persistent sm_103a kernel.
+8,760 hourly cases, each hour starting from the converged base case (K = T lanes: the
+reference's own time-series semantics), solved to <= 1e-8 p.u. mismatch by ONE launch of the
+persistent sm_103a kernel (with its start-table, shared-start and replication prologue kernels).
+Beside it (`warm_lanes`): the same hours in K = 730 twelve-hour warm-start lanes, hour h of a
+lane starting from hour h-1's converged voltage, with the oracle's replay of the same lanes.
 
   value : solves/s with inputs resident in HBM (CUDA events around the kernel, solver stream)
   e2e   : solves/s through the public API (p3s_gb300.solver.GpuSolver.solve_lanes_async /
@@ -10,6 +13,8 @@ mismatch by ONE launch of the persistent sm_103a kernel.
           inside the timed region, two steps in flight so one's copies overlap the other's
           kernel (wall clock over the steps); single_call_ms: one call alone
   fp64  : the same for the plain double-precision path (the headline value is the mixed path)
+  roofline.phases : the Newton kernel's time split by phase (SM clock counters of one extra
+          instrumented launch, shares of the CTA time) with each phase's algorithmic bytes
 
 Beside the headline (rank 0, outside the timed steps): the full N-1 sweep of the same grid
 (3,001 cases), the uneven multi-grid batch (256 grids x 16 scenarios in one launch), and the
@@ -132,6 +137,57 @@ def algorithmic_bytes(info: dict, g, mixed: bool):
     per_iteration = (3 * n * 8 + 2 * n * 8 + b * nnzJ + 8 * m) + (b * nnzLU + 16 * m) + (8 * m + 6 * n * 8)
     per_factorization = b * nnzJ + b * nnzLU
     return per_iteration, per_factorization
+
+
+def phase_bytes(info: dict, g, mixed: bool, iterations: int, factorizations: int) -> dict:
+    """The traffic model split by the Newton kernel's phases for one launch: the evaluation;
+    the factorization fused with the forward substitution (the refactorization term per
+    factorization, plus half of the substitutions' term per case-iteration); the backward
+    substitution (the other half); the voltage update. Refill / load and the decision move no
+    modelled bytes."""
+    n = g.n
+    m = len(g.pv) + 2 * len(g.pq)
+    from p3s_gb300.topology import jacobian_pattern
+
+    nnzJ = len(jacobian_pattern(g.Yp, g.Yj, g.pv, g.pq)[1])
+    nnzLU = 4 * info["n_blocks"]
+    b = 4 if mixed else 8
+    half_solve = b * nnzLU / 2 + 8 * m
+    return {"eval": iterations * (3 * n * 8 + 2 * n * 8 + b * nnzJ + 8 * m),
+            "factor_forward": factorizations * (b * nnzJ + b * nnzLU) + iterations * half_solve,
+            "backward": iterations * half_solve, "step": iterations * (8 * m + 6 * n * 8), "load": 0.0,
+            "decide": 0.0}
+
+
+def phase_table(cycles: dict, kernel_ms: float, bytes_: dict, peak: float) -> dict:
+    """Per phase: its share of the kernel's CTA time (SM clock counters), that share of the
+    kernel time, its algorithmic bytes and the bandwidth they make over that time."""
+    total = float(sum(cycles.values())) or 1.0
+    out = {}
+    for k, c in cycles.items():
+        share = c / total
+        ms = share * kernel_ms
+        gb = bytes_.get(k, 0.0) / 1e9
+        row = {"share": round(share, 4), "ms": round(ms, 3), "algorithmic_GB": round(gb, 3)}
+        if gb > 0 and ms > 0:
+            row["achieved_GBps"] = round(gb / (ms * 1e-3), 1)
+            row["frac"] = round(gb / (ms * 1e-3) / peak, 4)
+        out[k] = row
+    return out
+
+
+def headline_config(g, T: int, K: int) -> dict:
+    """The timed workload, the same dict in the GPU line and the reference line."""
+    return {
+        "workload": f"2,000-bus grid x {T} hourly cases, K={K} warm-start lanes (hour h of a lane starts from "
+                    f"hour h-1's converged voltage, a lane's first hour from the converged base case; K = {T}: "
+                    f"every hour starts from the converged base case, the reference's time-series semantics)",
+        "n_bus": g.n, "n_branch": g.n_branch, "n_pv": len(g.pv), "n_pq": len(g.pq), "hours": T, "lanes": K,
+        "tol_pu": 1e-8, "max_iter": 30,
+        "injection_scale": round(float(g.loading), 6),
+        "start": "the converged base case, solved once outside the timed region",
+        "l2": "inputs larger than L2 (S is 280 MB per step; L2 is 129 MB)",
+    }
 
 
 def algorithmic_bytes_per_iteration(info: dict, g, mixed: bool) -> float:
@@ -266,6 +322,41 @@ def run_gpu(args, rank, world, local):
         out[prec] = dict(ms=float(np.mean(ms)), wall_ms=wall * 1e3 / args.steps, it=it, cv=cv, stats=stats,
                          clocks=clocks.summary())
 
+    # the Newton kernel's time by phase: one instrumented launch per precision, outside the timed
+    # steps (SM clock counters at the phase barriers, summed over the CTAs)
+    for prec in ("mixed", "double"):
+        dev_step(GpuSolver.params(precision=prec, mixed_switch=args.mixed_switch, phase_timers=True))
+        out[prec]["phase_cycles"] = solver.stats["phase_cycles"]
+
+    # the same hours in K = 730 twelve-hour warm-start lanes (hour h from hour h-1's converged
+    # voltage): both precisions timed like the headline, the oracle's replay of the same lanes
+    # on the host cores beside them
+    K_warm = min(730, T)
+    off_w = lanes(T, K_warm).astype(np.int64)
+    doff_w = torch.from_numpy(off_w).to(dev)
+    warm = {"lanes": K_warm}
+    for prec in ("mixed", "double"):
+        p = GpuSolver.params(precision=prec, mixed_switch=args.mixed_switch)
+
+        def warm_step():
+            solver.solve_lanes_device(dS.data_ptr(), dV0.data_ptr(), doff_w.data_ptr(), T, K_warm, p, dV.data_ptr(),
+                                      dit.data_ptr(), dcv.data_ptr())
+            return solver.stats["kernel_ms"]
+
+        for _ in range(args.warmup):
+            warm_step()
+        ms = [warm_step() for _ in range(max(3, args.steps // 2))]
+        it = dit.cpu().numpy()
+        warm["fp64" if prec == "double" else prec] = {
+            "value": round(world * T / (np.mean(ms) * 1e-3), 1), "unit": "solves/s",
+            "ms_per_step": round(float(np.mean(ms)), 3), "iterations_mean": float(it.mean()),
+            "converged": bool(dcv.cpu().numpy().all())}
+    if rank == 0:
+        best = min(cpu_solve(g, S, K_warm, V0)[0] for _ in range(3))
+        warm["cpu_baseline"] = {"value": round(T / best, 1), "unit": "solves/s", "cores": cpu_cores(), "kind": "port",
+                                "sample": f"all {T} hours in the same {K_warm} lanes (the oracle's lane replay), "
+                                          f"best of 3, oracle/liboracle.so (OpenMP, {cpu_cores()} threads)"}
+
     # accuracy of the mixed result against the oracle's mismatch on a few hours
     p = GpuSolver.params(precision="mixed", mixed_switch=args.mixed_switch)
     dev_step(p)
@@ -329,7 +420,8 @@ def run_gpu(args, rank, world, local):
     d2h = bufs[0][1].nbytes + bufs[0][2].nbytes + bufs[0][3].nbytes
 
     res = dict(out=out, e2e_ms=e2e_wall, e2e_single_ms=float(np.min(single)), h2d=h2d, d2h=d2h, info=info,
-               K=len(off) - 1, T=T, worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish, vtol=p.vtol)
+               K=len(off) - 1, T=T, worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish, vtol=p.vtol,
+               warm=warm)
     return res
 
 
@@ -495,6 +587,14 @@ def gpu_line(args, res, rank, world):
         "chord_steps_per_launch": int(mixed["stats"].get("chord_steps", 0)),
         "first_steps_per_launch": int(mixed["stats"].get("first_steps", 0)),
     }
+    peak = hbm if hbm else 6800.0
+    roof["phases"] = phase_table(mixed["phase_cycles"], mixed["ms"],
+                                 phase_bytes(info, g, True, its_mixed, n_fac), peak)
+    roof["phases_source"] = ("SM clock counters at the Newton kernel's phase barriers, summed over its CTAs, of one "
+                             "instrumented launch (gbpf_params.phase_timers); ms = the phase's share of the CTA time x "
+                             "the timed kernel time; bytes from the per-case-iteration traffic model")
+    its_dbl = int(dbl["it"].sum())
+    n_fac_dbl = int(dbl["stats"]["single_factorizations"] + dbl["stats"]["double_factorizations"])
     # fp64 pipe roofline of the double path (GB300: ~1.2 TFLOP/s)
     fp64 = {
         "value": round(world * T / (ms_dbl * 1e-3), 1),
@@ -504,6 +604,7 @@ def gpu_line(args, res, rank, world):
         "achieved_GBps": round(algorithmic_bytes_per_iteration(info, g, False) * int(dbl["it"].sum())
                                / (dbl["ms"] * 1e-3) / 1e9, 1),
         "clocks": dbl["clocks"],
+        "phases": phase_table(dbl["phase_cycles"], dbl["ms"], phase_bytes(info, g, False, its_dbl, n_fac_dbl), peak),
     }
     cb = cpu_baseline(res["g"], args, res["K"])
     line = {
@@ -519,23 +620,19 @@ def gpu_line(args, res, rank, world):
         "vs_baseline": None,
         "dtype": "f32 Jacobian/LU + f64 mismatch/update",
         "data": "synthetic (seeded 2,000-bus grid and 8,760-hour load/generation series)",
-        "config": {
-            "workload": f"2,000-bus grid x {T} hourly cases, warm-start lanes K={res['K']} "
-                        f"(hour h of a lane starts from hour h-1's converged voltage, a lane's first hour "
-                        f"from the converged base case; K = {T} starts every hour from it)",
-            "n_bus": g.n, "n_branch": g.n_branch, "n_pv": len(g.pv), "n_pq": len(g.pq), "hours": T,
-            "lanes": res["K"], "tol_pu": 1e-8, "max_iter": 30, "precision": "mixed",
-            "mixed_switch": args.mixed_switch,
-            "cases_per_cta": info["cases_per_cta"], "grid_ctas": mixed["stats"]["grid"],
-            "l2": "inputs larger than L2 (S is 280 MB per step; L2 is 129 MB)",
+        "config": headline_config(g, T, res["K"]),
+        "run": {
+            "precision": "mixed", "mixed_switch": args.mixed_switch, "shared_start": True,
+            "cases_per_cta": info["cases_per_cta"], "threads_per_cta": info["threads_per_cta"],
+            "grid_ctas": mixed["stats"]["grid"],
             "iterations_mean": float(mixed["it"].mean()), "converged": bool(mixed["cv"].all()),
             "max_mismatch_pu_sampled": res["worst_mis"],
             "polish": res["polish"], "vtol": res["vtol"], "jinv_norm_est": info["jinv_norm"],
-            "threads_per_cta": info["threads_per_cta"],
             "single_factorizations": int(mixed["stats"]["single_factorizations"]),
             "double_factorizations": int(mixed["stats"]["double_factorizations"]),
         },
         "fp64": fp64,
+        "warm_lanes": res["warm"],
         "accuracy": res["accuracy"],
         "n1_sweep": res.get("n1"),
         "multigrid": res.get("multigrid"),
@@ -548,7 +645,8 @@ def gpu_line(args, res, rank, world):
                 "timing": "wall clock over the timed steps, two steps in flight (gbpf_solve_lanes_async)",
                 "single_call_ms": round(res["e2e_single_ms"], 3)},
         "clocks": mixed["clocks"],
-        "gpu_launches": 2 * args.steps,  # per step: the start-state table kernel + the Newton kernel
+        # per step: the start-state table, the shared start and its replication, the Newton kernel
+        "gpu_launches": 4 * args.steps,
         "wall_ms_per_step": round(mixed["wall_ms"], 3),
     }
     return line
@@ -620,9 +718,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded 2,000-bus grid and hourly load/generation series)",
-        "config": {"workload": f"2,000-bus grid x {hours} hourly cases (sample of the {HOURS}-hour series), "
-                               f"warm-start lanes K={K}", "n_bus": g.n, "hours": hours, "lanes": K,
-                   "tol_pu": 1e-8, "max_iter": 30},
+        "config": headline_config(g, hours, K),
         "cpu_baseline": {"value": round(value, 1), "unit": "solves/s", "cores": cpu_cores(), "kind": "port",
                          "sample": f"{hours} hours per step on all host cores (oracle/liboracle.so, a restatement "
                                    f"of the reference's nr_klu; the reference's own build needs its checkout)"},

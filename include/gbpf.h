@@ -50,6 +50,8 @@ typedef struct gbpf_params {
                             prologue) and every case's first step solves with it -- for bulk
                             batches; 0: every case evaluates and factors its own start (no
                             prologue on the launch's critical path: latency-bound serving) */
+    int phase_timers;    /* 1: the Newton kernel sums SM clock cycles per phase over its CTAs into
+                            gbpf_stats.phase_cycles (single-topology launches; 0: off, the default) */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -74,6 +76,11 @@ typedef struct gbpf_stats {
                                        case starts from one V0 on the base Ybus without pins, the
                                        first mismatch's injections and J(V0) are computed and
                                        factored once per launch */
+    unsigned long long phase_cycles[6]; /* with gbpf_params.phase_timers: SM cycles summed over the
+                                           CTAs of the last launch per phase -- slot refill and case
+                                           load, factorization with forward substitution, backward
+                                           substitution, voltage update, mismatch / Jacobian
+                                           evaluation, decision and write-back; 0 otherwise */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);
@@ -200,9 +207,11 @@ int gbpf_get_row_of_bus(gbpf_solver* s, int32_t* out);
 int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
 /* Self-test of the kernels' own double-precision numerics (no reference counterpart): per
  * element, recip = the Newton-refined reciprocal (x > 0, else 0), s_small / c_small = the
- * small-angle series sine / cosine (|x| < 1/4, else CUDA's), s_ref / c_ref = CUDA's sincos. */
+ * small-angle series sine / cosine (|x| < 1/4, else CUDA's), s_ref / c_ref = CUDA's sincos;
+ * with phasor (2 doubles, or NULL), rot (n x 2) = the phasor rotated by x as the voltage update
+ * rotates a bus phasor (|x| < 1/4, else 0). */
 int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
-                       double* c_ref);
+                       double* c_ref, const double* phasor, double* rot);
 
 /* Page-locked host memory for fast transfers. */
 void* gbpf_host_alloc(size_t bytes);

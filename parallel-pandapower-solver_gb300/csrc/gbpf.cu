@@ -548,6 +548,7 @@ int enqueue_launch(gbpf_solver* s, LaunchRes& R, gbpf::Batch& b, long long units
     L.njobs = 1;
     L.scratch = R.scr->as<char>();
     L.cta_bytes = job.off.total;
+    L.timed = b.timers;
     CK(cudaEventRecord(R.e0, R.stream));
     if (b.v0_shared)
         CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, R.btab->as<double4_32a>(), b.err, R.stream));
@@ -574,6 +575,7 @@ int finish_launch(const LaunchRes& R, int grid, int G, int NT, const char* who, 
     st->macro_steps = host_ctl[4];
     st->chord_steps = host_ctl[5];
     st->first_steps = host_ctl[6];
+    for (int k = 0; k < 6; ++k) st->phase_cycles[k] = host_ctl[8 + k];
     st->grid = grid;
     st->cases_per_cta = G;
     st->threads_per_cta = NT;
@@ -630,6 +632,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     // step like nr_klu)
     b.chord_tol = b.mixed && b.vote_rule == 1 && p.chord_tol > 0.0 ? p.chord_tol : 0.0;
     b.share_ok = p.shared_start != 0;
+    b.timers = p.phase_timers != 0;
     b.check_v0 = p.check_v0;
     b.rcond_min64 = p.pivot_ratio_double * s->plan.rcond0;  // nr_klu.cpp:567 REUSE_RCOND_RATIO = 1e-3
     b.rcond_min32 = p.pivot_ratio_single * s->plan.rcond0;
@@ -1453,19 +1456,24 @@ int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, 
 }
 
 int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
-                       double* c_ref) {
+                       double* c_ref, const double* phasor, double* rot) {
     if (n <= 0) return 0;
-    DBuf a, b;
+    DBuf a, b, c;
     CK(a.ensure((size_t)n * 8));
-    CK(b.ensure((size_t)n * 8 * 5));
+    CK(b.ensure((size_t)n * 8 * 7));
+    CK(c.ensure(16));
     double* o = b.as<double>();
     CK(cudaMemcpy(a.p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
-    CK(gbpf::launch_math(a.as<double>(), n, o, o + n, o + 2 * (size_t)n, o + 3 * (size_t)n, o + 4 * (size_t)n));
+    if (phasor) CK(cudaMemcpy(c.p, phasor, 16, cudaMemcpyHostToDevice));
+    CK(gbpf::launch_math(a.as<double>(), n, o, o + n, o + 2 * (size_t)n, o + 3 * (size_t)n, o + 4 * (size_t)n,
+                         phasor ? c.as<double>() : nullptr, o + 5 * (size_t)n));
     CK(cudaDeviceSynchronize());
     double* outs[5] = {recip, s_small, c_small, s_ref, c_ref};
     for (int k = 0; k < 5; ++k) CK(cudaMemcpy(outs[k], o + k * (size_t)n, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    if (phasor && rot) CK(cudaMemcpy(rot, o + 5 * (size_t)n, (size_t)n * 16, cudaMemcpyDeviceToHost));
     a.release();
     b.release();
+    c.release();
     return 0;
 }
 

@@ -107,11 +107,15 @@ struct Batch {
     const void* fac0;        // factors of J(V0), one copy per case slot: [blk][slot], float4 / double4
     const int* ok0;          // 1 when the shared factorization passed its pivot check
     int share_ok;            // the caller allows a shared start (gbpf_params.shared_start)
+    int timers;              // the launch counts SM cycles per phase into stats[8 .. 13] (gbpf_params.phase_timers)
     double rcond_min64;
     double rcond_min32;
     int* counter;            // work counter, zero before launch
     unsigned long long* stats;  // [0] fp32 factorizations [1] fp64 [2] fp32 rejected [3] fp64 rejected [4] macro steps
                                 // [5] chord steps [6] first steps with the shared start's factors
+                                // [8 .. 13] with timers: SM cycles summed over CTAs per phase (refill + load,
+                                // factorization + forward substitution, backward substitution, voltage
+                                // update, evaluation, decision + write-back)
     int* err;                // [0] code [1] bus [2] case
 };
 
@@ -151,6 +155,7 @@ struct Launch {
     int njobs;
     char* scratch;
     unsigned long long cta_bytes;
+    int timed;               // the instantiation that counts SM cycles per phase (stats[8 .. 13])
 };
 
 // Scratch layout of a job with n buses, nv block rows, nblk blocks and G slots.
@@ -195,7 +200,7 @@ void start_carve(StartJob& sj, char* base, int n, int nv, int nblk, int G, bool 
 cudaError_t launch_start(const StartJob* jobs, int njobs, cudaStream_t stream);
 cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d, float* d2f_small);
 cudaError_t launch_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
-                        double* c_ref);
+                        double* c_ref, const double* phasor, double* rot);
 // Ybus values from stamps (postproc.cu)
 cudaError_t launch_ybus_gather(int nnz, int m4, const int* ptr, const int* src, const double2* stamps,
                                const double2* shunt, double2* Y, float2* Y32, cudaStream_t stream);

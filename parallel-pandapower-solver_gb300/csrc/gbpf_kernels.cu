@@ -309,6 +309,16 @@ __device__ __forceinline__ double recip_nr(double x) {
     return r;
 }
 
+// Per-phase clock (timed launches only): thread 0, just past a barrier that ends phase k, adds
+// the SM cycles since the previous mark to the CTA's counter of phase k.
+__device__ __forceinline__ void phase_mark(unsigned long long* ph, long long* clk, int k) {
+    if (ph && threadIdx.x == 0) {
+        const long long now = clock64();
+        ph[k] += (unsigned long long)(now - *clk);
+        *clk = now;
+    }
+}
+
 // ---------------------------------------------------------------------------- block LU
 template <typename T>
 struct V4;
@@ -354,10 +364,11 @@ __device__ __forceinline__ void mm_sub(B4& acc, const B4& a, const B4& b) {
 // schedule and all threads work on that slot. Slots flagged in `chord` keep the factors already
 // in `fac` and run the substitutions only; when every slot of the CTA does (factor_any false),
 // the workers walk the substitution-only lists instead of skipping factor tasks one by one.
-template <typename real>
+template <typename real, bool TIMED = false>
 __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const double2* R, typename V4<real>::t2* y,
                         const int* on, int lg, unsigned long long* smin, unsigned long long* smax,
-                        const int* chord, bool factor_any, typename V4<real>::t* dinv_smem, int solo = -1) {
+                        const int* chord, bool factor_any, typename V4<real>::t* dinv_smem, int solo = -1,
+                        unsigned long long* ph = nullptr, long long* clk = nullptr) {
     using B4 = typename V4<real>::t;
     using B2 = typename V4<real>::t2;
     const int tid = threadIdx.x;
@@ -516,6 +527,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
         }
         __syncthreads();
     }
+    if constexpr (TIMED) phase_mark(ph, clk, 1);
     for (int h = 0; h < P.nblev; ++h) {
         if (act) {
             const int t0 = __ldg(&P.ptrC[h * W + w]), t1 = __ldg(&P.ptrC[h * W + w + 1]);
@@ -593,6 +605,7 @@ __device__ void lu_pass(const DevPlan& P, typename V4<real>::t* fac, const doubl
         atomicMax(&smax[s], dbits(dmax));
     }
     __syncthreads();
+    if constexpr (TIMED) phase_mark(ph, clk, 2);
 }
 
 __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long long bmax, double rc) {
@@ -605,7 +618,7 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 // NTB threads per CTA and 1024 / NTB resident CTAs per SM (64 registers per thread in
 // every variant): smaller CTAs let one CTA's latency-bound factorization overlap another's
 // double-precision evaluation on the same SM.
-template <int NTB>
+template <int NTB, bool TIMED>
 __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L) {
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
@@ -684,8 +697,16 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ int s_share;  // the launch's shared start is usable (its factorization passed)
     __shared__ int s_stk[MAX_SLOTS][MAX_STAMPS];
     __shared__ double2 s_stv[MAX_SLOTS][MAX_STAMPS];
+    __shared__ unsigned long long s_ph[6];  // timed launches: SM cycles per phase of this CTA and job
+    __shared__ long long s_clk;
 
     if (tid == 0) s_share = Bt.fac0 != nullptr && __ldg(Bt.ok0) == 1;  // written by the start kernel before this launch
+    if (TIMED && tid == 0) {
+        for (int k = 0; k < 6; ++k) s_ph[k] = 0ULL;
+        s_clk = clock64();
+    }
+    // timed launches (a separate instantiation, so untimed ones carry no trace of the counters)
+#define GBPF_PH (TIMED ? s_ph : nullptr)
     if (tid < G) {
         s_st[tid] = SL_EMPTY;
         s_lcur[tid] = s_lend[tid] = 0;
@@ -786,7 +807,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         if (tid == 0) s_solo = -1;
         const int alive = __syncthreads_count(tid < G && s_st[tid] != SL_RETIRED);
-        if (!alive) break;
+        if (!alive) {
+            if (TIMED && tid == 0)
+                for (int k = 0; k < 6; ++k) atomicAdd(&Bt.stats[8 + k], s_ph[k]);
+            break;
+        }
         // one case left in the CTA (its tail): every thread works on that slot this pass
         if (alive == 1 && G > 1 && tid < G && s_st[tid] != SL_RETIRED) s_solo = tid;
         __syncthreads();
@@ -890,6 +915,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             s_pmax[s] = 0ULL;
         }
         const int any32 = __syncthreads_or(tid < G && s_on32[tid]);
+        if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 0);
         if (any32) {
             // chord and first steps are decided per slot (a result never depends on the other
             // cases of its CTA); the factorization is left out altogether when no float slot
@@ -901,8 +927,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 const int sl = solo >= 0 ? solo : (tid & 31) & (G - 1);
                 const int buf = s_chord[sl] ? s_fb[sl] : 1 - s_fb[sl];
                 float4* const fl = s_first[sl] ? (float4*)Bt.fac0 : (buf ? fac32b : fac32);
-                lu_pass<float>(solo >= 0 ? s_plan1 : P, fl, R, y32, s_on32, lg, s_pmin, s_pmax, s_nofac, !all_chord,
-                               nullptr, solo);
+                lu_pass<float, TIMED>(solo >= 0 ? s_plan1 : P, fl, R, y32, s_on32, lg, s_pmin, s_pmax, s_nofac, !all_chord,
+                               nullptr, solo, GBPF_PH, &s_clk);
             }
             if (tid < G && s_on32[tid]) {
                 const int s = tid;
@@ -951,11 +977,11 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 const int all_first = __syncthreads_and(!(tid < G && s_on64[tid]) || s_nofac[tid]);
                 const int sl = solo >= 0 ? solo : (tid & 31) & (G - 1);
                 double4_32a* const fd = s_first[sl] ? (double4_32a*)Bt.fac0 : fac64;
-                lu_pass<double>(solo >= 0 ? s_plan1 : P, fd, R, y64, s_on64, lg, s_pmin, s_pmax, s_nofac, !all_first,
-                                s_dinv64, solo);
+                lu_pass<double, TIMED>(solo >= 0 ? s_plan1 : P, fd, R, y64, s_on64, lg, s_pmin, s_pmax, s_nofac, !all_first,
+                                s_dinv64, solo, GBPF_PH, &s_clk);
             } else {
-                lu_pass<double>(solo >= 0 ? s_plan1 : P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true,
-                                s_dinv64, solo);
+                lu_pass<double, TIMED>(solo >= 0 ? s_plan1 : P, fac64, R, y64, s_on64, lg, s_pmin, s_pmax, nullptr, true,
+                                s_dinv64, solo, GBPF_PH, &s_clk);
             }
             if (tid < G && s_on64[tid]) {
                 const int s = tid;
@@ -1058,6 +1084,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             s_res[tid] = 0ULL;
         }
         __syncthreads();
+        if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 3);
 
         // ---------------------------------------------------------------- evaluate
         // Buses are swept in reverse Cuthill-McKee order, so the buses a CTA evaluates at the
@@ -1095,6 +1122,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             atomicMax(&s_res[s], worst);
         }
         __syncthreads();
+        if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 4);
 
         // ---------------------------------------------------------------- decide
         if (tid < G) {
@@ -1214,7 +1242,9 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             s_st[s] = SL_EMPTY;
         }
         __syncthreads();
+        if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 5);
     }
+#undef GBPF_PH
     }  // jobs
 }
 
@@ -1257,9 +1287,21 @@ __global__ void conversions_kernel(const double* in, int n, float* d2f, double* 
 // IEEE division and CUDA's sincos): recip_nr(x) for x > 0, and sincos_small(d) with CUDA's
 // sincos(d) beside it for |d| < 1/4 (elements outside that range get sincos only).
 __global__ void math_kernel(const double* in, int n, double* recip, double* s_small, double* c_small,
-                            double* s_ref, double* c_ref) {
+                            double* s_ref, double* c_ref, const double* phasor, double* rot) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double x = in[i];
+        if (phasor) {  // the phasor (phasor[0], phasor[1]) rotated by x as the voltage update does, |x| < 1/4
+            const unsigned ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
+            double rc = 0.0, rs = 0.0;
+            if (ah < 0x3FD00000u) {
+                double sd, cd;
+                sincos_small(x, ah, &sd, &cd);
+                rc = fma(phasor[0], cd, -phasor[1] * sd);
+                rs = fma(phasor[1], cd, phasor[0] * sd);
+            }
+            rot[2 * i] = rc;
+            rot[2 * i + 1] = rs;
+        }
         recip[i] = x > 0.0 ? recip_nr(x) : 0.0;
         double sr, cr;
         sincos(x, &sr, &cr);
@@ -1279,8 +1321,8 @@ __global__ void math_kernel(const double* in, int n, double* recip, double* s_sm
 }
 
 cudaError_t launch_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
-                        double* c_ref) {
-    math_kernel<<<(n + 255) / 256, 256>>>(in, n, recip, s_small, c_small, s_ref, c_ref);
+                        double* c_ref, const double* phasor, double* rot) {
+    math_kernel<<<(n + 255) / 256, 256>>>(in, n, recip, s_small, c_small, s_ref, c_ref, phasor, rot);
     return cudaGetLastError();
 }
 
@@ -1524,11 +1566,14 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
 
 cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream) {
     if (threads == 1024)
-        newton_kernel<1024><<<grid, 1024, 0, stream>>>(L);
+        L.timed ? newton_kernel<1024, true><<<grid, 1024, 0, stream>>>(L)
+                : newton_kernel<1024, false><<<grid, 1024, 0, stream>>>(L);
     else if (threads == 512)
-        newton_kernel<512><<<grid, 512, 0, stream>>>(L);
+        L.timed ? newton_kernel<512, true><<<grid, 512, 0, stream>>>(L)
+                : newton_kernel<512, false><<<grid, 512, 0, stream>>>(L);
     else if (threads == 256)
-        newton_kernel<256><<<grid, 256, 0, stream>>>(L);
+        L.timed ? newton_kernel<256, true><<<grid, 256, 0, stream>>>(L)
+                : newton_kernel<256, false><<<grid, 256, 0, stream>>>(L);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -1542,9 +1587,9 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
 }
 
 const void* newton_kernel_ptr(int threads) {
-    if (threads == 1024) return (const void*)newton_kernel<1024>;
-    if (threads == 512) return (const void*)newton_kernel<512>;
-    return (const void*)newton_kernel<256>;
+    if (threads == 1024) return (const void*)newton_kernel<1024, false>;
+    if (threads == 512) return (const void*)newton_kernel<512, false>;
+    return (const void*)newton_kernel<256, false>;
 }
 
 }  // namespace gbpf

@@ -37,6 +37,7 @@ class Params(C.Structure):
         ("vtol", C.c_double),
         ("chord_tol", C.c_double),
         ("shared_start", C.c_int),
+        ("phase_timers", C.c_int),
     ]
 
 
@@ -73,6 +74,7 @@ class Stats(C.Structure):
         ("threads_per_cta", C.c_int),
         ("chord_steps", C.c_ulonglong),
         ("first_steps", C.c_ulonglong),
+        ("phase_cycles", C.c_ulonglong * 6),
     ]
 
 
@@ -132,7 +134,7 @@ SIGNATURES = {
     "gbpf_dc_start_batch": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _bp]),
     "gbpf_eval_jacobian": (C.c_int, [_vp, _dp, _dp, _bp, _dp, _dp]),
     "gbpf_selftest_conversions": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
-    "gbpf_selftest_math": (C.c_int, [_dp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "gbpf_selftest_math": (C.c_int, [_dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gbpf_host_alloc": (_vp, [C.c_size_t]),
     "gbpf_host_free": (None, [_vp]),
     "gbpf_plan_selftest": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int, _dp, _dp,
@@ -200,6 +202,16 @@ def check(rc: int, what: str = ""):
     if rc != 0:
         msg = last_error()
         raise RuntimeError(msg if msg else f"{what} failed ({rc})")
+
+
+PHASES = ("load", "factor_forward", "backward", "step", "eval", "decide")
+
+
+def stats_dict(o: Stats) -> dict:
+    """gbpf_stats as a dict; phase_cycles as {phase: SM cycles summed over CTAs}."""
+    out = {f: getattr(o, f) for f, _ in o._fields_ if f != "phase_cycles"}
+    out["phase_cycles"] = dict(zip(PHASES, (int(x) for x in o.phase_cycles)))
+    return out
 
 
 def d(a: np.ndarray):

@@ -64,7 +64,7 @@ class GpuGroup:
     def stats(self) -> dict:
         o = _lib.Stats()
         _lib.check(_lib.load().gbpf_group_stats(self._h, C.byref(o)), "gbpf_group_stats")
-        return {f: getattr(o, f) for f, _ in o._fields_}
+        return _lib.stats_dict(o)
 
     def solve(self, jobs: list[GroupJob], params: _lib.Params, pinned_out: bool = False) -> list[dict]:
         """One launch over `jobs`; per job a dict of V (n, T), iterations, converged and, for

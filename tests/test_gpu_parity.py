@@ -340,7 +340,9 @@ def test_own_double_numerics_within_an_ulp():
                         [0.0, -0.0, 2.0 ** -14, -(2.0 ** -6), 0.2499999]])
     inp = np.ascontiguousarray(np.concatenate([x, d]))
     outs = [np.empty(len(inp)) for _ in range(5)]
-    rc = _lib.load().gbpf_selftest_math(_lib.d(inp), len(inp), *[_lib.d(o) for o in outs])
+    ph = np.array([np.cos(0.7), np.sin(0.7)])
+    rot = np.empty((len(inp), 2))
+    rc = _lib.load().gbpf_selftest_math(_lib.d(inp), len(inp), *[_lib.d(o) for o in outs], _lib.d(ph), _lib.d(rot))
     assert rc == 0, _lib.last_error()
     recip, s_small, c_small, s_ref, c_ref = outs
     nx = len(x)
@@ -352,6 +354,15 @@ def test_own_double_numerics_within_an_ulp():
         assert (np.abs(got - exact) <= ulp).all()
         assert (np.abs(got - cuda) <= 2 * ulp).all()
     assert s_small[nx + 20000] == 0.0 and c_small[nx + 20000] == 1.0
+    # the voltage update's rotation of a committed phasor by the increment d against the rotation
+    # of the same double phasor in extended precision: within 2 ulp
+    L = np.longdouble
+    c0, s0 = L(ph[0]), L(ph[1])
+    dl = dd.astype(L)
+    want_c = (c0 * np.cos(dl) - s0 * np.sin(dl)).astype(np.float64)
+    want_s = (s0 * np.cos(dl) + c0 * np.sin(dl)).astype(np.float64)
+    assert (np.abs(rot[nx:, 0] - want_c) <= 2 * np.spacing(np.abs(want_c))).all()
+    assert (np.abs(rot[nx:, 1] - want_s) <= 2 * np.spacing(np.abs(want_s))).all()
 
 
 def test_n1_sweep_of_the_2000_bus_grid(grid2000):
