@@ -108,6 +108,11 @@ int gbpf_update_Y(gbpf_solver* s, const double* Yx, int nnz);
 
 int gbpf_get_info(gbpf_solver* s, gbpf_info* out);
 int gbpf_get_stats(gbpf_solver* s, gbpf_stats* out);
+/* Final mismatch infinity norm (p.u.) of every case of the solver's last synchronous solve (n =
+ * its case count). Times gbpf_info.jinv_norm it bounds each result's distance from the exact
+ * power-flow solution to first order, and so from a converged FP64 solve (the per-result
+ * accuracy statement of the mixed path). No reference counterpart. */
+int gbpf_get_mismatch(gbpf_solver* s, double* out, long long n);
 /* CTA shape (threads per CTA, case slots per CTA) the solver launches for a batch of
  * `units` work items (cases, or lanes), and an override per batch-size class
  * (ceil(log2(units))) -- what an autotuner sets after timing candidate shapes. Results do not

@@ -173,6 +173,8 @@ struct gbpf_solver {
     DBuf scr;
     // per-call buffers (grow-only)
     DBuf bS, bV0, bV, bit, bcv, bctl, blane, bstp, bstk, bstv, bYd, bpin, btab, bjobs;
+    DBuf bmis;            // final mismatch of every case of the last synchronous call
+    long long mis_n = 0;  // its case count (0: none recorded)
     // islanding buffers (grow-only)
     DBuf iin, iscr, ibest, iout;
     // branch table for outage cases (gbpf_set_branches)
@@ -190,7 +192,7 @@ struct gbpf_solver {
         shapes.clear();
         for (DBuf* b : {&dYp, &dYj, &dY, &dY32, &dposmap, &drow_of_bus, &dbus_pq, &dpairs, &drow_pq, &dbus_of_row, &deval_order,
                         &ddpos, &scr, &bS, &bV0, &bV, &bit, &bcv, &bctl, &blane, &bstp, &bstk, &bstv, &bYd, &bpin,
-                        &btab, &bjobs, &iin, &iscr, &ibest, &iout, &dbr_f, &dbr_t, &dbr_live, &dbr_pos, &dbr_val,
+                        &btab, &bjobs, &bmis, &iin, &iscr, &ibest, &iout, &dbr_f, &dbr_t, &dbr_live, &dbr_pos, &dbr_val,
                         &dslack, &dprio, &dg_ptr, &dg_src, &dshunt})
             b->release();
         for (cudaEvent_t e : {e0, e1, c0, c1})
@@ -598,8 +600,12 @@ int run(gbpf_solver* s, gbpf::Batch& b, long long units, const char* who) {
     unsigned long long host_ctl[32];
     LaunchRes R{s->stream, s->e0, s->e1, &s->scr, &s->bctl, &s->btab, &s->bjobs, host_ctl};
     int grid = 0, G = 0, NT = 0;
+    s->mis_n = 0;
+    CK(s->bmis.ensure((size_t)b.B * 8));
+    b.mis = s->bmis.as<double>();
     if (int rc = enqueue_launch(s, R, b, units, who, &grid, &G, &NT)) return rc;
     CK(cudaStreamSynchronize(s->stream));
+    s->mis_n = b.B;
     return finish_launch(R, grid, G, NT, who, &s->last);
 }
 
@@ -1044,6 +1050,17 @@ int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cas
     return 0;
 }
 
+int gbpf_get_mismatch(gbpf_solver* s, double* out, long long n) {
+    if (!s || !out) return fail("get_mismatch: null argument");
+    if (s->mis_n <= 0) return fail("get_mismatch: no synchronous solve recorded its cases' mismatch");
+    if (n != s->mis_n)
+        return fail("get_mismatch: the last call solved " + std::to_string(s->mis_n) + " cases, not " +
+                    std::to_string(n));
+    CK(cudaMemcpyAsync(out, s->bmis.p, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
 int gbpf_get_stats(gbpf_solver* s, gbpf_stats* o) {
     if (!s || !o) return fail("null argument");
     *o = s->last;
@@ -1195,6 +1212,7 @@ int gbpf_solve_lanes_async(gbpf_solver* s, int slot, int T, const double* S, con
     }
     ExecSlot& X = *s->slots[slot];
     if (X.pending) return fail("solve_lanes_async: slot " + std::to_string(slot) + " is still in flight (wait for it first)");
+    s->mis_n = 0;  // asynchronous calls record no per-case mismatch
     const size_t n = s->n;
     const size_t sb = n * (size_t)T * 16, vb = n * 16;
     CK(X.bS.ensure(sb));

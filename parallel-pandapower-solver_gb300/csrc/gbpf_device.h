@@ -92,6 +92,7 @@ struct Batch {
     long long sV;
     int* iters;
     uint8_t* conv;
+    double* mis;             // or null: every case's final mismatch infinity norm (p.u.)
     int max_iter;
     double tol;
     int line_search;

@@ -1238,6 +1238,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int s = tid;
             Bt.iters[s_case[s]] = s_it[s];
             Bt.conv[s_case[s]] = (uint8_t)s_conv[s];
+            if (Bt.mis) Bt.mis[s_case[s]] = s_nrm[s];
             s_warm[s] = Bt.lanes && s_conv[s];
             s_st[s] = SL_EMPTY;
         }

@@ -134,6 +134,7 @@ SIGNATURES = {
     "gbpf_dc_start_batch": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _bp]),
     "gbpf_eval_jacobian": (C.c_int, [_vp, _dp, _dp, _bp, _dp, _dp]),
     "gbpf_selftest_conversions": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
+    "gbpf_get_mismatch": (C.c_int, [_vp, _dp, C.c_longlong]),
     "gbpf_selftest_math": (C.c_int, [_dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gbpf_host_alloc": (_vp, [C.c_size_t]),
     "gbpf_host_free": (None, [_vp]),

@@ -65,8 +65,22 @@ class PolarNewtonSolverCUDA:
                                 vote_rule=self.vote_rule, polish=self.polish, vtol=self.vtol)
 
     def _record(self, B, r, st=None):
+        own = st is None  # a launch of this solver (not of a group): its cases' mismatch is recorded
         st = self._s.stats if st is None else st
         failed = int((~r["converged"]).sum())
+        # per-result accuracy: every case's final mismatch and |J^-1| x mismatch, a first-order
+        # bound on its voltage's distance from the exact solution (and so from a converged FP64
+        # solve); |J^-1| is the topology's estimate from its flat-start factorization
+        mis = self._s.last_mismatch(B) if own else None
+        jinv = float(self._s.info["jinv_norm"])
+        bound = max_mis = None
+        if mis is not None:
+            r["mismatch"] = mis
+            with np.errstate(over="ignore"):  # a failed case's mismatch is DBL_MAX: no bound
+                r["error_bound"] = mis * jinv
+            ok = np.asarray(r["converged"], bool)
+            max_mis = float(mis[ok].max()) if ok.any() else None
+            bound = None if max_mis is None else max_mis * jinv
         self.last_stats = {
             "systems": B,
             "chunk": B,
@@ -81,6 +95,12 @@ class PolarNewtonSolverCUDA:
             "kernel_ms": float(st["kernel_ms"]),
             "grid": int(st["grid"]),
             "cases_per_cta": int(st["cases_per_cta"]),
+            # counters of the persistent kernel (beyond the reference's chunk-loop statistics)
+            "chord_steps": int(st.get("chord_steps", 0)),
+            "first_steps": int(st.get("first_steps", 0)),
+            "jinv_norm": jinv,
+            "max_mismatch": max_mis,  # over the converged cases
+            "error_bound": bound,     # jinv_norm x max_mismatch
         }
         return r
 

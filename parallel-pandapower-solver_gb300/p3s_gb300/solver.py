@@ -161,6 +161,14 @@ class GpuSolver:
         _lib.check(_lib.load().gbpf_get_stats(self._h, C.byref(o)), "gbpf_get_stats")
         return _lib.stats_dict(o)
 
+    def last_mismatch(self, n_cases: int):
+        """Final mismatch infinity norm (p.u.) of every case of the last synchronous solve, or
+        None when the last call recorded none (an asynchronous call, or another case count)."""
+        out = np.empty(int(n_cases))
+        if _lib.load().gbpf_get_mismatch(self._h, _lib.d(out), int(n_cases)) != 0:
+            return None
+        return out
+
     def shape(self, units: int):
         """(threads per CTA, case slots per CTA) launched for a batch of `units` work items."""
         nt, g = C.c_int(), C.c_int()

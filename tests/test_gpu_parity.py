@@ -543,3 +543,26 @@ def test_shared_start_equals_each_case_starting_on_its_own(grid2000):
         assert np.array_equal(shared["iterations"], own["iterations"])
         assert np.array_equal(shared["V"], own["V"])
         assert shared["converged"].all()
+
+
+def test_per_result_accuracy_bound_covers_the_distance_to_the_converged_oracle(grid2000):
+    """Every mixed result carries its final mismatch and |J^-1| x mismatch (``error_bound``); the
+    bound covers the result's distance from the oracle solved to convergence (tol 1e-12), up to
+    that oracle's own bound, and last_stats states the largest one."""
+    g = grid2000
+    S = timeseries_injections(g, 96)
+    tight = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).solve_batch(S, g.V0, tol=1e-12)
+    gpu = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    gpu.precision = "mixed"
+    r = gpu.solve_batch(S, g.V0)
+    assert r["converged"].all() and tight["converged"].all()
+    jinv = gpu.last_stats["jinv_norm"]
+    assert jinv > 1.0 and (r["mismatch"] <= 1e-8).all()
+    assert np.array_equal(r["error_bound"], r["mismatch"] * jinv)
+    dist = np.abs(r["V"] - tight["V"]).max(axis=0)
+    assert (dist <= r["error_bound"] + jinv * 1e-12).all()
+    assert gpu.last_stats["error_bound"] == r["error_bound"].max() < 1e-7
+    # the double path records its own
+    gpu.precision = "double"
+    rd = gpu.solve_batch(S, g.V0)
+    assert (rd["mismatch"] < 1e-8).all() and gpu.last_stats["max_mismatch"] == rd["mismatch"].max()
