@@ -43,6 +43,7 @@ def lib():
         L.oracle_solve_batch_contingency.argtypes = [_P, _dp, _dp, C.c_int, _dp, _dp, _bp, C.c_int, C.c_double,
                                                      C.c_int, C.c_int, _dp, _ip, _bp, C.c_char_p, C.c_int]
         L.oracle_debug_J.argtypes = [_P, _dp, _dp, _ip, _ip, _dp, _dp]
+        L.oracle_last_paths.argtypes = [_P, _ip, C.c_int]
         _lib = L
     return _lib
 
@@ -85,6 +86,15 @@ class Solver:
         if h and _lib is not None:
             _lib.oracle_destroy(h)
             self._h = None
+
+    def last_paths(self):
+        """Per column of the last batch call: 0 solved on the frozen (lean) pivot order throughout,
+        1 a lean refactorization failed its pivot check and the column went on with pivoting
+        LU (nr_klu.cpp:610-652), 2 re-run from its start on pivoting LU (nr_klu.cpp:845-857)."""
+        n = lib().oracle_last_paths(self._h, None, 0)
+        out = np.zeros(n, dtype=np.int32)
+        lib().oracle_last_paths(self._h, _i(out), n)
+        return out
 
     @property
     def lean_active(self) -> bool:

@@ -59,6 +59,10 @@ struct Topo {
     std::vector<double> Ym, Ya;
     std::vector<int> order;  // fill-reducing column order of J (the "analyze" step)
     Lean lean;
+    // per column of the last batch call: 0 solved on the frozen (lean) order throughout, 1 a lean
+    // refactorization failed its pivot check and the column went on with pivoting LU
+    // (nr_klu.cpp:610-652), 2 re-run from its start on pivoting LU (nr_klu.cpp:845-857)
+    std::vector<int> last_path;
 };
 
 struct State {
@@ -66,6 +70,7 @@ struct State {
     std::vector<char> pin;
     std::unique_ptr<slu::Factors> num;  // pivoting factorization (fallback path)
     bool use_lean = true;
+    bool left_lean = false;  // a lean refactorization of this column failed its pivot check
     explicit State(const Topo& t) {
         Jx.assign(t.Ji.size(), 0.0);
         Vm.assign(t.n, 0.0);
@@ -349,6 +354,7 @@ void lean_solve(const Lean& pl, const double* LU, double* b, double* y) {
 struct Result {
     int iterations;
     bool converged;
+    int path = 0;  // Topo::last_path's code
 };
 
 // ---- Newton loop (nr_klu.cpp:569-711). `fresh` = no inherited pivoting factorization.
@@ -376,6 +382,7 @@ Result run_newton(const Topo& w, State& st, int max_iter, double tol, bool line_
                 lean_done = true;
             } else {
                 st.use_lean = false;
+                st.left_lean = true;
                 st.num.reset();
             }
         }
@@ -444,13 +451,17 @@ Result run_column(const Topo& w, State& s, Init&& init, int max_iter, double tol
     const bool reused = w.lean.valid;
     init(s);
     s.use_lean = true;
+    s.left_lean = false;
     s.num.reset();
     Result r = run_newton(w, s, max_iter, tol, ls);
+    r.path = s.left_lean ? 1 : 0;
     if (r.converged || !reused) return r;
     s.num.reset();
     s.use_lean = false;
     init(s);
-    return run_newton(w, s, max_iter, tol, ls);
+    Result r2 = run_newton(w, s, max_iter, tol, ls);
+    r2.path = 2;
+    return r2;
 }
 
 void build_topo(Topo& t, int n, const int* Yp, const int* Yj, const double* Yx, int nnz, const int* pv, int npv,
@@ -525,6 +536,14 @@ void oracle_destroy(void* h) { delete static_cast<Topo*>(h); }
 
 int oracle_lean_active(void* h) { return static_cast<Topo*>(h)->lean.valid ? 1 : 0; }
 
+// Path code of every column of the last batch call (see Topo::last_path); returns the count.
+int oracle_last_paths(void* h, int* out, int n) {
+    const auto& p = static_cast<Topo*>(h)->last_path;
+    const int k = std::min(n, (int)p.size());
+    for (int i = 0; i < k; ++i) out[i] = p[i];
+    return (int)p.size();
+}
+
 void oracle_sizes(void* h, int* m, int* nnzJ) {
     auto* t = static_cast<Topo*>(h);
     *m = t->m;
@@ -548,6 +567,7 @@ int oracle_solve_batch(void* h, const double* S, int T, const double* V0, int v0
                        int errlen) {
     const Topo& t = *static_cast<Topo*>(h);
     const int n = t.n;
+    static_cast<Topo*>(h)->last_path.assign(T, 0);
     std::string first;
     const int nt = n_workers(n_threads, T);
 #pragma omp parallel num_threads(nt)
@@ -582,6 +602,7 @@ int oracle_solve_batch(void* h, const double* S, int T, const double* V0, int v0
                 }
                 iters[c] = r.iterations;
                 conv[c] = r.converged ? 1 : 0;
+                static_cast<Topo*>(h)->last_path[c] = r.path;
             } catch (const std::exception& e) {
 #pragma omp critical
                 {
@@ -604,6 +625,7 @@ int oracle_solve_batch_contingency(void* h, const double* Ymag, const double* Ya
                                    char* err, int errlen) {
     const Topo& t = *static_cast<Topo*>(h);
     const int n = t.n, nnz = (int)t.Yj.size();
+    static_cast<Topo*>(h)->last_path.assign(L, 0);
     std::string first;
     const int nt = n_workers(n_threads, L);
 #pragma omp parallel num_threads(nt)
@@ -638,6 +660,7 @@ int oracle_solve_batch_contingency(void* h, const double* Ymag, const double* Ya
                 }
                 iters[c] = r.iterations;
                 conv[c] = r.converged ? 1 : 0;
+                static_cast<Topo*>(h)->last_path[c] = r.path;
             } catch (const std::exception& e) {
 #pragma omp critical
                 {

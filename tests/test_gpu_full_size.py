@@ -39,8 +39,9 @@ def setup_module(_):
 
 
 def double_tol(n, base=TOL_V):
-    """The double path's bar on an n-bus grid: `base`, or on the large grids twice the spread
-    of the reference's own two builds there (golden_floor.json, made by make_golden_floor.py)."""
+    """The double path's bar on an n-bus grid (or a named stressed case): `base`, or on the
+    large grids and near the loading limit twice the spread of the reference's own two builds
+    there (golden_floor.json, made by make_golden_floor.py)."""
     with open(os.path.join(os.path.dirname(__file__), "golden", "golden_floor.json")) as fh:
         floor = json.load(fh)
     return max(base, 2.0 * floor.get(str(n), 0.0))
@@ -85,6 +86,14 @@ def check_double(got, ref, tol=TOL_V):
     assert np.array_equal(got["converged"], ref["converged"])
     assert np.array_equal(got["iterations"], ref["iterations"])
     ok = ref["converged"]
+    assert np.nanmax(np.abs(got["V"][:, ok] - ref["V"][:, ok])) < tol
+
+
+def check_converged(got, ref, tol=TOL_V):
+    """Flags equal on every case; iterations and voltages on the converged ones."""
+    assert np.array_equal(got["converged"], ref["converged"])
+    ok = ref["converged"]
+    assert np.array_equal(got["iterations"][ok], ref["iterations"][ok])
     assert np.nanmax(np.abs(got["V"][:, ok] - ref["V"][:, ok])) < tol
 
 
@@ -249,3 +258,48 @@ def test_largest_serving_topologies_through_the_server():
         check_double({"V": rd.V, "iterations": rd.iterations, "converged": rd.converged}, ref, tol_d)
         check_mixed({"V": rm.V, "iterations": rm.iterations, "converged": rm.converged}, ref, tight,
                     mismatch(g, rm.V, S, Yx, pin))
+
+
+def test_flags_match_where_the_reference_falls_back_to_pivoting_lu(grid2000):
+    """Cases on which the reference leaves its frozen pivot order for pivoting LU (nr_klu.cpp:
+    610-652, 845-857; the oracle records each column's path): the 2,000-bus grid loaded 7.5x
+    (near the nose: some cases converge on the frozen order, the rest are re-run on pivoting LU)
+    and its full N-1 sweep loaded 6x. The device path has no pivoting LU; its convergence flags
+    equal the reference's on every case (the fallback rescues none of these); where they converge,
+    iterations and voltages as the other double-path bars. (A non-converged case reports the
+    iteration at which its frozen-order factorization was rejected; the reference reports its
+    pivoting retry's, up to max_iter.)"""
+    import dataclasses
+
+    from p3s_gb300 import contingency
+    from p3s_gb300.cuda.nr_polar_solver import PolarNewtonSolverCUDA
+
+    g = grid2000
+    osv = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    S = np.ascontiguousarray(np.repeat(g.Sbus[:, None] * 7.5, 16, axis=1) * np.linspace(0.95, 1.05, 16)[None, :])
+    ref = osv.solve_batch(S, g.V0)
+    paths = osv.last_paths()
+    assert (paths == 0).sum() >= 4 and (paths != 0).sum() >= 4
+    gpu = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
+    check_converged(gpu.solve_batch(S, g.V0), ref, double_tol("2000x7.5"))
+    gpu.precision = "mixed"
+    assert np.array_equal(gpu.solve_batch(S, g.V0)["converged"], ref["converged"])
+
+    g6 = dataclasses.replace(g, Sbus=g.Sbus * 6.0)
+    batch = contingency.build_batch(g6)
+    prio = np.zeros(g.n)
+    prio[g.pv] = np.maximum(g.p_gen[g.pv], np.finfo(float).tiny)
+    _, served, rb, _ = oisl.islands(g.n, g.f, g.t, batch.live, batch.groups, g.ref, True, prio)
+    V0, pin = oisl.start_and_pins(g.V0, served, rb, g.ref)
+    Yx = batch.Yx_matrix
+    ref = osv.solve_batch_contingency(np.ascontiguousarray(np.abs(Yx)), np.ascontiguousarray(np.angle(Yx)),
+                                      g6.Sbus, V0, pin)
+    ref["V"] = np.where(served, ref["V"], np.nan)
+    paths = osv.last_paths()
+    assert (paths != 0).sum() >= 5 and not ref["converged"][paths != 0].any()
+    for prec in ("double", "mixed"):
+        res = contingency.solve_contingencies(g6, reslack_islands=True, precision=prec, return_islands=False)
+        assert np.array_equal(res.converged, ref["converged"]), prec
+        if prec == "double":
+            check_converged({"V": res.V, "iterations": res.iterations, "converged": res.converged}, ref,
+                            double_tol("n1_2000x6", TOL_V_N1))
