@@ -270,6 +270,49 @@ int gbpf_group_set_shape(gbpf_group* g, int threads_per_cta, int slot_budget);
 /* Counters of the last group launch (summed over its jobs). */
 int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
 
+/* ---------------------------------------------------------------- stream launch (serving)
+ * ONE persistent launch of the Newton kernel that takes jobs while it runs: each submitted job
+ * (gbpf_job: one topology's cases -- a single solve, a time-series chunk or N-1 outages) is
+ * staged and appended to a ring, and the CTAs that find no open job take it as their slots free
+ * up; its results are written straight into the caller's page-locked host arrays and its flag
+ * (gbpf_stream_flags()[job]) is set once all its cases are written back. No reference
+ * counterpart: the reference solves one call at a time (nr_polar_solver.py:466-596) and has no
+ * serving loop.
+ * create: capacity = jobs per launch; arena_bytes = device staging for the inputs of one launch;
+ *   ctas = 512-thread CTAs (0: two per SM less 16, which keeps room for the submits' islanding
+ *   kernels); slot_budget = variable buses x case slots a CTA takes per job (0: 8,192).
+ * start: launches the kernel for the given topologies (schedules built, scratch sized for them,
+ *   the kernels that submits launch loaded into the context first; gbpf_params as for the other
+ *   calls, the shared start off). A CTA without an open job polls every ~20 us; once no job has
+ *   been published for idle_seconds it returns (status 1 at stop) -- the launch never waits
+ *   without bound.
+ * submit: returns the job's index, -2 when the ring of this launch is full (stop, start again,
+ *   resubmit) or its staging arena is held by unfinished jobs (try again once some are done;
+ *   a job's staging is released when it and every older job are done), -1 on error. Every
+ *   host array of the job must be page-locked (gbpf_host_alloc; a copy from pageable memory
+ *   would synchronize with the device, i.e. wait for the running launch): S, V0 and the outage
+ *   lists are copied to the device asynchronously and must stay unchanged until the job's flag
+ *   is set; V, iterations, converged (and served) are written by the kernel. Jobs take one
+ *   start V0 (n,), no pins and no explicit stamps.
+ * done: 1 once the job's results are in its host arrays (with an acquire fence), else 0.
+ * alive: 1 while the launch runs. stop: marks the end of submits, waits for the launch (it
+ *   serves every submitted job first) and returns 0, or 1 if its CTAs had returned at their
+ *   idle limit, or -1 on a device error. After 1, a job whose flag is still 0 was published
+ *   after the last CTA had left and was not started (none of its results written): submit it
+ *   again to the next launch. A job some CTA started is always finished.
+ * While a stream launch runs it holds most of the device's SMs: other solves on that device
+ * wait until it is stopped (or its CTAs reach their idle limit) -- submit work to it instead. */
+typedef struct gbpf_stream gbpf_stream;
+gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int ctas, int slot_budget);
+void gbpf_stream_destroy(gbpf_stream* st);
+int gbpf_stream_start(gbpf_stream* st, int nsolvers, gbpf_solver* const* solvers, const gbpf_params* p,
+                      double idle_seconds);
+int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* job);
+const int* gbpf_stream_flags(gbpf_stream* st);
+int gbpf_stream_done(gbpf_stream* st, int job);
+int gbpf_stream_alive(gbpf_stream* st);
+int gbpf_stream_stop(gbpf_stream* st);
+
 /* Islanding of N-1 cases on the device (case_generator.py:355-430 semantics).
  * Graph: n buses, m branches (f[e], t[e]); live[e] != 0 if the branch couples its ends.
  * Case c removes branches out_idx[out_ptr[c] .. out_ptr[c+1]). Labels are the connected

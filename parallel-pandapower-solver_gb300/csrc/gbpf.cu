@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <complex>
@@ -780,6 +781,7 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         o.off = solver_offsets(s, G, mixed);
         o.G = G;
         o.log2G = ilog2(G);
+        o.seq = q;
         cta_bytes = std::max(cta_bytes, o.off.total);
         want += (J.n_cases + G - 1) / G;
         gbpf::Batch b{};
@@ -1797,6 +1799,361 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out) {
     if (!g || !out) return fail("null argument");
     *out = g->last;
     return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------ stream launch
+// One persistent launch that serves jobs as they are submitted (see gbpf.h, gbpf_stream_*).
+// Device control block (ints): [0] published, [1] stop, [2] status, [3] unused, then per job
+// its written-back case count and its work counter; then the launch's 32 statistics words and
+// 16 error words. Descriptors are never overwritten while the launch runs (the ring is filled
+// front to back); a job's staged inputs take one 256-byte aligned block of a circular arena,
+// released once the job and every older one are done -- the launch reads staged inputs past
+// L1, so a block refilled for a later job is never read stale.
+struct gbpf_stream {
+    int device = 0, nsm = 0;
+    cudaStream_t run = nullptr, sub = nullptr;  // the launch's stream; copies and islanding of submits
+    cudaEvent_t ended = nullptr;
+    DBuf scr, ring, ctl, arena;
+    int* host_done = nullptr;            // page-locked, per job
+    int* host_pub = nullptr;             // page-locked: the published count after each job
+    int* host_one = nullptr;             // page-locked: the stop value
+    gbpf::Job* host_jobs = nullptr;      // page-locked staging of the descriptors
+    int capacity = 0, ctas = 0, slot_budget = 8192;
+    size_t arena_bytes = 0;
+    // circular arena: live blocks from `tail` to `head` (wrapping past the end when `wrapped`);
+    // job_beg / job_end: each job's block, released in job order from tail_job on
+    size_t head = 0, tail = 0;
+    bool wrapped = false;
+    int tail_job = 0;
+    std::vector<size_t> job_beg, job_end;
+    unsigned long long cta_bytes = 0;
+    int published = 0;
+    bool running = false, mixed = false;
+    gbpf_params p{};
+    std::vector<gbpf_solver*> topo;  // the topologies the running launch was sized and scheduled for
+    ~gbpf_stream() {
+        if (run) cudaStreamSynchronize(run);
+        if (sub) cudaStreamSynchronize(sub);
+        for (DBuf* b : {&scr, &ring, &ctl, &arena}) b->release();
+        for (void* h : {(void*)host_done, (void*)host_pub, (void*)host_one, (void*)host_jobs})
+            if (h) cudaFreeHost(h);
+        if (ended) cudaEventDestroy(ended);
+        for (cudaStream_t st : {run, sub})
+            if (st) cudaStreamDestroy(st);
+    }
+    int* dctl() { return ctl.as<int>(); }
+    int* ddone() { return dctl() + 4; }
+    int* dcounter() { return dctl() + 4 + capacity; }
+    unsigned long long* dstats() {
+        return reinterpret_cast<unsigned long long*>(ctl.as<char>() + (((size_t)(4 + 2 * capacity) * 4 + 255) & ~(size_t)255));
+    }
+    int* derr() { return reinterpret_cast<int*>(dstats() + 32); }
+    size_t ctl_bytes() const { return (((size_t)(4 + 2 * capacity) * 4 + 255) & ~(size_t)255) + 32 * 8 + 16 * 4; }
+    static size_t job_stride() { return sizeof(gbpf::Job); }  // the kernel's stride (a multiple of 256)
+};
+
+namespace {
+constexpr unsigned STREAM_SLEEP_NS = 20000;  // a CTA without an open job polls every ~20 us
+
+int stream_slots(const gbpf_stream* st, const gbpf_solver* s) {
+    return job_slots(gbpf::MAX_SLOTS, s->plan.nv, st->slot_budget);
+}
+
+size_t up256s(size_t b) { return (std::max<size_t>(b, 1) + 255) & ~(size_t)255; }
+
+// A block of `need` bytes (a multiple of 256) of the circular arena for job `q`, after releasing
+// the blocks of the completed jobs, oldest first; SIZE_MAX when it does not fit now.
+size_t arena_block(gbpf_stream* st, int q, size_t need) {
+    while (st->tail_job < st->published && *(volatile const int*)(st->host_done + st->tail_job)) {
+        const int j = st->tail_job++;
+        if (st->wrapped && st->job_beg[j] < st->tail) st->wrapped = false;  // the block after the wrap
+        st->tail = st->job_end[j];
+    }
+    if (st->tail_job == st->published) {  // nothing live: the arena is empty
+        st->head = st->tail = 0;
+        st->wrapped = false;
+    }
+    size_t at = SIZE_MAX;
+    if (!st->wrapped) {
+        if (st->arena_bytes - st->head >= need) {
+            at = st->head;
+        } else if (st->tail > need) {  // wrap to the front (strictly below tail: full != empty)
+            at = 0;
+            st->wrapped = true;
+        }
+    } else if (st->tail - st->head > need) {
+        at = st->head;
+    }
+    if (at == SIZE_MAX) return at;
+    st->head = at + need;
+    st->job_beg[q] = at;
+    st->job_end[q] = at + need;
+    return at;
+}
+}  // namespace
+
+extern "C" {
+
+gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int ctas, int slot_budget) {
+    if (capacity <= 0 || arena_bytes < 4096 || ctas < 0 || slot_budget < 0) {
+        fail("stream_create: capacity > 0, arena_bytes >= 4096, ctas >= 0, slot_budget >= 0");
+        return nullptr;
+    }
+    std::unique_ptr<gbpf_stream> st(new gbpf_stream);
+    st->capacity = capacity;
+    st->arena_bytes = arena_bytes & ~(size_t)255;
+    st->job_beg.assign(capacity, 0);
+    st->job_end.assign(capacity, 0);
+    if (slot_budget) st->slot_budget = slot_budget;
+    auto ok = [&](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        fail(std::string("stream_create: ") + cudaGetErrorString(e));
+        return false;
+    };
+    if (!ok(cudaGetDevice(&st->device))) return nullptr;
+    if (!ok(cudaDeviceGetAttribute(&st->nsm, cudaDevAttrMultiProcessorCount, st->device))) return nullptr;
+    // two 512-thread CTAs per SM, less 16 CTAs' room kept free for the submits' islanding kernels
+    st->ctas = ctas ? ctas : std::max(1, 2 * st->nsm - 16);
+    if (!ok(cudaStreamCreateWithFlags(&st->run, cudaStreamNonBlocking))) return nullptr;
+    if (!ok(cudaStreamCreateWithFlags(&st->sub, cudaStreamNonBlocking))) return nullptr;
+    if (!ok(cudaEventCreateWithFlags(&st->ended, cudaEventDisableTiming))) return nullptr;
+    if (!ok(st->ring.ensure((size_t)capacity * gbpf_stream::job_stride()))) return nullptr;
+    if (!ok(st->ctl.ensure(st->ctl_bytes()))) return nullptr;
+    if (!ok(st->arena.ensure(arena_bytes))) return nullptr;
+    if (!ok(cudaMallocHost((void**)&st->host_done, (size_t)capacity * 4))) return nullptr;
+    if (!ok(cudaMallocHost((void**)&st->host_pub, (size_t)capacity * 4))) return nullptr;
+    if (!ok(cudaMallocHost((void**)&st->host_one, 4))) return nullptr;
+    if (!ok(cudaMallocHost((void**)&st->host_jobs, (size_t)capacity * sizeof(gbpf::Job)))) return nullptr;
+    for (int q = 0; q < capacity; ++q) st->host_pub[q] = q + 1;
+    *st->host_one = 1;
+    return st.release();
+}
+
+void gbpf_stream_destroy(gbpf_stream* st) {
+    if (!st) return;
+    if (st->running) gbpf_stream_stop(st);
+    delete st;
+}
+
+int gbpf_stream_start(gbpf_stream* st, int nsolvers, gbpf_solver* const* solvers, const gbpf_params* pp,
+                      double idle_seconds) {
+    if (!st) return fail("null stream");
+    if (st->running) return fail("stream_start: the launch is running (stop it first)");
+    if (nsolvers <= 0 || !solvers) return fail("stream_start: no topology");
+    if (!(idle_seconds > 0.0)) return fail("stream_start: idle_seconds must be > 0");
+    const gbpf_params p = pp ? *pp : default_params();
+    if (int rc = check_params(p, "stream_start")) return rc;
+    st->p = p;
+    st->p.shared_start = 0;   // no prologue kernels: jobs arrive while the launch runs
+    st->p.phase_timers = 0;
+    st->mixed = p.precision == 1;
+    // every topology's schedules for its slot count, and scratch for the largest of them
+    unsigned long long cta = 0;
+    for (int k = 0; k < nsolvers; ++k) {
+        gbpf_solver* s = solvers[k];
+        if (!s) return fail("stream_start: null solver");
+        if (s->device != st->device) return fail("stream_start: a solver lives on another device");
+        const int G = stream_slots(st, s);
+        Shape* sh = nullptr;
+        if (int rc = get_shape(s, 512, G, &sh)) return rc;
+        if (G > 1)
+            if (int rc = get_shape(s, 512, 1, &sh)) return rc;
+        cta = std::max(cta, solver_offsets(s, G, st->mixed).total);
+    }
+    st->cta_bytes = cta;
+    st->topo.assign(solvers, solvers + nsolvers);
+    // the kernels that submits launch beside the running launch, loaded before it starts
+    CK(gbpf::preload_v0_table());
+    CK(gbpf::preload_islands());
+    CK(st->scr.ensure((size_t)st->ctas * cta));
+    // the control block is zero before the launch reads it and before any submit copies to it
+    CK(cudaStreamSynchronize(st->sub));
+    CK(cudaMemsetAsync(st->ctl.p, 0, st->ctl_bytes(), st->sub));
+    CK(cudaStreamSynchronize(st->sub));
+    std::memset(st->host_done, 0, (size_t)st->capacity * 4);
+    st->head = st->tail = 0;
+    st->wrapped = false;
+    st->tail_job = 0;
+    st->published = 0;
+    gbpf::Launch L{};
+    L.jobs = st->ring.as<gbpf::Job>();
+    L.njobs = st->capacity;
+    L.scratch = st->scr.as<char>();
+    L.cta_bytes = cta;
+    L.ring.published = st->dctl();
+    L.ring.stop = st->dctl() + 1;
+    L.ring.status = st->dctl() + 2;
+    L.ring.done_cases = st->ddone();
+    int* dflags = nullptr;
+    CK(cudaHostGetDevicePointer((void**)&dflags, st->host_done, 0));
+    L.ring.host_done = dflags;
+    L.ring.sleep_ns = STREAM_SLEEP_NS;
+    L.ring.idle_polls = std::max<long long>(1, (long long)(idle_seconds * 1e9 / STREAM_SLEEP_NS));
+    CK(gbpf::launch_newton(L, st->ctas, 512, st->run));
+    CK(cudaEventRecord(st->ended, st->run));
+    st->running = true;
+    return 0;
+}
+
+int gbpf_stream_alive(gbpf_stream* st) {
+    if (!st) return fail("null stream");
+    if (!st->running) return 0;
+    const cudaError_t e = cudaEventQuery(st->ended);
+    if (e == cudaErrorNotReady) return 1;
+    if (e != cudaSuccess) return fail(std::string("stream_alive: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* J) {
+    if (!st || !J) return fail("stream_submit: null argument");
+    if (!st->running) return fail("stream_submit: the launch is not running (gbpf_stream_start)");
+    const int alive = gbpf_stream_alive(st);
+    if (alive < 0) return -1;
+    if (!alive) return fail("stream_submit: the launch has ended (its idle limit passed); stop and start it again");
+    gbpf_solver* s = J->solver;
+    if (!s) return fail("stream_submit: job without a solver");
+    if (std::find(st->topo.begin(), st->topo.end(), s) == st->topo.end())
+        return fail("stream_submit: the job's topology was not given to gbpf_stream_start");
+    if (J->n_cases <= 0) return fail("stream_submit: the job has no cases");
+    if (!J->S || !J->V0 || !J->V || !J->iterations || !J->converged)
+        return fail("stream_submit: the job lacks an input or output array");
+    if (J->pin || J->st_ptr || J->v0_per_col)
+        return fail("stream_submit: stream jobs take one start V0 (n,), no pins and no explicit stamps");
+    // every host array page-locked: the kernel writes the outputs directly, and a copy from
+    // pageable memory would synchronize with the device -- that is, wait for the running launch
+    for (const void* a : {(const void*)J->V, (const void*)J->iterations, (const void*)J->converged,
+                          (const void*)J->served, (const void*)J->S, (const void*)J->V0, (const void*)J->out_ptr,
+                          (const void*)J->out_idx}) {
+        if (!a) continue;
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, a) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            return fail("stream_submit: inputs and outputs must be page-locked host memory (gbpf_host_alloc)");
+        }
+    }
+    if (J->out_ptr) {
+        if (!s->m) return fail("stream_submit: outage cases need the solver's branch table (gbpf_set_branches)");
+        if (J->s_per_col || J->v0_per_col || !J->out_idx)
+            return fail("stream_submit: outage cases take one S and one V0 (n,) and out_ptr / out_idx");
+        if (J->out_ptr[0] != 0) return fail("stream_submit: outage pointers must start at 0");
+        for (int c = 0; c < J->n_cases; ++c)
+            if (J->out_ptr[c + 1] < J->out_ptr[c]) return fail("stream_submit: outage pointers must not decrease");
+        for (int q = 0; q < J->out_ptr[J->n_cases]; ++q)
+            if (J->out_idx[q] < 0 || J->out_idx[q] >= s->m) return fail("stream_submit: outage index out of range");
+    } else if (J->served) {
+        return fail("stream_submit: a served mask belongs to outage cases");
+    }
+    const int G = stream_slots(st, s);
+    if (st->published >= st->capacity) return -2;  // the ring is full: stop, then start again
+    const size_t n = s->n, T = J->n_cases;
+    const size_t sb = n * (J->s_per_col ? T : 1) * 16, vb = n * 16;
+    const int nout = J->out_ptr ? J->out_ptr[T] : 0;
+    const int igrid = (int)std::min<size_t>(T, 32);  // the islanding runs beside the launch, on spare SMs
+    // the job's staging: S, V0, its start table, and for outage cases the lists and islanding
+    const size_t parts[] = {sb, vb, n * 64, (T + 1) * 4, (size_t)std::max(nout, 1) * 4, n * T * 4, n * T * 4,
+                            n * T, T * 4, (size_t)igrid * 4 * n * 4, (size_t)igrid * n * 8};
+    const int nparts = J->out_ptr ? 11 : 3;
+    size_t need = 0;
+    for (int k = 0; k < nparts; ++k) need += up256s(parts[k]);
+    if (need > st->arena_bytes) return fail("stream_submit: the job needs more staging than the arena holds");
+    const int q = st->published;
+    const size_t at = arena_block(st, q, need);
+    if (at == SIZE_MAX) return -2;  // the arena is busy with earlier jobs: wait for them, or stop and start again
+    char* blk[11] = {};
+    size_t pos = at;
+    for (int k = 0; k < nparts; ++k) {
+        blk[k] = st->arena.as<char>() + pos;
+        pos += up256s(parts[k]);
+    }
+    char *dS = blk[0], *dV0 = blk[1], *dtab = blk[2], *dop = blk[3], *doi = blk[4], *dlab = blk[5],
+         *dref = blk[6], *dsv = blk[7], *dni = blk[8], *dscr = blk[9], *dbest = blk[10];
+    CK(cudaMemcpyAsync(dS, J->S, sb, cudaMemcpyHostToDevice, st->sub));
+    CK(cudaMemcpyAsync(dV0, J->V0, vb, cudaMemcpyHostToDevice, st->sub));
+    gbpf::Job& o = st->host_jobs[q];
+    o = gbpf::Job{};
+    Shape* sh = nullptr;
+    if (int rc = get_shape(s, 512, G, &sh)) return rc;
+    o.P = sh->dp;
+    Shape* sh1 = sh;
+    if (G > 1)
+        if (int rc = get_shape(s, 512, 1, &sh1)) return rc;
+    o.P1 = sh1->dp;
+    o.off = solver_offsets(s, G, st->mixed);
+    o.G = G;
+    o.log2G = ilog2(G);
+    o.seq = q;
+    gbpf::Batch b{};
+    b.B = (int)T;
+    b.S = reinterpret_cast<const double2*>(dS);
+    b.s_shared = !J->s_per_col;
+    b.sS = (long long)T;
+    b.V0 = reinterpret_cast<const double2*>(dV0);
+    b.v0_shared = 1;
+    b.v0tab = reinterpret_cast<const double4_32a*>(dtab);
+    if (J->out_ptr) {
+        CK(cudaMemcpyAsync(dop, J->out_ptr, (T + 1) * 4, cudaMemcpyHostToDevice, st->sub));
+        if (nout) CK(cudaMemcpyAsync(doi, J->out_idx, (size_t)nout * 4, cudaMemcpyHostToDevice, st->sub));
+        CK(gbpf::launch_islands(s->n, s->m, s->dbr_f.as<int>(), s->dbr_t.as<int>(), s->dbr_live.as<uint8_t>(),
+                                (int)T, reinterpret_cast<const int*>(dop), reinterpret_cast<const int*>(doi),
+                                s->dslack.as<uint8_t>(), s->dprio.as<double>(), J->reslack,
+                                reinterpret_cast<int*>(dscr), reinterpret_cast<unsigned long long*>(dbest),
+                                reinterpret_cast<int*>(dlab), reinterpret_cast<uint8_t*>(dsv),
+                                reinterpret_cast<int*>(dref), reinterpret_cast<int*>(dni), st->derr() + 6, igrid,
+                                st->sub));
+        if (J->served) CK(cudaMemcpyAsync(J->served, dsv, n * T, cudaMemcpyDeviceToHost, st->sub));
+        b.ymode = 3;
+        b.out_ptr = reinterpret_cast<const int*>(dop);
+        b.out_idx = reinterpret_cast<const int*>(doi);
+        b.ref_bus = reinterpret_cast<const int*>(dref);
+        b.sref = (long long)T;
+    }
+    b.Vout = reinterpret_cast<double2*>(J->V);
+    b.sV = (long long)T;
+    b.iters = J->iterations;
+    b.conv = J->converged;
+    fill_common(b, s, st->p);
+    b.counter = st->dcounter() + q;
+    b.stats = st->dstats();
+    b.err = st->derr();
+    o.B = b;
+    // the start table (run beside the launch on the submit stream, before the job is published)
+    CK(gbpf::launch_v0_table(b.V0, s->n, b.check_v0, const_cast<double4_32a*>(b.v0tab), b.err, st->sub));
+    // descriptor first, then the published count: stream order puts both behind the inputs
+    CK(cudaMemcpyAsync(st->ring.as<char>() + (size_t)q * gbpf_stream::job_stride(), &o, sizeof(gbpf::Job),
+                       cudaMemcpyHostToDevice, st->sub));
+    CK(cudaMemcpyAsync(st->dctl(), st->host_pub + q, 4, cudaMemcpyHostToDevice, st->sub));
+    st->published = q + 1;
+    return q;
+}
+
+const int* gbpf_stream_flags(gbpf_stream* st) { return st ? st->host_done : nullptr; }
+
+int gbpf_stream_done(gbpf_stream* st, int q) {
+    if (!st) return fail("null stream");
+    if (q < 0 || q >= st->published) return fail("stream_done: no such job in this launch");
+    const int v = *(volatile const int*)(st->host_done + q);
+    std::atomic_thread_fence(std::memory_order_acquire);  // the job's results are read after its flag
+    return v ? 1 : 0;
+}
+
+int gbpf_stream_stop(gbpf_stream* st) {
+    if (!st) return fail("null stream");
+    if (!st->running) return 0;
+    st->running = false;
+    CK(cudaMemcpyAsync(st->dctl() + 1, st->host_one, 4, cudaMemcpyHostToDevice, st->sub));
+    CK(cudaStreamSynchronize(st->sub));
+    CK(cudaStreamSynchronize(st->run));
+    int words[3] = {0, 0, 0}, err[16];
+    CK(cudaMemcpy(words, st->dctl(), 12, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(err, st->derr(), sizeof err, cudaMemcpyDeviceToHost));
+    if (err[0] == gbpf::DE_V0_NONFINITE || err[0] == gbpf::DE_V0_MAGNITUDE)
+        return fail("stream: invalid initial voltage at bus " + std::to_string(err[1]));
+    if (err[0] == gbpf::DE_STAMPS) return fail("stream: an outage case has too many stamp entries");
+    if (err[6]) return fail("stream: label propagation of an outage job did not settle");
+    if (words[2] == 2) return fail("stream: a job descriptor did not hold the job its index names");
+    return words[2] ? 1 : 0;
 }
 
 }  // extern "C"

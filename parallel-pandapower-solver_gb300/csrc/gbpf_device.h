@@ -141,22 +141,45 @@ struct ScratchOffsets {
 
 // One job of a launch: a topology's plan (with the schedule of the launch's CTA shape), a
 // batch of its cases, and where its scratch sits in a CTA's region.
-struct Job {
+// 256-byte aligned, so an array of jobs has one stride on the host and the device and no two
+// jobs share a cache line.
+struct alignas(256) Job {
     DevPlan P;
     DevPlan P1;              // the same topology with the one-slot schedule of the launch's CTA size
     Batch B;
     ScratchOffsets off;
     int G, log2G;            // case slots per CTA for this job (the schedule has NT / G workers)
+    int seq;                 // its index in the launch's job array (checked by stream launches)
+};
+static_assert(sizeof(Job) % 256 == 0, "jobs are laid out at a 256-byte stride");
+
+// A stream launch's job ring: the host appends job descriptors while the kernel runs and then
+// raises `published` (both by copies on one stream, so a job's descriptor and inputs are in
+// device memory before its index is published). The kernel serves published jobs in order,
+// counts every job's written-back cases and, when a job is complete, sets its flag in
+// page-locked host memory. A CTA that finds no open job polls, sleeping `sleep_ns` between
+// polls, until `stop` is set or `idle_polls` polls have passed (then it sets status 1 and
+// returns): no wait is unbounded.
+struct Ring {
+    const int* published;    // device: jobs published so far (null: not a stream launch)
+    const int* stop;         // device: 1 once no more jobs will be published
+    int* status;             // device: 1 if a CTA returned at its idle limit, 2 if a descriptor was not
+                             // the job its index says (it is then not used)
+    int* done_cases;         // device, per job: cases written back
+    int* host_done;          // page-locked host memory, per job: 1 once all its cases are written back
+    long long idle_polls;
+    unsigned sleep_ns;
 };
 
 // A launch of the persistent Newton kernel: CTAs serve the jobs in order, each job until its
 // cases run out; every CTA owns `cta_bytes` of scratch, reused job after job.
 struct Launch {
-    const Job* jobs;         // device array
+    const Job* jobs;         // device array (a stream launch: its ring of descriptors)
     int njobs;
     char* scratch;
     unsigned long long cta_bytes;
     int timed;               // the instantiation that counts SM cycles per phase (stats[8 .. 13])
+    Ring ring;
 };
 
 // Scratch layout of a job with n buses, nv block rows, nblk blocks and G slots.
@@ -210,6 +233,12 @@ cudaError_t launch_islands(int n, int m, const int* f, const int* t, const uint8
                            const int* out_idx, const uint8_t* is_slack, const double* prio, int reslack, int* scratch,
                            unsigned long long* best, int* labels, uint8_t* served, int* ref_bus, int* n_islands,
                            int* err, int grid, cudaStream_t stream);
+// Load a kernel's code into the context now (cudaFuncGetAttributes). With lazy module loading
+// a kernel is otherwise loaded at its first launch, and loading waits for the kernels running on
+// the device -- for a stream launch, until it ends; the stream launch preloads every kernel that
+// its submits launch.
+cudaError_t preload_v0_table();
+cudaError_t preload_islands();
 void set_error(const std::string& msg);  // message returned by gbpf_last_error()
 const void* newton_kernel_ptr(int threads);
 

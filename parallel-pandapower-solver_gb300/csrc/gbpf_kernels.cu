@@ -309,6 +309,67 @@ __device__ __forceinline__ double recip_nr(double x) {
     return r;
 }
 
+// Acquire load at GPU scope (a flag or count another agent writes) and release store at system
+// scope (a flag the host reads).
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys(int* p, int v) {
+    asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The next job a CTA serves (thread 0; -1: none left): the first job from *next_job on whose
+// work counter is below its units. In a stream launch (published != null), a CTA that finds
+// none polls until `stop` is set or no job has been published for idle_polls polls (status 1):
+// every newly published job starts the idle window again, so the CTAs leave together, after
+// the stream has been quiet for the whole window. Kept out of line: it runs once per job, and
+// inlined its temporaries would crowd the solve's registers.
+__device__ __noinline__ int bind_job(const Job* jobs, int njobs, const int* published, const int* stop, int* status,
+                                     long long idle_polls, unsigned sleep_ns, int* next_job) {
+    long long polls = 0;
+    int seen = -1;
+    for (;;) {
+        // a stream launch: `stop` is read before `published` (the host raises it last)
+        const bool stopping = published && ld_acquire(stop) != 0;
+        const int pub = published ? ld_acquire(published) : njobs;
+        if (pub != seen) {
+            seen = pub;
+            polls = 0;
+        }
+        for (; *next_job < pub; ++*next_job) {
+            if (published && __ldcg(&jobs[*next_job].seq) != *next_job) {  // never use a wrong descriptor
+                atomicExch(status, 2);
+                return -1;
+            }
+            const Batch* b = &jobs[*next_job].B;
+            const int* cnt = reinterpret_cast<const int*>(__ldcg(reinterpret_cast<const unsigned long long*>(&b->counter)));
+            const int units = __ldcg(&b->lanes) ? __ldcg(&b->K) : __ldcg(&b->B);
+            if (*(volatile const int*)cnt < units) return (*next_job)++;
+        }
+        if (!published || stopping) return -1;
+        if (++polls > idle_polls) {  // no job for the whole idle window: return
+            atomicCAS(status, 0, 1);
+            return -1;
+        }
+        __nanosleep(sleep_ns);
+    }
+}
+
+// A load of a job's staged input: past L1 in a stream launch, whose staging memory is refilled
+// (by the copy engine, for a later job) while the kernel runs.
+template <bool RING, typename T>
+__device__ __forceinline__ T ld_in(const T* p) {
+    if constexpr (RING) return __ldcg(p);
+    else return *p;
+}
+__device__ __forceinline__ double4_32a ldcg4(const double4_32a* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return make_double4_32a(a.x, a.y, b.x, b.y);
+}
+
 // Per-phase clock (timed launches only): thread 0, just past a barrier that ends phase k, adds
 // the SM cycles since the previous mark to the CTA's counter of phase k.
 __device__ __forceinline__ void phase_mark(unsigned long long* ph, long long* clk, int k) {
@@ -618,7 +679,7 @@ __device__ __forceinline__ bool pivots_ok(unsigned long long bmin, unsigned long
 // NTB threads per CTA and 1024 / NTB resident CTAs per SM (64 registers per thread in
 // every variant): smaller CTAs let one CTA's latency-bound factorization overlap another's
 // double-precision evaluation on the same SM.
-template <int NTB, bool TIMED>
+template <int NTB, bool TIMED, bool RING>
 __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L) {
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
@@ -629,12 +690,20 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ int s_solo;
     __shared__ double4_32a s_dinv64[NTB];  // double passes: each worker's inverse diagonal (off the registers)
     __shared__ int s_job;
+    __shared__ ScratchOffsets s_off;
+    __shared__ int s_G, s_lg, s_fin;
     int next_job = 0;  // thread 0: first job this CTA has not finished yet
+    if (tid == 0) s_fin = 0;
     for (;;) {
     // ------------------------------------------------------------------ bind the next job
     // Jobs are taken in order; a job is open while its work counter is below its units.
-    // Every CTA that finds a job open serves it until the job runs out of cases.
-    if (tid == 0) {
+    // Every CTA that finds a job open serves it until the job runs out of cases. Descriptors
+    // are read past L1 (a stream launch's descriptors are written while the kernel runs).
+    if constexpr (RING) {
+        if (tid == 0)
+            s_job = bind_job(L.jobs, L.njobs, L.ring.published, L.ring.stop, L.ring.status, L.ring.idle_polls,
+                             L.ring.sleep_ns, &next_job);
+    } else if (tid == 0) {
         int sel = -1;
         for (; next_job < L.njobs; ++next_job) {
             const Batch& b = L.jobs[next_job].B;
@@ -649,18 +718,29 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     const int job = s_job;
     if (job < 0) break;
     {
+        // (a stream launch's descriptors are written while the kernel runs: read past L1)
         const int* src = reinterpret_cast<const int*>(&L.jobs[job].P);
         int* dst = reinterpret_cast<int*>(&s_plan);
-        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = src[w];
+        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = RING ? __ldcg(src + w) : src[w];
         src = reinterpret_cast<const int*>(&L.jobs[job].B);
         dst = reinterpret_cast<int*>(&s_batch);
-        for (int w = tid; w < (int)(sizeof(Batch) / 4); w += NT) dst[w] = src[w];
+        for (int w = tid; w < (int)(sizeof(Batch) / 4); w += NT) dst[w] = RING ? __ldcg(src + w) : src[w];
         src = reinterpret_cast<const int*>(&L.jobs[job].P1);
         dst = reinterpret_cast<int*>(&s_plan1);
-        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = src[w];
+        for (int w = tid; w < (int)(sizeof(DevPlan) / 4); w += NT) dst[w] = RING ? __ldcg(src + w) : src[w];
+        if constexpr (RING) {
+            src = reinterpret_cast<const int*>(&L.jobs[job].off);
+            dst = reinterpret_cast<int*>(&s_off);
+            for (int w = tid; w < (int)(sizeof(ScratchOffsets) / 4); w += NT) dst[w] = __ldcg(src + w);
+            if (tid == 0) {
+                s_G = __ldcg(&L.jobs[job].G);
+                s_lg = __ldcg(&L.jobs[job].log2G);
+            }
+        }
     }
-    const ScratchOffsets& off = L.jobs[job].off;
-    const int G = L.jobs[job].G, lg = L.jobs[job].log2G;  // case slots of this job's CTAs
+    if constexpr (RING) __syncthreads();
+    const ScratchOffsets& off = RING ? s_off : L.jobs[job].off;
+    const int G = RING ? s_G : L.jobs[job].G, lg = RING ? s_lg : L.jobs[job].log2G;  // case slots of this job's CTAs
     double4_32a* fac64 = reinterpret_cast<double4_32a*>(region + off.fac64);
     float4* fac32 = off.fac32 != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32) : nullptr;
     float4* fac32b = off.fac32b != ~0ULL ? reinterpret_cast<float4*>(region + off.fac32b) : nullptr;
@@ -757,7 +837,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     s_vote[s] = Bt.mixed ? 1 : 0;
                     int nst = 0;
                     if (Bt.ymode == 3) {  // the stamps of the case's outaged branches
-                        const int e0 = Bt.out_ptr[c], e1 = Bt.out_ptr[c + 1];
+                        const int e0 = ld_in<RING>(Bt.out_ptr + c), e1 = ld_in<RING>(Bt.out_ptr + c + 1);
                         int nb = e1 - e0;
                         if (nb < 0 || 4 * nb > MAX_STAMPS) {
                             if (atomicCAS(&Bt.err[0], 0, DE_STAMPS) == 0) {
@@ -767,7 +847,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                             nb = nb < 0 ? 0 : MAX_STAMPS / 4;
                         }
                         for (int q = 0; q < nb; ++q) {
-                            const int b = Bt.out_idx[e0 + q];
+                            const int b = ld_in<RING>(Bt.out_idx + e0 + q);
                             if (b < 0 || b >= P.m) {  // never indexes the branch table out of range
                                 if (atomicCAS(&Bt.err[0], 0, DE_OUTAGE) == 0) {
                                     Bt.err[1] = b;
@@ -834,7 +914,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 // previous hour of the lane converged here: its evaluated state is the start point
             } else if (Bt.v0_shared) {
                 // shared start: the state table built once per launch (v0_table_kernel)
-                const double4_32a t0 = Bt.v0tab[2 * bus], t1 = Bt.v0tab[2 * bus + 1];
+                const double4_32a t0 = RING ? ldcg4(Bt.v0tab + 2 * bus) : Bt.v0tab[2 * bus];
+                const double4_32a t1 = RING ? ldcg4(Bt.v0tab + 2 * bus + 1) : Bt.v0tab[2 * bus + 1];
                 Vb0[idx] = t0;
                 if (fixed) Vb1[idx] = t0;
                 Et[idx] = make_double2(t1.x, t1.y);
@@ -871,7 +952,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 // islands of an outage case (solver_cpp.py:121-134): an unserved bus is pinned at
                 // 1 + 0j; an island re-slacked to bus r starts rotated so that r has angle 0 (r
                 // itself at |v0| + 0j, pinned); islands holding a slack keep the start as it is
-                const int r = Bt.ref_bus[(size_t)bus * Bt.sref + c];
+                const int r = ld_in<RING>(Bt.ref_bus + (size_t)bus * Bt.sref + c);
                 if (r < 0 || !P.is_slack[r]) {
                     double4_32a v;
                     double iv;
@@ -886,7 +967,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                             v = make_double4_32a(t0.x, 0.0, 1.0, 0.0);
                             pinned = 1;
                         } else {
-                            const double4_32a tr = Bt.v0tab[2 * r];
+                            const double4_32a tr = RING ? ldcg4(Bt.v0tab + 2 * r) : Bt.v0tab[2 * r];
                             v = make_double4_32a(t0.x, t0.y - tr.y, fma(t0.z, tr.z, t0.w * tr.w),
                                                  fma(t0.w, tr.z, -t0.z * tr.w));
                         }
@@ -1097,7 +1178,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int row = P.row_of_bus[bus];
             if (row < 0) continue;
             const int c = s_case[s];
-            const double2 Ssp = Bt.s_shared ? Bt.S[bus] : Bt.S[(size_t)bus * Bt.sS + c];
+            const double2 Ssp = ld_in<RING>(Bt.s_shared ? Bt.S + bus : Bt.S + (size_t)bus * Bt.sS + c);
             const bool pq = P.bus_pq[bus] != 0;
             if (st == SL_FRESH && s_first[s]) {
                 // from the shared start: S - S(V0) with S(V0) computed once (the same operation
@@ -1229,10 +1310,13 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int bus = idx >> lg;
             const double4_32a v = (s_tb[s] ? Vb1 : Vb0)[idx];
             double2 o = make_double2(v.x * v.z, v.x * v.w);
-            if (Bt.ref_bus && Bt.ref_bus[(size_t)bus * Bt.sref + s_case[s]] < 0)
+            if (Bt.ref_bus && ld_in<RING>(Bt.ref_bus + (size_t)bus * Bt.sref + s_case[s]) < 0)
                 o = make_double2(__longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0x7ff8000000000000LL));
             Bt.Vout[(size_t)bus * Bt.sV + s_case[s]] = o;
         }
+        // a stream launch's results go to host memory: each writer makes its stores visible
+        // to the host before the job's completion can be flagged
+        if constexpr (RING) __threadfence_system();
         __syncthreads();
         if (tid < G && s_st[tid] == SL_FINISH) {
             const int s = tid;
@@ -1241,8 +1325,20 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             if (Bt.mis) Bt.mis[s_case[s]] = s_nrm[s];
             s_warm[s] = Bt.lanes && s_conv[s];
             s_st[s] = SL_EMPTY;
+            if constexpr (RING) {
+                __threadfence_system();
+                atomicAdd(&s_fin, 1);
+            }
         }
         __syncthreads();
+        if (RING && tid == 0 && s_fin) {  // the job's last cases written back: flag it
+            const int old = atomicAdd(&L.ring.done_cases[job], s_fin);
+            if (old + s_fin == Bt.B) {
+                __threadfence_system();
+                st_release_sys(&L.ring.host_done[job], 1);
+            }
+            s_fin = 0;
+        }
         if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 5);
     }
 #undef GBPF_PH
@@ -1335,6 +1431,11 @@ cudaError_t launch_conversions(const double* in, int n, float* d2f, double* f2d,
 cudaError_t launch_v0_table(const double2* V0, int n, int check, double4_32a* tab, int* err, cudaStream_t stream) {
     v0_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(V0, n, check, tab, err);
     return cudaGetLastError();
+}
+
+cudaError_t preload_v0_table() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, v0_table_kernel);
 }
 
 // DC start (NewtonPowerflowCpp.py:422-440 _pre_dc_solve, timeseries.py:200-247
@@ -1566,15 +1667,18 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
 }
 
 cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream) {
-    if (threads == 1024)
-        L.timed ? newton_kernel<1024, true><<<grid, 1024, 0, stream>>>(L)
-                : newton_kernel<1024, false><<<grid, 1024, 0, stream>>>(L);
+    if (L.ring.published) {  // a stream launch: 512-thread CTAs, untimed
+        if (threads != 512 || L.timed) return cudaErrorInvalidValue;
+        newton_kernel<512, false, true><<<grid, 512, 0, stream>>>(L);
+    } else if (threads == 1024)
+        L.timed ? newton_kernel<1024, true, false><<<grid, 1024, 0, stream>>>(L)
+                : newton_kernel<1024, false, false><<<grid, 1024, 0, stream>>>(L);
     else if (threads == 512)
-        L.timed ? newton_kernel<512, true><<<grid, 512, 0, stream>>>(L)
-                : newton_kernel<512, false><<<grid, 512, 0, stream>>>(L);
+        L.timed ? newton_kernel<512, true, false><<<grid, 512, 0, stream>>>(L)
+                : newton_kernel<512, false, false><<<grid, 512, 0, stream>>>(L);
     else if (threads == 256)
-        L.timed ? newton_kernel<256, true><<<grid, 256, 0, stream>>>(L)
-                : newton_kernel<256, false><<<grid, 256, 0, stream>>>(L);
+        L.timed ? newton_kernel<256, true, false><<<grid, 256, 0, stream>>>(L)
+                : newton_kernel<256, false, false><<<grid, 256, 0, stream>>>(L);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -1588,9 +1692,9 @@ cudaError_t launch_eval_debug(const DevPlan& P, const double2* V, const double2*
 }
 
 const void* newton_kernel_ptr(int threads) {
-    if (threads == 1024) return (const void*)newton_kernel<1024, false>;
-    if (threads == 512) return (const void*)newton_kernel<512, false>;
-    return (const void*)newton_kernel<256, false>;
+    if (threads == 1024) return (const void*)newton_kernel<1024, false, false>;
+    if (threads == 512) return (const void*)newton_kernel<512, false, false>;
+    return (const void*)newton_kernel<256, false, false>;
 }
 
 }  // namespace gbpf

@@ -173,6 +173,11 @@ cudaError_t gbpf::launch_islands(int n, int m, const int* f, const int* t, const
     return cudaGetLastError();
 }
 
+cudaError_t gbpf::preload_islands() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, islands_kernel);
+}
+
 extern "C" int gbpf_islands(int n, int m, const int32_t* f, const int32_t* t, const uint8_t* live, int L,
                             const int32_t* out_ptr, const int32_t* out_idx, const uint8_t* is_slack,
                             const double* gen_prio, int reslack, int32_t* labels, uint8_t* served, int32_t* ref_bus,

@@ -362,3 +362,135 @@ def poisson_stream(topos: list[Topology], rate: float, duration: float, seed: in
             outs = np.sort(rng.choice(nb, L, replace=False)).astype(np.int32)
             out.append(Request(len(out), k, kind, t, g.Sbus.copy(), outs))
     return out
+
+
+class StreamServer:
+    """Slot-level admission: ONE persistent launch (``stream.GpuStream``) serves the stream.
+    Every request becomes a job of its own the moment it arrives -- its inputs are staged and
+    its descriptor appended to the running launch -- and the kernel's CTAs take it as soon as
+    they run out of cases of earlier jobs; its results land in page-locked host memory and its
+    flag is polled here. Requests therefore never wait for another launch to finish. Staging and
+    result memory are reused as jobs finish (a request waits only while they are all held by
+    running jobs); when a launch's ring of job slots is used up, the server stops it (it finishes
+    every job it took), starts a new one and goes on.
+
+    Same request and response types as ``Server``; every case runs the same arithmetic as in
+    any other launch, so each result equals the one it gets alone (bit for bit). ``backend``:
+    the launch object (a ``GpuStream`` by default; tests may pass a stand-in)."""
+
+    def __init__(self, topologies: list[Topology], precision: str = "mixed", tol: float = 1e-8, max_iter: int = 30,
+                 capacity: int = 8192, arena_bytes: int = 8 << 30, result_bytes: int = 4 << 30,
+                 idle_seconds: float = 10.0, backend=None, **solver_params):
+        self.topos = topologies
+        solver_params.setdefault("shared_start", False)
+        self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
+        self.idle_seconds = idle_seconds
+        if backend is None:
+            from .stream import GpuStream
+
+            backend = GpuStream(capacity=capacity, arena_bytes=arena_bytes, result_bytes=result_bytes)
+        self.backend = backend
+        self.launches = 0
+
+    def _start(self):
+        self.backend.start([tp.solver for tp in self.topos], self.params, self.idle_seconds)
+        self.launches += 1
+
+    def _submit(self, r: Request):
+        tp = self.topos[r.topo]
+        if r.kind == "n1":
+            L = len(r.outages)
+            outages = (np.arange(L + 1, dtype=np.int32), np.ascontiguousarray(r.outages, dtype=np.int32))
+            return self.backend.submit(tp.solver, r.S, tp.V_warm, outages=outages, reslack=True)
+        return self.backend.submit(tp.solver, r.S, tp.V_warm)
+
+    def run(self, requests: list[Request], realtime: bool = True, keep_results: bool = True) -> list[Response]:
+        """Serve a request stream (``Server.run``'s semantics). A response's ``start`` is the
+        moment its job was handed to the running launch; ``launch`` counts the launches."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        responses: dict[int, Response] = {}
+        pending: deque = deque()
+        outstanding: dict[int, tuple] = {}
+        t0 = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t0
+
+        def finish(q, done_t):
+            r, outs, started = outstanding.pop(q)
+            V, it, cv, sv = outs
+            if keep_results:  # out of the launch's result memory, which later jobs reuse
+                V, sv = np.array(V), (None if sv is None else np.array(sv, dtype=bool))
+            else:
+                V = sv = None
+            responses[r.rid] = Response(r.rid, V, np.array(it), np.array(cv, dtype=bool), r.arrival, started,
+                                        done_t, self.launches - 1, sv)
+            self.backend.release(q)
+
+        def drain():
+            # every job the launch started has its results when stop returns; after an idle
+            # return (1), jobs published once its CTAs had left were never started: they go
+            # back to the front of the queue, for the next launch
+            idle = self.backend.stop() == 1
+            t = now()
+            flags = self.backend.flags()
+            redo = []
+            for q in sorted(outstanding):
+                if flags[q] and self.backend.done(q):
+                    finish(q, t)
+                elif idle:
+                    redo.append(outstanding.pop(q)[0])
+                else:
+                    raise RuntimeError(f"stream launch stopped with job {q} unfinished")
+            pending.extendleft(reversed(redo))
+
+        self._start()
+        try:
+            i = 0
+            while i < len(reqs) or pending or outstanding:
+                t = now()
+                while i < len(reqs) and (not realtime or reqs[i].arrival <= t):
+                    pending.append(reqs[i])
+                    i += 1
+                busy = False
+                if pending and not self.backend.alive():  # the launch reached its idle limit
+                    drain()
+                    self._start()
+                while pending:
+                    r = pending[0]
+                    sub = self._submit(r)
+                    if sub is None:
+                        if outstanding and not self.backend.full():
+                            break  # staging / result memory held by running jobs: retry as they finish
+                        drain()  # the launch's ring is full: finish it and start the next
+                        self._start()
+                        sub = self._submit(r)
+                        if sub is None:
+                            raise RuntimeError(f"request {r.rid} does not fit an empty launch (raise its limits)")
+                    pending.popleft()
+                    outstanding[sub[0]] = (r, sub[1], now())
+                    busy = True
+                if outstanding:
+                    flags = self.backend.flags()
+                    ready = [q for q in outstanding if flags[q]]
+                    if ready:
+                        t = now()
+                        for q in ready:
+                            if self.backend.done(q):  # (an acquire fence before the results are read)
+                                finish(q, t)
+                        busy = True
+                    elif not self.backend.alive():  # ended at its idle limit before these jobs started
+                        drain()
+                        self._start()
+                        busy = True
+                if not busy:
+                    wait = 2e-5
+                    if realtime and i < len(reqs) and not outstanding:
+                        wait = max(wait, min(reqs[i].arrival - now(), 0.002))
+                    time.sleep(wait)
+        finally:
+            if outstanding:
+                drain()
+            else:
+                self.backend.stop()
+        return [responses[r.rid] for r in requests]

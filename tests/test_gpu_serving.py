@@ -49,3 +49,57 @@ def test_served_mixed_results_match_the_converged_double_solution(topos):
         ok = a.converged
         if ok.any():
             assert np.nanmax(np.abs(a.V[:, ok] - b.V[:, ok])) < 1e-9
+
+
+def test_stream_launch_results_are_the_same_alone_and_in_the_mix(topos):
+    """Slot-level admission: one running launch takes every request as it arrives; each result
+    equals the request's own launch bit for bit (also N-1 islanding)."""
+    from p3s_gb300.serving import StreamServer
+
+    reqs = poisson_stream(topos, rate=400.0, duration=0.3, seed=7, chunk=12, n1_outages=24, mix=(0.6, 0.3, 0.1))
+    assert {r.kind for r in reqs} == {"single", "chunk", "n1"}
+    srv = StreamServer(topos, precision="mixed", capacity=64, arena_bytes=1 << 30, result_bytes=256 << 20)
+    got = srv.run(reqs, realtime=True)
+    assert srv.launches >= 2  # the 64-job ring was refilled by a new launch
+    alone = Server(topos, precision="mixed", contexts=1)
+    for r, g in zip(reqs, got):
+        ref = alone.run([r], realtime=False)[0]
+        assert np.array_equal(g.iterations, ref.iterations) and np.array_equal(g.converged, ref.converged)
+        assert np.array_equal(np.isnan(g.V), np.isnan(ref.V)) and np.array_equal(np.nan_to_num(g.V),
+                                                                                   np.nan_to_num(ref.V))
+        if r.kind == "n1":
+            assert np.array_equal(g.served, ref.served)
+    assert latency_summary(got)["converged_fraction"] == 1.0
+
+
+def test_stream_launch_returns_at_its_idle_limit_and_starts_again(topos):
+    """A launch that gets no job for its idle window returns by itself (status 1 at stop) --
+    its polling is bounded; a full ring refuses the next job until the launch is restarted."""
+    import time
+
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.stream import GpuStream
+
+    tp = topos[1]
+    p = GpuSolver.params(precision="double", shared_start=False)
+    st = GpuStream(capacity=2, arena_bytes=64 << 20, result_bytes=16 << 20)
+    st.start([tp.solver], p, idle_seconds=0.05)
+    t = time.perf_counter()
+    while st.alive() and time.perf_counter() - t < 20.0:
+        time.sleep(0.01)
+    assert not st.alive()
+    assert st.stop() == 1
+    S = tp.grid.Sbus
+    # (before the launch: while a stream launch runs it holds the SMs, and another launch waits)
+    ref = tp.solver.solve_batch(S[:, None], tp.V_warm, p)
+    st.start([tp.solver], p, idle_seconds=10.0)
+    jobs = [st.submit(tp.solver, S, tp.V_warm) for _ in range(2)]
+    assert all(j is not None for j in jobs)
+    assert st.submit(tp.solver, S, tp.V_warm) is None  # ring full
+    t = time.perf_counter()
+    while not all(st.flags()[q] for q, _ in jobs) and time.perf_counter() - t < 20.0:
+        time.sleep(0.001)
+    assert all(st.done(q) for q, _ in jobs)
+    for _, (V, it, cv, _) in jobs:
+        assert np.array_equal(V, ref["V"]) and np.array_equal(it, ref["iterations"]) and cv.all()
+    assert st.stop() == 0

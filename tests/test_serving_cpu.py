@@ -139,3 +139,151 @@ def test_serving_loop_delivers_every_request(keep):
         else:
             assert r.V is None and r.served is None
     assert sum(sum(g.calls) for g in s.groups) >= len({r.launch for r in resp})
+
+
+class _FakeStream:
+    """Stand-in for a stream launch: a job's results (V = its request's S, iterations 3) are
+    ready `delay` polls after its submit; at most `capacity` jobs per launch."""
+
+    def __init__(self, capacity, delay=2, die_after=None):
+        self.capacity, self.delay, self.die_after = capacity, delay, die_after
+        self.starts, self.stops, self.polls = 0, 0, 0
+
+    def start(self, solvers, params, idle_seconds):
+        self.starts += 1
+        self.jobs, self.flag = [], np.zeros(self.capacity, np.int32)
+        self.running = True
+        self.launch_polls = 0
+
+    def submit(self, solver, S, V0, outages=None, reslack=True):
+        assert self.running
+        if len(self.jobs) == self.capacity:
+            return None
+        T = S.shape[1] if S.ndim == 2 else 1
+        outs = (np.array(S).reshape(-1, T).copy(), np.full(T, 3, np.int32), np.ones(T, np.uint8),
+                np.ones((len(V0), T), np.uint8) if outages is not None else None)
+        self.jobs.append(self.polls)
+        return len(self.jobs) - 1, outs
+
+    def _dead(self):  # only the first launch reaches its idle limit, after die_after polls
+        return self.die_after is not None and self.starts == 1 and self.launch_polls >= self.die_after
+
+    def flags(self):
+        if self.running and not self._dead():
+            self.polls += 1
+            self.launch_polls += 1
+            for q, t in enumerate(self.jobs):
+                if self.polls - t >= self.delay:
+                    self.flag[q] = 1
+        return self.flag
+
+    def done(self, q):
+        return bool(self.flag[q])
+
+    def full(self):
+        return len(self.jobs) == self.capacity
+
+    def release(self, q):
+        self.released = getattr(self, "released", 0) + 1
+
+    def alive(self):
+        return not self._dead()
+
+    def stop(self):
+        self.stops += 1
+        self.running = False
+        if self._dead():  # returned at its idle limit: unstarted jobs keep flag 0
+            return 1
+        self.flag[:len(self.jobs)] = 1
+        return 0
+
+
+def _stream_server(topos, backend):
+    from p3s_gb300.serving import StreamServer
+
+    s = object.__new__(StreamServer)
+    s.topos, s.params, s.idle_seconds, s.backend, s.launches = topos, None, 1.0, backend, 0
+    return s
+
+
+def test_stream_server_admits_as_requests_arrive_and_restarts_a_full_launch():
+    topos = [SimpleNamespace(solver=None, V_warm=np.ones(118, complex), grid=grid_118(), n=118)]
+    reqs = [Request(i, 0, "single" if i % 3 else "chunk", 0.0,
+                    np.full((118,) if i % 3 else (118, 4), i + 1.0, complex)) for i in range(10)]
+    reqs.append(Request(10, 0, "n1", 0.0, np.zeros(118, complex), np.arange(5)))
+    fake = _FakeStream(capacity=3)
+    srv = _stream_server(topos, fake)
+    out = srv.run(reqs, realtime=False)
+    assert [r.rid for r in out] == list(range(11))
+    assert fake.starts == 4 and fake.stops == 4  # 11 jobs, 3 per launch
+    for r, resp in zip(reqs, out):
+        assert np.array_equal(resp.V.reshape(r.S.shape) if r.kind != "n1" else resp.V[:, 0], r.S if r.kind != "n1"
+                              else np.zeros(118))
+        assert (resp.iterations == 3).all() and resp.converged.all() and resp.done >= resp.start
+    assert out[10].served is not None and out[10].served.all()
+    assert {r.launch for r in out} == {0, 1, 2, 3}
+
+
+def test_stream_server_resubmits_the_jobs_a_launch_left_at_its_idle_limit():
+    """A launch whose CTAs left at their idle limit before some jobs were published: the
+    server stops it (status 1), keeps the finished jobs' results and submits the unstarted
+    ones again, in order, to a new launch."""
+    topos = [SimpleNamespace(solver=None, V_warm=np.ones(118, complex), grid=grid_118(), n=118)]
+    reqs = [Request(i, 0, "single", 0.0, np.full(118, i + 1.0, complex)) for i in range(3)]
+    fake = _FakeStream(capacity=8, delay=4, die_after=3)
+    srv = _stream_server(topos, fake)
+    out = srv.run(reqs, realtime=False)
+    assert fake.starts == 2 and fake.stops == 2
+    assert [r.launch for r in out] == [1, 1, 1]  # none finished in the first launch
+    for r, resp in zip(reqs, out):
+        assert np.array_equal(resp.V[:, 0], r.S) and resp.converged.all()
+
+
+def test_stream_server_reports_a_stopped_launch_with_jobs_unfinished():
+    class Broken(_FakeStream):
+        def stop(self):
+            self.stops += 1
+            self.running = False
+            return 0  # a clean stop must leave no job unfinished
+
+    topos = [SimpleNamespace(solver=None, V_warm=np.ones(118, complex), grid=grid_118(), n=118)]
+    reqs = [Request(0, 0, "single", 0.0, np.ones(118, complex))]
+    srv = _stream_server(topos, Broken(capacity=4, delay=10 ** 9, die_after=3))
+    with pytest.raises(RuntimeError, match="unfinished"):
+        srv.run(reqs, realtime=False)
+
+
+def test_stream_result_memory_is_reused_in_job_order_and_refuses_when_full():
+    """The stream launch's circular result memory: blocks in job order, refused while every
+    byte is held by unconsumed jobs, given back in job order (a later job's release waits for
+    the older ones), reused across the wrap; a block taken for a job that was then not
+    submitted is given back at once."""
+    from p3s_gb300 import stream
+
+    class Slab(stream._Slab):
+        def __init__(self, n):
+            self.nbytes, self.buf = n, bytearray(n)
+            self.reset()
+
+        def __del__(self):
+            pass
+
+    f8 = np.float64
+    s = Slab(4096)
+    assert s.take(0, [((100,), f8)]) is not None and s.take(1, [((200,), f8)]) is not None
+    assert s.take(2, [((150,), f8)]) is not None and s.head == 4096
+    assert s.take(3, [((10,), f8)]) is None  # full
+    s.release(1)
+    assert s.tail == 0  # job 0 still holds the front
+    s.release(0)
+    assert s.tail == 2816
+    v = s.take(3, [((100,), f8), ((4,), np.int32)])
+    assert v is not None and s.wrapped and s.head == 1024 + 256 and v[0].shape == (100,) and v[1].dtype == np.int32
+    s.undo(3)
+    assert s.head == 4096 and not s.wrapped
+    assert s.take(3, [((100,), f8)]) is not None and s.wrapped
+    s.release(2)
+    s.release(3)
+    assert s.order == [] and s.head == s.tail
+    with pytest.raises(ValueError, match="exceed the result memory"):
+        s.take(4, [((1000,), f8)])
