@@ -279,8 +279,11 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
  * counterpart: the reference solves one call at a time (nr_polar_solver.py:466-596) and has no
  * serving loop.
  * create: capacity = jobs per launch; arena_bytes = device staging for the inputs of one launch;
- *   ctas = 512-thread CTAs (0: two per SM less 16, which keeps room for the submits' islanding
- *   kernels); slot_budget = variable buses x case slots a CTA takes per job (0: 8,192).
+ *   threads = threads per CTA, 512 or 1024 (0: 1024); ctas = CTAs (0: as many as fit on all
+ *   SMs but 8, which keep room for the submits' islanding and start-table kernels); slot_budget
+ *   = variable buses x case slots a CTA takes per job (0: 8,192). A job's CTAs take the
+ *   smallest power of two of slots that holds its cases, up to that budget: a single solve
+ *   runs on all of a CTA's threads.
  * start: launches the kernel for the given topologies (schedules built, scratch sized for them,
  *   the kernels that submits launch loaded into the context first; gbpf_params as for the other
  *   calls, the shared start off). A CTA without an open job polls every ~20 us; once no job has
@@ -303,7 +306,7 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
  * While a stream launch runs it holds most of the device's SMs: other solves on that device
  * wait until it is stopped (or its CTAs reach their idle limit) -- submit work to it instead. */
 typedef struct gbpf_stream gbpf_stream;
-gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int ctas, int slot_budget);
+gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int threads, int ctas, int slot_budget);
 void gbpf_stream_destroy(gbpf_stream* st);
 int gbpf_stream_start(gbpf_stream* st, int nsolvers, gbpf_solver* const* solvers, const gbpf_params* p,
                       double idle_seconds);

@@ -1820,7 +1820,7 @@ struct gbpf_stream {
     int* host_pub = nullptr;             // page-locked: the published count after each job
     int* host_one = nullptr;             // page-locked: the stop value
     gbpf::Job* host_jobs = nullptr;      // page-locked staging of the descriptors
-    int capacity = 0, ctas = 0, slot_budget = 8192;
+    int capacity = 0, threads = 1024, ctas = 0, slot_budget = 8192;
     size_t arena_bytes = 0;
     // circular arena: live blocks from `tail` to `head` (wrapping past the end when `wrapped`);
     // job_beg / job_end: each job's block, released in job order from tail_job on
@@ -1861,6 +1861,14 @@ int stream_slots(const gbpf_stream* st, const gbpf_solver* s) {
     return job_slots(gbpf::MAX_SLOTS, s->plan.nv, st->slot_budget);
 }
 
+// Case slots of a job's CTAs: the topology's slot count, but no more than the job has cases (a
+// single solve takes one slot, with all of the CTA's threads, for the lowest latency).
+int stream_job_slots(const gbpf_stream* st, const gbpf_solver* s, int cases) {
+    int g = 1;
+    while (g < cases && g < stream_slots(st, s)) g *= 2;
+    return g;
+}
+
 size_t up256s(size_t b) { return (std::max<size_t>(b, 1) + 255) & ~(size_t)255; }
 
 // A block of `need` bytes (a multiple of 256) of the circular arena for job `q`, after releasing
@@ -1896,13 +1904,15 @@ size_t arena_block(gbpf_stream* st, int q, size_t need) {
 
 extern "C" {
 
-gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int ctas, int slot_budget) {
-    if (capacity <= 0 || arena_bytes < 4096 || ctas < 0 || slot_budget < 0) {
-        fail("stream_create: capacity > 0, arena_bytes >= 4096, ctas >= 0, slot_budget >= 0");
+gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int threads, int ctas, int slot_budget) {
+    if (capacity <= 0 || arena_bytes < 4096 || ctas < 0 || slot_budget < 0 ||
+        (threads != 0 && threads != 512 && threads != 1024)) {
+        fail("stream_create: capacity > 0, arena_bytes >= 4096, threads 0, 512 or 1024, ctas >= 0, slot_budget >= 0");
         return nullptr;
     }
     std::unique_ptr<gbpf_stream> st(new gbpf_stream);
     st->capacity = capacity;
+    st->threads = threads ? threads : 1024;
     st->arena_bytes = arena_bytes & ~(size_t)255;
     st->job_beg.assign(capacity, 0);
     st->job_end.assign(capacity, 0);
@@ -1914,8 +1924,10 @@ gbpf_stream* gbpf_stream_create(int capacity, size_t arena_bytes, int ctas, int 
     };
     if (!ok(cudaGetDevice(&st->device))) return nullptr;
     if (!ok(cudaDeviceGetAttribute(&st->nsm, cudaDevAttrMultiProcessorCount, st->device))) return nullptr;
-    // two 512-thread CTAs per SM, less 16 CTAs' room kept free for the submits' islanding kernels
-    st->ctas = ctas ? ctas : std::max(1, 2 * st->nsm - 16);
+    // every SM's room for Newton CTAs (one of 1,024 threads or two of 512), less 8 SMs' room kept
+    // free for the submits' islanding and start-table kernels
+    const int per_sm = 1024 / st->threads;
+    st->ctas = ctas ? ctas : std::max(1, per_sm * (st->nsm - 8));
     if (!ok(cudaStreamCreateWithFlags(&st->run, cudaStreamNonBlocking))) return nullptr;
     if (!ok(cudaStreamCreateWithFlags(&st->sub, cudaStreamNonBlocking))) return nullptr;
     if (!ok(cudaEventCreateWithFlags(&st->ended, cudaEventDisableTiming))) return nullptr;
@@ -1956,10 +1968,10 @@ int gbpf_stream_start(gbpf_stream* st, int nsolvers, gbpf_solver* const* solvers
         if (!s) return fail("stream_start: null solver");
         if (s->device != st->device) return fail("stream_start: a solver lives on another device");
         const int G = stream_slots(st, s);
-        Shape* sh = nullptr;
-        if (int rc = get_shape(s, 512, G, &sh)) return rc;
-        if (G > 1)
-            if (int rc = get_shape(s, 512, 1, &sh)) return rc;
+        for (int g = 1; g <= G; g *= 2) {  // a job takes any power of two up to G slots
+            Shape* sh = nullptr;
+            if (int rc = get_shape(s, st->threads, g, &sh)) return rc;
+        }
         cta = std::max(cta, solver_offsets(s, G, st->mixed).total);
     }
     st->cta_bytes = cta;
@@ -1991,7 +2003,7 @@ int gbpf_stream_start(gbpf_stream* st, int nsolvers, gbpf_solver* const* solvers
     L.ring.host_done = dflags;
     L.ring.sleep_ns = STREAM_SLEEP_NS;
     L.ring.idle_polls = std::max<long long>(1, (long long)(idle_seconds * 1e9 / STREAM_SLEEP_NS));
-    CK(gbpf::launch_newton(L, st->ctas, 512, st->run));
+    CK(gbpf::launch_newton(L, st->ctas, st->threads, st->run));
     CK(cudaEventRecord(st->ended, st->run));
     st->running = true;
     return 0;
@@ -2045,7 +2057,7 @@ int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* J) {
     } else if (J->served) {
         return fail("stream_submit: a served mask belongs to outage cases");
     }
-    const int G = stream_slots(st, s);
+    const int G = stream_job_slots(st, s, J->n_cases);
     if (st->published >= st->capacity) return -2;  // the ring is full: stop, then start again
     const size_t n = s->n, T = J->n_cases;
     const size_t sb = n * (J->s_per_col ? T : 1) * 16, vb = n * 16;
@@ -2074,11 +2086,11 @@ int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* J) {
     gbpf::Job& o = st->host_jobs[q];
     o = gbpf::Job{};
     Shape* sh = nullptr;
-    if (int rc = get_shape(s, 512, G, &sh)) return rc;
+    if (int rc = get_shape(s, st->threads, G, &sh)) return rc;  // (built by gbpf_stream_start)
     o.P = sh->dp;
     Shape* sh1 = sh;
     if (G > 1)
-        if (int rc = get_shape(s, 512, 1, &sh1)) return rc;
+        if (int rc = get_shape(s, st->threads, 1, &sh1)) return rc;
     o.P1 = sh1->dp;
     o.off = solver_offsets(s, G, st->mixed);
     o.G = G;

@@ -1667,9 +1667,14 @@ __global__ void eval_debug_kernel(const DevPlan P, const double2* V, const doubl
 }
 
 cudaError_t launch_newton(const Launch& L, int grid, int threads, cudaStream_t stream) {
-    if (L.ring.published) {  // a stream launch: 512-thread CTAs, untimed
-        if (threads != 512 || L.timed) return cudaErrorInvalidValue;
-        newton_kernel<512, false, true><<<grid, 512, 0, stream>>>(L);
+    if (L.ring.published) {  // a stream launch: untimed
+        if (L.timed) return cudaErrorInvalidValue;
+        if (threads == 1024)
+            newton_kernel<1024, false, true><<<grid, 1024, 0, stream>>>(L);
+        else if (threads == 512)
+            newton_kernel<512, false, true><<<grid, 512, 0, stream>>>(L);
+        else
+            return cudaErrorInvalidValue;
     } else if (threads == 1024)
         L.timed ? newton_kernel<1024, true, false><<<grid, 1024, 0, stream>>>(L)
                 : newton_kernel<1024, false, false><<<grid, 1024, 0, stream>>>(L);

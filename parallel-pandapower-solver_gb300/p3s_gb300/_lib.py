@@ -145,7 +145,7 @@ SIGNATURES = {
     "gbpf_group_create": (_vp, []),
     "gbpf_group_destroy": (None, [_vp]),
     "gbpf_group_solve": (C.c_int, [_vp, C.c_int, C.POINTER(Job), C.POINTER(Params)]),
-    "gbpf_stream_create": (_vp, [C.c_int, C.c_size_t, C.c_int, C.c_int]),
+    "gbpf_stream_create": (_vp, [C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int]),
     "gbpf_stream_destroy": (None, [_vp]),
     "gbpf_stream_start": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(Params), C.c_double]),
     "gbpf_stream_submit": (C.c_int, [_vp, C.POINTER(Job)]),

@@ -380,7 +380,7 @@ class StreamServer:
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", tol: float = 1e-8, max_iter: int = 30,
                  capacity: int = 8192, arena_bytes: int = 8 << 30, result_bytes: int = 4 << 30,
-                 idle_seconds: float = 10.0, backend=None, **solver_params):
+                 idle_seconds: float = 10.0, backend=None, threads: int = 1024, **solver_params):
         self.topos = topologies
         solver_params.setdefault("shared_start", False)
         self.params = GpuSolver.params(max_iter=max_iter, tol=tol, precision=precision, **solver_params)
@@ -388,7 +388,7 @@ class StreamServer:
         if backend is None:
             from .stream import GpuStream
 
-            backend = GpuStream(capacity=capacity, arena_bytes=arena_bytes, result_bytes=result_bytes)
+            backend = GpuStream(capacity=capacity, arena_bytes=arena_bytes, result_bytes=result_bytes, threads=threads)
         self.backend = backend
         self.launches = 0
 

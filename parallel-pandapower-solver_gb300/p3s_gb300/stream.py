@@ -101,9 +101,9 @@ class _Slab:
 
 class GpuStream:
     def __init__(self, capacity: int = 8192, arena_bytes: int = 8 << 30, result_bytes: int = 4 << 30, ctas: int = 0,
-                 slot_budget: int = 8192, input_bytes: int = 0):
+                 slot_budget: int = 8192, input_bytes: int = 0, threads: int = 1024):
         L = _lib.require_device()
-        h = L.gbpf_stream_create(int(capacity), int(arena_bytes), int(ctas), int(slot_budget))
+        h = L.gbpf_stream_create(int(capacity), int(arena_bytes), int(threads), int(ctas), int(slot_budget))
         if not h:
             raise RuntimeError(_lib.last_error())
         self._h = h
