@@ -615,8 +615,9 @@ def gpu_line(args, res, rank, world):
         "unit": "GB/s",
         "frac": round(achieved / (hbm if hbm else 6800.0), 4),
         "traffic": None if tr is None else float(tr) * its_mixed,
-        "traffic_source": None if tr is None else "ncu DRAM bytes per case-iteration of one bench launch "
-                                                  "(profiles/newton_kernel_traffic.json) x this launch's case-iterations",
+        "traffic_source": None if tr is None else "ncu DRAM bytes per case-iteration of one launch of the "
+                                                  "2,000-bus x 2,432-hour case (profiles/newton_kernel_traffic.json) "
+                                                  "x this launch's case-iterations",
         "peak_source": "measured" if hbm else "fallback",
         "kernel": "newton_kernel",
         "algorithmic_bytes_per_case_iteration": B,
