@@ -455,7 +455,7 @@ gbpf::ScratchOffsets solver_offsets(const gbpf_solver* s, int G, bool mixed) {
 }
 
 gbpf_params default_params() {
-    gbpf_params p;
+    gbpf_params p{};
     p.max_iter = 30;
     p.tol = 1e-8;
     p.line_search = 1;
