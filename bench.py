@@ -544,8 +544,17 @@ def run_serving(args):
     for prec in ("mixed", "double"):
         srv = StreamServer(topos, precision=prec, backend=backend)
         srv.run(poisson_stream(topos, rate=200.0, duration=0.5, seed=1), keep_results=False)  # warm-up
-        out["fp64" if prec == "double" else prec] = {"server": "stream (slot-level admission into one running launch)",
-                                                     **sweep_rates(srv)}
+        row = {"server": "stream (slot-level admission into one running launch)"}
+        if prec == "mixed":
+            # per topology and request kind, the precision that finishes a request sooner in the
+            # running launch (measured alone, both ways): large grids' latency-bound requests
+            # may run on double factors
+            chosen = srv.tune()
+            row["precision"] = ("mixed launch; per topology and request kind the precision measured faster "
+                                "at warm-up (StreamServer.tune)")
+            row["double_by_kind"] = {k: sum(1 for (t, kk), p in chosen.items() if kk == k and p == "double")
+                                     for k in ("single", "chunk", "n1")}
+        out["fp64" if prec == "double" else prec] = {**row, **sweep_rates(srv)}
     del backend
     out["contexts"] = {}
     groups = [GpuGroup() for _ in range(4)]  # both context servers run on the same 4 launch contexts

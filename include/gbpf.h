@@ -256,6 +256,9 @@ typedef struct gbpf_job {
     int reslack;
     uint8_t* served;         /* out, outage jobs: (n, n_cases) 1 where the bus's island is served
                                 (the device islanding's mask, gbpf_islands semantics), or NULL */
+    int precision;           /* stream launches: 0 = the launch's gbpf_params.precision, 1 = double
+                                factors, 2 = mixed (a launch started with mixed precision); every
+                                other parameter is the launch's. Group launches: 0 only. */
 } gbpf_job;
 
 gbpf_group* gbpf_group_create(void);

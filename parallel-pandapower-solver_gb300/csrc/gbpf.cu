@@ -700,6 +700,8 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
             return fail(std::string(who) + ": job " + std::to_string(j) + " lacks an input or output array");
         if (J.cases_per_cta < 0 || J.cases_per_cta > gbpf::MAX_SLOTS || (J.cases_per_cta & (J.cases_per_cta - 1)))
             return fail(std::string(who) + ": job " + std::to_string(j) + ": cases_per_cta must be 0 or a power of two in 1..32");
+        if (J.precision != 0)
+            return fail(std::string(who) + ": job " + std::to_string(j) + ": a group launch takes its precision from its parameters (precision 0)");
         if (J.out_ptr) {
             if (!J.solver->m) return fail(std::string(who) + ": job " + std::to_string(j) + ": outage cases need the solver's branch table (gbpf_set_branches)");
             if (J.s_per_col || J.v0_per_col || !J.out_idx)
@@ -2033,6 +2035,15 @@ int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* J) {
         return fail("stream_submit: the job lacks an input or output array");
     if (J->pin || J->st_ptr || J->v0_per_col)
         return fail("stream_submit: stream jobs take one start V0 (n,), no pins and no explicit stamps");
+    // the job's own precision: double factors in any launch, mixed only where the launch's
+    // scratch holds the float factor buffers (a launch started with mixed precision)
+    gbpf_params pj = st->p;
+    if (J->precision == 1)
+        pj.precision = 0;
+    else if (J->precision == 2 && st->mixed)
+        pj.precision = 1;
+    else if (J->precision != 0)
+        return fail("stream_submit: precision must be 0 (the launch's), 1 (double) or 2 (mixed, in a mixed launch)");
     // every host array page-locked: the kernel writes the outputs directly, and a copy from
     // pageable memory would synchronize with the device -- that is, wait for the running launch
     for (const void* a : {(const void*)J->V, (const void*)J->iterations, (const void*)J->converged,
@@ -2125,7 +2136,7 @@ int gbpf_stream_submit(gbpf_stream* st, const gbpf_job* J) {
     b.sV = (long long)T;
     b.iters = J->iterations;
     b.conv = J->converged;
-    fill_common(b, s, st->p);
+    fill_common(b, s, pj);
     b.counter = st->dcounter() + q;
     b.stats = st->dstats();
     b.err = st->derr();

@@ -100,6 +100,7 @@ class Job(C.Structure):
         ("out_idx", _vp),
         ("reslack", C.c_int),
         ("served", _vp),
+        ("precision", C.c_int),
     ]
 
 

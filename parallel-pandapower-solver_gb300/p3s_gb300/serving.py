@@ -376,7 +376,13 @@ class StreamServer:
 
     Same request and response types as ``Server``; every case runs the same arithmetic as in
     any other launch, so each result equals the one it gets alone (bit for bit). ``backend``:
-    the launch object (a ``GpuStream`` by default; tests may pass a stand-in)."""
+    the launch object (a ``GpuStream`` by default; tests may pass a stand-in).
+
+    A mixed-precision server can run some jobs on double factors: ``tune`` measures, per
+    topology and request kind, which precision finishes a request sooner in the running launch
+    and keeps that choice (``precision_of``). On large grids a request's cases run one per CTA,
+    latency-bound, where float factors save little per iteration and the float path's extra
+    polish iterations cost more than they save."""
 
     def __init__(self, topologies: list[Topology], precision: str = "mixed", tol: float = 1e-8, max_iter: int = 30,
                  capacity: int = 8192, arena_bytes: int = 8 << 30, result_bytes: int = 4 << 30,
@@ -391,6 +397,7 @@ class StreamServer:
             backend = GpuStream(capacity=capacity, arena_bytes=arena_bytes, result_bytes=result_bytes, threads=threads)
         self.backend = backend
         self.launches = 0
+        self.precision_of: dict = {}  # (topology, kind) -> "double" / "mixed" (tune); else the launch's
 
     def _start(self):
         self.backend.start([tp.solver for tp in self.topos], self.params, self.idle_seconds)
@@ -398,11 +405,72 @@ class StreamServer:
 
     def _submit(self, r: Request):
         tp = self.topos[r.topo]
+        prec = self.precision_of.get((r.topo, r.kind))
         if r.kind == "n1":
             L = len(r.outages)
             outages = (np.arange(L + 1, dtype=np.int32), np.ascontiguousarray(r.outages, dtype=np.int32))
-            return self.backend.submit(tp.solver, r.S, tp.V_warm, outages=outages, reslack=True)
-        return self.backend.submit(tp.solver, r.S, tp.V_warm)
+            return self.backend.submit(tp.solver, r.S, tp.V_warm, outages=outages, reslack=True, precision=prec)
+        return self.backend.submit(tp.solver, r.S, tp.V_warm, precision=prec)
+
+    def _time_alone(self, r: Request) -> float:
+        """Seconds from submitting `r` alone to the running launch until its flag is set (a
+        launch that is full, or has left at its idle limit, is renewed first)."""
+        for _ in range(3):
+            if self.backend.full() or not self.backend.alive():
+                self.backend.stop()
+                self._start()
+            t0 = time.perf_counter()
+            sub = self._submit(r)
+            if sub is None:  # staging still held by this launch's earlier jobs: renew the launch
+                self.backend.stop()
+                self._start()
+                continue
+            q = sub[0]
+            while not self.backend.flags()[q] and self.backend.alive():
+                time.sleep(2e-5)
+            if self.backend.flags()[q]:
+                dt = time.perf_counter() - t0
+                self.backend.done(q)
+                self.backend.release(q)
+                return dt
+            self.backend.stop()  # the launch left before starting the job: renew and submit again
+            self._start()
+        raise RuntimeError("tune: a request did not complete in three launches")
+
+    def tune(self, chunk: int = 96, n1_outages: int = 200, repeats: int = 3, seed: int = 0) -> dict:
+        """For a mixed-precision server: per topology and request kind (single solve, chunk of
+        `chunk` steps, sweep of `n1_outages` outages), submit a request of that kind alone to a
+        running launch in each precision, `repeats` times, and keep the precision whose median
+        completion time is shorter. Returns {(topology, kind): precision}."""
+        if self.params.precision != 1:
+            return {}
+        rng = np.random.default_rng(seed)
+        reqs = []
+        for k, tp in enumerate(self.topos):
+            g = tp.grid
+            S1 = g.Sbus.copy()
+            S1[g.pq] *= rng.uniform(0.8, 1.2, len(g.pq))
+            Sc = np.repeat(g.Sbus[:, None], chunk, axis=1)
+            Sc[g.pq, :] *= rng.uniform(0.8, 1.2, (len(g.pq), chunk))
+            nb = len(g.f)
+            outs = np.sort(rng.choice(nb, min(n1_outages, nb), replace=False)).astype(np.int32)
+            reqs += [Request(0, k, "single", 0.0, S1), Request(0, k, "chunk", 0.0, np.ascontiguousarray(Sc)),
+                     Request(0, k, "n1", 0.0, g.Sbus.copy(), outs)]
+        self.precision_of = {}
+        times: dict = {}
+        self._start()
+        try:
+            for r in reqs:
+                for prec in ("mixed", "double"):
+                    self.precision_of[(r.topo, r.kind)] = prec
+                    for _ in range(repeats):
+                        times.setdefault((r.topo, r.kind, prec), []).append(self._time_alone(r))
+        finally:
+            self.backend.stop()
+        self.precision_of = {
+            (r.topo, r.kind): min(("mixed", "double"), key=lambda p: float(np.median(times[(r.topo, r.kind, p)])))
+            for r in reqs}
+        return dict(self.precision_of)
 
     def run(self, requests: list[Request], realtime: bool = True, keep_results: bool = True) -> list[Response]:
         """Serve a request stream (``Server.run``'s semantics). A response's ``start`` is the

@@ -134,10 +134,12 @@ class GpuStream:
         ptr = _lib.load().gbpf_stream_flags(self._h)
         self._flags = np.ctypeslib.as_array(ptr, shape=(self.capacity,))
 
-    def submit(self, solver: GpuSolver, S, V0, outages=None, reslack: bool = True):
-        """Stage one job: S (n,) or (n, T), V0 (n,); outages = (ptr (T+1,), idx) for N-1 cases.
+    def submit(self, solver: GpuSolver, S, V0, outages=None, reslack: bool = True, precision: str | None = None):
+        """Stage one job: S (n,) or (n, T), V0 (n,); outages = (ptr (T+1,), idx) for N-1 cases;
+        precision: None (the launch's), "double" or "mixed" (a launch started mixed).
         Returns (index, (V, iterations, converged, served)) -- arrays in page-locked memory that
         the kernel fills -- or None when this launch can take no more."""
+        prec = {None: 0, "double": 1, "mixed": 2}[precision]
         n = solver.n
         S = c128(S)
         V0 = c128(V0).ravel()
@@ -182,17 +184,19 @@ class GpuStream:
         J.V0 = V0.ctypes.data
         J.v0_per_col = 0
         J.V, J.iterations, J.converged = outs[0].ctypes.data, outs[1].ctypes.data, outs[2].ctypes.data
+        J.precision = prec
         keep = [S, V0]
         if outages is not None:
             J.out_ptr, J.out_idx, J.reslack = optr.ctypes.data, oidx.ctypes.data, int(bool(reslack))
             J.served = outs[3].ctypes.data
             keep += [optr, oidx]
         q = _lib.load().gbpf_stream_submit(self._h, C.byref(J))
-        if q == -2:
-            self._slab.undo(self.submitted)  # the job was not taken: its blocks are given back
+        if q < 0:  # the job was not taken: its blocks are given back
+            self._slab.undo(self.submitted)
             self._in.undo(self.submitted)
-            return None
-        _lib.check(0 if q >= 0 else -1, "stream_submit")
+            if q == -2:
+                return None
+            _lib.check(-1, "stream_submit")
         assert q == self.submitted
         self.submitted += 1
         self._keep.append(keep)

@@ -72,6 +72,39 @@ def test_stream_launch_results_are_the_same_alone_and_in_the_mix(topos):
     assert latency_summary(got)["converged_fraction"] == 1.0
 
 
+def test_stream_jobs_take_their_own_precision(topos):
+    """In a mixed-precision stream launch a job may ask for double factors (and one for mixed,
+    or the launch's): each result equals, bit for bit, that precision's own launch; a launch
+    started in double refuses a mixed job."""
+    import time
+
+    from p3s_gb300.solver import GpuSolver
+    from p3s_gb300.stream import GpuStream
+
+    tp = topos[2]
+    pm = GpuSolver.params(precision="mixed", shared_start=False)
+    pd = GpuSolver.params(precision="double", shared_start=False)
+    S = tp.grid.Sbus
+    # (before the launch: while a stream launch runs it holds the SMs, and another launch waits)
+    ref = {"mixed": tp.solver.solve_batch(S[:, None], tp.V_warm, pm),
+           "double": tp.solver.solve_batch(S[:, None], tp.V_warm, pd)}
+    st = GpuStream(capacity=8, arena_bytes=256 << 20, result_bytes=64 << 20)
+    st.start([tp.solver], pm, idle_seconds=10.0)
+    jobs = [(st.submit(tp.solver, S, tp.V_warm, precision=pr), want)
+            for pr, want in ((None, "mixed"), ("double", "double"), ("mixed", "mixed"))]
+    t = time.perf_counter()
+    while not all(st.flags()[j[0]] for j, _ in jobs) and time.perf_counter() - t < 20.0:
+        time.sleep(0.001)
+    assert all(st.done(j[0]) for j, _ in jobs)
+    for (_, (V, it, cv, _)), want in jobs:
+        assert np.array_equal(V, ref[want]["V"]) and np.array_equal(it, ref[want]["iterations"]) and cv.all()
+    assert st.stop() == 0
+    st.start([tp.solver], pd, idle_seconds=10.0)
+    with pytest.raises(RuntimeError, match="precision"):
+        st.submit(tp.solver, S, tp.V_warm, precision="mixed")
+    assert st.stop() == 0
+
+
 def test_stream_launch_returns_at_its_idle_limit_and_starts_again(topos):
     """A launch that gets no job for its idle window returns by itself (status 1 at stop) --
     its polling is bounded; a full ring refuses the next job until the launch is restarted."""

@@ -155,8 +155,9 @@ class _FakeStream:
         self.running = True
         self.launch_polls = 0
 
-    def submit(self, solver, S, V0, outages=None, reslack=True):
+    def submit(self, solver, S, V0, outages=None, reslack=True, precision=None):
         assert self.running
+        self.precisions = getattr(self, "precisions", []) + [precision]
         if len(self.jobs) == self.capacity:
             return None
         T = S.shape[1] if S.ndim == 2 else 1
@@ -203,6 +204,7 @@ def _stream_server(topos, backend):
 
     s = object.__new__(StreamServer)
     s.topos, s.params, s.idle_seconds, s.backend, s.launches = topos, None, 1.0, backend, 0
+    s.precision_of = {}
     return s
 
 
@@ -237,6 +239,34 @@ def test_stream_server_resubmits_the_jobs_a_launch_left_at_its_idle_limit():
     assert [r.launch for r in out] == [1, 1, 1]  # none finished in the first launch
     for r, resp in zip(reqs, out):
         assert np.array_equal(resp.V[:, 0], r.S) and resp.converged.all()
+
+
+def test_stream_server_tunes_the_precision_per_topology_and_kind():
+    """``tune`` times each request kind of each topology alone in the running launch in both
+    precisions and keeps the faster; later requests are submitted with that precision."""
+
+    class Timed(_FakeStream):
+        def submit(self, solver, S, V0, outages=None, reslack=True, precision=None):
+            sub = super().submit(solver, S, V0, outages, reslack, precision)
+            kind = "n1" if outages is not None else ("chunk" if S.ndim == 2 else "single")
+            slow = "mixed" if kind == "n1" else "double"  # this stand-in's slower precision per kind
+            if sub is not None and precision == slow:
+                self.jobs[-1] += 300  # its flag comes 300 polls later
+            return sub
+
+    topos = [SimpleNamespace(solver=None, V_warm=np.ones(118, complex), grid=grid_118(), n=118)]
+    fake = Timed(capacity=64)
+    srv = _stream_server(topos, fake)
+    srv.params = SimpleNamespace(precision=1)  # a mixed-precision launch
+    got = srv.tune(chunk=4, n1_outages=3, repeats=2)
+    assert got == {(0, "single"): "mixed", (0, "chunk"): "mixed", (0, "n1"): "double"}
+    fake.precisions = []
+    reqs = [Request(0, 0, "single", 0.0, np.ones(118, complex)),
+            Request(1, 0, "n1", 0.0, np.ones(118, complex), np.array([1, 2], np.int32))]
+    srv.run(reqs, realtime=False)
+    assert fake.precisions == ["mixed", "double"]
+    srv.params = SimpleNamespace(precision=0)  # a double launch: nothing to choose
+    assert srv.tune() == {}
 
 
 def test_stream_server_reports_a_stopped_launch_with_jobs_unfinished():
