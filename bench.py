@@ -111,6 +111,10 @@ def shared_start(g):
     return np.ascontiguousarray(r["V"][:, 0])
 
 
+# autotune candidates of the headline launch: the rule's shape and its neighbours
+TUNE_SHAPES = ((512, 32), (512, 16), (1024, 32), (1024, 16))
+
+
 def n_lanes(T, cases_per_cta=32, threads_per_cta=512, nsm=None):
     """Warm-start lanes: one per case slot of the launch (SMs x resident CTAs x slots), at most
     one per hour. K = T starts every hour from the shared start (the reference's semantics)."""
@@ -300,9 +304,28 @@ def run_gpu(args, rank, world, local):
                                   dit.data_ptr(), dcv.data_ptr())
         return solver.stats
 
+    # the launch shape (threads, case slots per CTA) and the factorization schedule's chain cap
+    # of this workload, per precision, measured before the timed steps (autotune): every
+    # candidate solves the same cases to the same bits, only the time differs
+    tuned = {}
+
+    def use(prec):
+        if prec in tuned:
+            t = tuned[prec]
+            solver.set_chain_cap(t["chain_cap"])
+            solver.set_shape(K, t["threads_per_cta"], t["cases_per_cta"])
+
     out = {}
     for prec in ("mixed", "double"):
         p = GpuSolver.params(precision=prec, mixed_switch=args.mixed_switch)
+        if not args.no_tune:
+            from p3s_gb300 import autotune
+
+            choice, timings = autotune.tune(solver, K, lambda: dev_step(p), candidates=TUNE_SHAPES,
+                                            chain_caps=autotune.CHAIN_CAPS, reps=1)
+            tuned[prec] = {"threads_per_cta": choice[0], "cases_per_cta": choice[1], "chain_cap": choice[2],
+                           "kernel_ms": {f"{k[0]}x{k[1]} cap {k[2]:g}": round(v, 3) for k, v in timings.items()}}
+        use(prec)
         for _ in range(args.warmup):
             dev_step(p)
         barrier(world)
@@ -325,6 +348,7 @@ def run_gpu(args, rank, world, local):
     # the Newton kernel's time by phase: one instrumented launch per precision, outside the timed
     # steps (SM clock counters at the phase barriers, summed over the CTAs)
     for prec in ("mixed", "double"):
+        use(prec)
         dev_step(GpuSolver.params(precision=prec, mixed_switch=args.mixed_switch, phase_timers=True))
         out[prec]["phase_cycles"] = solver.stats["phase_cycles"]
 
@@ -357,7 +381,9 @@ def run_gpu(args, rank, world, local):
                                 "sample": f"all {T} hours in the same {K_warm} lanes (the oracle's lane replay), "
                                           f"best of 3, oracle/liboracle.so (OpenMP, {cpu_cores()} threads)"}
 
-    # accuracy of the mixed result against the oracle's mismatch on a few hours
+    # accuracy of the mixed result against the oracle's mismatch on a few hours (the mixed
+    # launch configuration from here on: the end-to-end steps below are mixed)
+    use("mixed")
     p = GpuSolver.params(precision="mixed", mixed_switch=args.mixed_switch)
     dev_step(p)
     V = dV.cpu().numpy().view(np.complex128).reshape(g.n, T)
@@ -421,7 +447,7 @@ def run_gpu(args, rank, world, local):
 
     res = dict(out=out, e2e_ms=e2e_wall, e2e_single_ms=float(np.min(single)), h2d=h2d, d2h=d2h, info=info,
                K=len(off) - 1, T=T, worst_mis=worst_mis, g=g, accuracy=accuracy, polish=p.polish, vtol=p.vtol,
-               warm=warm)
+               warm=warm, tuned=tuned)
     return res
 
 
@@ -595,6 +621,11 @@ def run_serving(args):
     return out
 
 
+def solver_chain_cap(res, prec):
+    t = res.get("tuned") or {}
+    return t[prec]["chain_cap"] if prec in t else 1.0
+
+
 def gpu_line(args, res, rank, world):
     out = res["out"]
     T = res["T"]
@@ -672,8 +703,8 @@ def gpu_line(args, res, rank, world):
         "config": headline_config(g, T, res["K"]),
         "run": {
             "precision": "mixed", "mixed_switch": args.mixed_switch, "shared_start": True,
-            "cases_per_cta": info["cases_per_cta"], "threads_per_cta": info["threads_per_cta"],
-            "grid_ctas": mixed["stats"]["grid"],
+            "cases_per_cta": mixed["stats"]["cases_per_cta"], "threads_per_cta": mixed["stats"]["threads_per_cta"],
+            "grid_ctas": mixed["stats"]["grid"], "chain_cap": solver_chain_cap(res, "mixed"),
             "iterations_mean": float(mixed["it"].mean()), "converged": bool(mixed["cv"].all()),
             "max_mismatch_pu_sampled": res["worst_mis"],
             "polish": res["polish"], "vtol": res["vtol"], "jinv_norm_est": info["jinv_norm"],
@@ -682,6 +713,7 @@ def gpu_line(args, res, rank, world):
         },
         "fp64": fp64,
         "warm_lanes": res["warm"],
+        "autotune": res["tuned"] or None,
         "accuracy": res["accuracy"],
         "n1_sweep": res.get("n1"),
         "multigrid": res.get("multigrid"),
@@ -789,6 +821,7 @@ def main():
     ap.add_argument("--no-n1", action="store_true", help="skip the N-1 sweep block")
     ap.add_argument("--no-multigrid", action="store_true", help="skip the uneven multi-grid block")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving block")
+    ap.add_argument("--no-tune", action="store_true", help="keep the solver's shape rule (no autotune)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="length of each serving stream")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup

@@ -127,6 +127,13 @@ int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cas
  * no later launch builds one on its critical path (a serving loop's warm-up). No reference
  * counterpart. */
 int gbpf_prepare_shapes(gbpf_solver* s, int max_cases_per_cta);
+/* Factorization schedule knob (no reference counterpart; the reference deals each level's
+ * tasks to a fixed number of lists, lean_lu_plan.py:172-190): within a level, a pivot's chain
+ * of diagonal and L-column tasks heavier than chain_cap x the level's mean work per worker is
+ * cut into segments on different workers, each later segment recomputing the diagonal's
+ * inverse. 1.0 is the default; 0 never cuts. Applies to the CTA shapes used from now on
+ * (shapes built with other caps stay cached); results do not change, only the speed. */
+int gbpf_set_chain_cap(gbpf_solver* s, double chain_cap);
 
 /* The solver's current Ybus values (nnz complex), e.g. after gbpf_update_Y_from_branches. */
 int gbpf_get_Y(gbpf_solver* s, double* Yx);
@@ -213,8 +220,9 @@ int gbpf_selftest_conversions(const double* in, int n, float* d2f, double* f2d, 
 /* Self-test of the kernels' own double-precision numerics (no reference counterpart): per
  * element, recip = the Newton-refined reciprocal (x > 0, else 0), s_small / c_small = the
  * small-angle series sine / cosine (|x| < 1/4, else CUDA's), s_ref / c_ref = CUDA's sincos;
- * with phasor (2 doubles, or NULL), rot (n x 2) = the phasor rotated by x as the voltage update
- * rotates a bus phasor (|x| < 1/4, else 0). */
+ * with phasor (2 doubles, or NULL), rot (n x 4) = the phasor rotated by x as the voltage update
+ * rotates a bus phasor, then as it does after a float step at a PQ bus (the increment formed
+ * in float) (|x| < 1/4, else 0). */
 int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, double* c_small, double* s_ref,
                        double* c_ref, const double* phasor, double* rot);
 
@@ -422,7 +430,7 @@ int gbpf_branch_flows_device(int nbr, int L, const int32_t* f, const int32_t* t,
  * (lean_lu_plan.py:324-360) plays this role for its own plan. */
 int gbpf_plan_selftest(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz, const int32_t* pv,
                        int npv, const int32_t* pq, int npq, int workers, const double* Vm, const double* Va,
-                       const double* S, double* dx, int32_t* shape, char* msg, int msglen);
+                       const double* S, double* dx, int32_t* shape, char* msg, int msglen, double chain_cap);
 
 #ifdef __cplusplus
 }

@@ -124,6 +124,7 @@ gbpf::ScratchOffsets gbpf::scratch_offsets(int n, int nv, int nblk, int G, bool 
 // and the factorization schedule dealt to its NT / G workers (built on first use).
 struct Shape {
     int NT = 0, G = 0, lg = 0, occ = 1;
+    double chain_cap = 1.0;  // the schedule's chain segment cap (make_schedule)
     DBuf dtaskA, dptrA, dtaskC, dptrC, dheadA, dheadC, dtaskF, dheadF, dptrF;
     gbpf::DevPlan dp{};
     ~Shape() {
@@ -164,7 +165,8 @@ struct gbpf_solver {
     cudaEvent_t e0 = nullptr, e1 = nullptr, c0 = nullptr, c1 = nullptr;
     int fixed_NT = 0, fixed_G = 0;               // CTA shape requested at creation (0: by batch size)
     int table_NT[N_SIZE_CLASSES] = {}, table_G[N_SIZE_CLASSES] = {};  // shapes set per size class
-    std::vector<std::unique_ptr<Shape>> shapes;
+    std::vector<std::unique_ptr<Shape>> shapes;  // every shape built, kept for the solver's lifetime
+    double chain_cap = 1.0;  // schedule of the shapes built from now on (gbpf_set_chain_cap)
     std::mutex shapes_mu;  // launches of several groups on this topology may look up shapes at once
     std::vector<std::unique_ptr<ExecSlot>> slots;  // asynchronous calls (gbpf_solve_lanes_async)
     // topology on the device
@@ -332,20 +334,21 @@ void choose_shape(const gbpf_solver* s, long long units, int* NT, int* G) {
 int get_shape(gbpf_solver* s, int NT, int G, Shape** out) {
     std::lock_guard<std::mutex> lock(s->shapes_mu);
     for (auto& sh : s->shapes)
-        if (sh->NT == NT && sh->G == G) {
+        if (sh->NT == NT && sh->G == G && sh->chain_cap == s->chain_cap) {
             *out = sh.get();
             return 0;
         }
     std::unique_ptr<Shape> sh(new Shape);
     sh->NT = NT;
     sh->G = G;
+    sh->chain_cap = s->chain_cap;
     sh->lg = ilog2(G);
     int occ = 1;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbpf::newton_kernel_ptr(NT), NT, 0));
     sh->occ = std::max(1, occ);
     const gbpf::Plan& p = s->plan;
     gbpf::Schedule sc;
-    gbpf::make_schedule(p, NT / G, sc);
+    gbpf::make_schedule(p, NT / G, sc, s->chain_cap);
     // DIAG tasks carry the "two real pivots" flag (PQ row) in bit 5 of their code
     for (size_t t = 0; t < sc.taskA.size() / 4; ++t) {
         if ((sc.taskA[4 * t + 1] & 3) == gbpf::TK_DIAG) {
@@ -1054,6 +1057,14 @@ int gbpf_set_shape(gbpf_solver* s, long long units, int threads_per_cta, int cas
     return 0;
 }
 
+int gbpf_set_chain_cap(gbpf_solver* s, double chain_cap) {
+    if (!s) return fail("null solver");
+    if (!(chain_cap >= 0.0) || !std::isfinite(chain_cap)) return fail("set_chain_cap: chain_cap must be finite and >= 0");
+    std::lock_guard<std::mutex> lock(s->shapes_mu);
+    s->chain_cap = chain_cap;  // shapes of other caps stay built: launches may still hold them
+    return 0;
+}
+
 int gbpf_get_mismatch(gbpf_solver* s, double* out, long long n) {
     if (!s || !out) return fail("get_mismatch: null argument");
     if (s->mis_n <= 0) return fail("get_mismatch: no synchronous solve recorded its cases' mismatch");
@@ -1482,7 +1493,7 @@ int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, 
     if (n <= 0) return 0;
     DBuf a, b, c;
     CK(a.ensure((size_t)n * 8));
-    CK(b.ensure((size_t)n * 8 * 7));
+    CK(b.ensure((size_t)n * 8 * 9));
     CK(c.ensure(16));
     double* o = b.as<double>();
     CK(cudaMemcpy(a.p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
@@ -1492,7 +1503,7 @@ int gbpf_selftest_math(const double* in, int n, double* recip, double* s_small, 
     CK(cudaDeviceSynchronize());
     double* outs[5] = {recip, s_small, c_small, s_ref, c_ref};
     for (int k = 0; k < 5; ++k) CK(cudaMemcpy(outs[k], o + k * (size_t)n, (size_t)n * 8, cudaMemcpyDeviceToHost));
-    if (phasor && rot) CK(cudaMemcpy(rot, o + 5 * (size_t)n, (size_t)n * 16, cudaMemcpyDeviceToHost));
+    if (phasor && rot) CK(cudaMemcpy(rot, o + 5 * (size_t)n, (size_t)n * 32, cudaMemcpyDeviceToHost));
     a.release();
     b.release();
     c.release();

@@ -132,6 +132,25 @@ __device__ __forceinline__ void sincos_small(double d, unsigned ahi, double* s, 
     *c = fma(pc, z, 1.0);
 }
 
+// Rotation of a unit phasor (c, s) by a small angle d (|d| < 1/4) whose increment
+// (c + js)(cos d - 1 + j sin d) is formed in float -- sin d - d and cos d - 1 from their
+// Maclaurin series in d^2 (Horner; the first term left out is below 2^-30 relative) -- and
+// added to the double phasor: within ~2^-21 |d| of the exact rotation, against ~1e-16 for
+// sincos_small. For the mixed path's steps solved with float factors at PQ buses: such a
+// step is itself off by ~cond(J) 2^-24 relative, and the Newton steps that follow correct
+// both the angle and the magnitude of a PQ bus (a PV bus's magnitude is never corrected, so
+// PV buses keep the double rotation).
+__device__ __forceinline__ void rotate_f32(double c, double s, double d, double* cs, double* sn) {
+    const float df = d2f_fast(d);
+    const float z = df * df;
+    const float sm = df * z * fmaf(fmaf(z, -1.f / 5040.f, 1.f / 120.f), z, -1.f / 6.f);               // sin d - d
+    const float cm = z * fmaf(fmaf(fmaf(z, 1.f / 40320.f, -1.f / 720.f), z, 1.f / 24.f), z, -0.5f);  // cos d - 1
+    const float c32 = d2f_trunc(c), s32 = d2f_trunc(s);
+    const float sd = df + sm;
+    *cs = c + f2d_fast(fmaf(c32, cm, -s32 * sd));
+    *sn = s + f2d_fast(fmaf(s32, cm, c32 * sd));
+}
+
 // --------------------------------------------------------------------------------------
 // Evaluation of one bus row for one slot, rectangular state e + jf = V.
 //   I_i = sum_j Y_ij V_j                      (4 double FMAs per entry)
@@ -1136,7 +1155,9 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     const double vm = !pq ? vc.x : (active ? vc.x + dvm : fma(alpha, dvm, vc.x));
                     double cs, sn;
                     const unsigned ahi = (unsigned)__double2hiint(d) & 0x7fffffffu;
-                    if (ahi < 0x3FD00000u) {  // |d| < 1/4: rotate the committed phasor by d
+                    if (ahi < 0x3FD00000u && ystep32 && pq) {  // a float step at a PQ bus
+                        rotate_f32(vc.z, vc.w, d, &cs, &sn);
+                    } else if (ahi < 0x3FD00000u) {  // |d| < 1/4: rotate the committed phasor by d
                         double sd, cd;
                         sincos_small(d, ahi, &sd, &cd);
                         cs = fma(vc.z, cd, -vc.w * sd);
@@ -1389,15 +1410,18 @@ __global__ void math_kernel(const double* in, int n, double* recip, double* s_sm
         const double x = in[i];
         if (phasor) {  // the phasor (phasor[0], phasor[1]) rotated by x as the voltage update does, |x| < 1/4
             const unsigned ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
-            double rc = 0.0, rs = 0.0;
+            double rc = 0.0, rs = 0.0, fc = 0.0, fs = 0.0;
             if (ah < 0x3FD00000u) {
                 double sd, cd;
                 sincos_small(x, ah, &sd, &cd);
                 rc = fma(phasor[0], cd, -phasor[1] * sd);
                 rs = fma(phasor[1], cd, phasor[0] * sd);
+                rotate_f32(phasor[0], phasor[1], x, &fc, &fs);  // a float step's rotation at a PQ bus
             }
-            rot[2 * i] = rc;
-            rot[2 * i + 1] = rs;
+            rot[4 * i] = rc;
+            rot[4 * i + 1] = rs;
+            rot[4 * i + 2] = fc;
+            rot[4 * i + 3] = fs;
         }
         recip[i] = x > 0.0 ? recip_nr(x) : 0.0;
         double sr, cr;

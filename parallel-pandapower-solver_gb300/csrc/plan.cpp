@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <queue>
 #include <set>
 #include <utility>
@@ -120,7 +121,7 @@ std::vector<int> rcm_order(int n, const int* Yp, const int* Yj) {
 // TASK_NOSTORE (it recomputes the inverse from the Jacobian's diagonal, which the pass
 // leaves in place). Units are dealt longest-first onto the least-loaded worker.
 void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& out, std::vector<int>& ptr,
-            std::vector<int>* level_work, bool four, const std::vector<int>* key = nullptr) {
+            std::vector<int>* level_work, bool four, const std::vector<int>* key = nullptr, double chain_cap = 1.0) {
     std::vector<std::vector<int>> by_level(nlev);
     for (int i = 0; i < (int)tasks.size(); ++i)
         if (tasks[i].head) by_level[tasks[i].level].push_back(i);
@@ -143,7 +144,10 @@ void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& o
         long long total = 0;
         for (int id : ids)
             for (int q = id; q >= 0; q = tasks[q].next) total += tasks[q].w;
-        const long long cap = std::max<long long>(1, (total + W - 1) / W);
+        // a chain heavier than chain_cap x the level's mean work per worker is cut into
+        // segments (0: never cut)
+        const long long cap = chain_cap > 0.0 ? std::max<long long>(1, (long long)std::ceil(chain_cap * (double)total / W))
+                                              : std::numeric_limits<long long>::max();
         units.clear();
         wts.clear();
         for (int id : ids) {
@@ -199,7 +203,7 @@ void layout(const std::vector<Task>& tasks, int nlev, int W, std::vector<int>& o
 }  // namespace
 
 std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, const int* pv, int npv,
-                       const int* pq, int npq, int workers) {
+                       const int* pq, int npq, int workers, double chain_cap) {
     p = Plan();
     p.n = n;
     p.nnzY = nnz;
@@ -420,7 +424,7 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
     p.tasksA = std::move(A);
     p.tasksC = std::move(C);
     Schedule sc;
-    make_schedule(p, W, sc);
+    make_schedule(p, W, sc, chain_cap);
     p.taskA = std::move(sc.taskA);
     p.ptrA = std::move(sc.ptrA);
     p.taskC = std::move(sc.taskC);
@@ -429,7 +433,7 @@ std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, co
     return std::string();
 }
 
-void make_schedule(const Plan& p, int workers, Schedule& out) {
+void make_schedule(const Plan& p, int workers, Schedule& out, double chain_cap) {
     const int W = out.W = std::max(1, workers);
     out.level_work.assign(std::max(p.nlev, p.nblev), 0);
     // factor-level key: the task's destination block (a forward row: its diagonal block)
@@ -438,10 +442,10 @@ void make_schedule(const Plan& p, int workers, Schedule& out) {
         const Task& t = p.tasksA[i];
         keyA[i] = (t.code & 3) == TK_FWD ? p.base[t.dst] : t.dst;
     }
-    layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true, &keyA);
+    layout(p.tasksA, p.nlev, W, out.taskA, out.ptrA, &out.level_work, true, &keyA, chain_cap);
     std::vector<int> keyC(p.tasksC.size());
     for (size_t i = 0; i < p.tasksC.size(); ++i) keyC[i] = p.tasksC[i].dst;
-    layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true, &keyC);
+    layout(p.tasksC, p.nblev, W, out.taskC, out.ptrC, nullptr, true, &keyC, chain_cap);
 }
 
 // ----------------------------------------------------------------------------- host replica
@@ -713,9 +717,10 @@ std::string schedule_selftest(const Plan& p, double* blk, const double* R, doubl
 extern "C" int gbpf_plan_selftest(int n, const int32_t* Yp, const int32_t* Yj, const double* Yx, int nnz,
                                   const int32_t* pv, int npv, const int32_t* pq, int npq, int workers,
                                   const double* Vm, const double* Va, const double* S, double* dx, int32_t* shape,
-                                  char* msg, int msglen) {
+                                  char* msg, int msglen, double chain_cap) {
     gbpf::Plan p;
-    std::string e = gbpf::build_plan(p, n, Yp, Yj, nnz, pv, npv, pq, npq, workers);
+    std::string e = chain_cap >= 0.0 ? gbpf::build_plan(p, n, Yp, Yj, nnz, pv, npv, pq, npq, workers, chain_cap)
+                                     : std::string("chain_cap must be >= 0");
     if (e.empty()) {
         std::vector<double> blk(4 * ((size_t)p.nblk + p.nv)), R(2 * (size_t)std::max(p.nv, 1)),
             y(2 * (size_t)std::max(p.nv, 1));

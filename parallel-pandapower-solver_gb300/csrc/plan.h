@@ -95,10 +95,13 @@ struct Plan {
 
 // Build everything topology-only. Returns an empty string on success, else the error.
 std::string build_plan(Plan& p, int n, const int* Yp, const int* Yj, int nnz, const int* pv, int npv,
-                       const int* pq, int npq, int workers);
+                       const int* pq, int npq, int workers, double chain_cap = 1.0);
 
-// Deal the plan's tasks to `workers` workers (longest first onto the least-loaded one).
-void make_schedule(const Plan& p, int workers, Schedule& out);
+// Deal the plan's tasks to `workers` workers (longest first onto the least-loaded one); a
+// level's diagonal-and-L chain heavier than chain_cap x the level's mean work per worker is
+// cut into segments on different workers, each later one recomputing the diagonal inverse
+// (0: chains are never cut).
+void make_schedule(const Plan& p, int workers, Schedule& out, double chain_cap = 1.0);
 
 // Host replica of the device algorithm (double precision): Jacobian blocks at (Vm, Va)
 // written to `blocks` (nblk*4, zero where not in the Jacobian) and residual R (nv*2).

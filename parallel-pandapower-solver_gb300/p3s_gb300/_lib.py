@@ -140,7 +140,8 @@ SIGNATURES = {
     "gbpf_host_alloc": (_vp, [C.c_size_t]),
     "gbpf_host_free": (None, [_vp]),
     "gbpf_plan_selftest": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int, _dp, _dp,
-                                     _dp, _dp, _ip, C.c_char_p, C.c_int]),
+                                     _dp, _dp, _ip, C.c_char_p, C.c_int, C.c_double]),
+    "gbpf_set_chain_cap": (C.c_int, [_vp, C.c_double]),
     "gbpf_islands": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _bp, C.c_int, _ip, _ip, _bp, _dp, C.c_int, _ip, _bp,
                                _ip, _ip]),
     "gbpf_group_create": (_vp, []),

@@ -1,12 +1,15 @@
-"""CTA-shape autotuner: time candidate shapes on a caller's batch and pin the fastest.
+"""Autotuner of the Newton kernel's launch: CTA shape and factorization schedule.
 
-The solver picks a CTA shape (threads per CTA, case slots per CTA) from the batch size by a
-rule measured on GB300 (``GpuSolver.shape``). For a grid or batch size the rule was not
-measured on, ``tune_lanes`` / ``tune_batch`` time every candidate shape on the real inputs
-and pin the fastest for that batch-size class (``GpuSolver.set_shape``). Every shape runs
-the same arithmetic per case, so tuning changes only the speed, never a result.
+The solver picks a CTA shape (threads per CTA, case slots per CTA -- which also fixes the
+workers each case's factorization is dealt to) from the batch size by a rule measured on
+GB300 (``GpuSolver.shape``), and deals each elimination level's tasks with chains cut at
+``chain_cap`` x the level's mean work per worker (``GpuSolver.set_chain_cap``). ``tune``
+times every candidate (shape, chain cap) on the caller's real launch and pins the fastest:
+the shape for that batch-size class, the chain cap for the solver. Every candidate runs the
+same arithmetic per case, so tuning changes only the speed, never a result.
 No reference counterpart: the reference's lean LU kernel takes a fixed warps-per-block
-``slots`` argument (p3s/cuda/nr_polar_solver.py:285-300).
+``slots`` argument and deals each level to that many lists (p3s/cuda/nr_polar_solver.py:285-300,
+p3s/cuda/lean_lu_plan.py:172-190).
 """
 
 from __future__ import annotations
@@ -20,19 +23,33 @@ CANDIDATES = ((1024, 1), (1024, 2), (1024, 4), (512, 2), (512, 4), (512, 8), (51
               (256, 8), (256, 16))
 
 
-def _tune(solver: GpuSolver, units: int, run, candidates, reps: int):
+CHAIN_CAPS = (1.0, 0.5, 2.0, 0.0)
+
+
+def tune(solver: GpuSolver, units: int, run, candidates=CANDIDATES, chain_caps=(1.0,), reps: int = 2):
+    """Time `run()` (one launch of `units` work items on `solver`) for every (threads, slots)
+    in `candidates` and every chain cap in `chain_caps`; pin the fastest and return it as
+    (threads, slots, chain_cap) with the best kernel milliseconds of every candidate."""
     timings = {}
-    for nt, g in candidates:
-        solver.set_shape(units, nt, g)
-        best = None
-        for _ in range(reps + 1):  # the first run builds the shape's schedule and scratch
-            run()
-            t = solver.stats["kernel_ms"]
-            best = t if best is None else min(best, t)
-        timings[(nt, g)] = best
+    for cap in chain_caps:
+        solver.set_chain_cap(cap)
+        for nt, g in candidates:
+            solver.set_shape(units, nt, g)
+            best = None
+            for _ in range(reps + 1):  # the first run builds the shape's schedule and scratch
+                run()
+                t = solver.stats["kernel_ms"]
+                best = t if best is None else min(best, t)
+            timings[(nt, g, cap)] = best
     choice = min(timings, key=timings.get)
-    solver.set_shape(units, *choice)
+    solver.set_chain_cap(choice[2])
+    solver.set_shape(units, choice[0], choice[1])
     return choice, timings
+
+
+def _tune(solver: GpuSolver, units: int, run, candidates, reps: int):
+    choice, timings = tune(solver, units, run, candidates, (getattr(solver, "chain_cap", 1.0),), reps)
+    return choice[:2], {k[:2]: v for k, v in timings.items()}
 
 
 def tune_lanes(solver: GpuSolver, S, V0, offsets, params, candidates=CANDIDATES, reps: int = 2):

@@ -138,6 +138,7 @@ class GpuSolver:
             raise RuntimeError(_lib.last_error())
         self._h = h
         self._pattern = None
+        self.chain_cap = 1.0
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -184,6 +185,12 @@ class GpuSolver:
         """Pin the CTA shape for batches of `units`' size class (0, 0 restores the rule)."""
         _lib.check(_lib.load().gbpf_set_shape(self._h, int(units), int(threads_per_cta), int(cases_per_cta)),
                    "gbpf_set_shape")
+
+    def set_chain_cap(self, chain_cap: float):
+        """Schedule knob of the factorization (gbpf_set_chain_cap): a level's pivot chain heavier
+        than chain_cap x the level's mean work per worker is split over workers (0: never)."""
+        _lib.check(_lib.load().gbpf_set_chain_cap(self._h, float(chain_cap)), "gbpf_set_chain_cap")
+        self.chain_cap = float(chain_cap)
 
     def posmap(self) -> np.ndarray:
         out = np.empty(self.nnz, dtype=np.int32)

@@ -341,7 +341,7 @@ def test_own_double_numerics_within_an_ulp():
     inp = np.ascontiguousarray(np.concatenate([x, d]))
     outs = [np.empty(len(inp)) for _ in range(5)]
     ph = np.array([np.cos(0.7), np.sin(0.7)])
-    rot = np.empty((len(inp), 2))
+    rot = np.empty((len(inp), 4))
     rc = _lib.load().gbpf_selftest_math(_lib.d(inp), len(inp), *[_lib.d(o) for o in outs], _lib.d(ph), _lib.d(rot))
     assert rc == 0, _lib.last_error()
     recip, s_small, c_small, s_ref, c_ref = outs
@@ -363,6 +363,11 @@ def test_own_double_numerics_within_an_ulp():
     want_s = (s0 * np.cos(dl) + c0 * np.sin(dl)).astype(np.float64)
     assert (np.abs(rot[nx:, 0] - want_c) <= 2 * np.spacing(np.abs(want_c))).all()
     assert (np.abs(rot[nx:, 1] - want_s) <= 2 * np.spacing(np.abs(want_s))).all()
+    # after a float step at a PQ bus the increment is formed in float from truncated float
+    # copies (each within 2^-23): within 2^-20 |d| (plus the double addition's rounding) of the
+    # exact rotation
+    bound = 2.0 ** -20 * np.abs(dd) + 2 * np.spacing(1.0)
+    assert (np.abs(rot[nx:, 2] - want_c) <= bound).all() and (np.abs(rot[nx:, 3] - want_s) <= bound).all()
 
 
 def test_n1_sweep_of_the_2000_bus_grid(grid2000):
@@ -411,9 +416,10 @@ def test_n1_sweep_of_the_2000_bus_grid(grid2000):
 
 
 def test_results_do_not_depend_on_the_cta_shape(grid2000):
-    """Every CTA shape runs the same arithmetic per case: the batch-size rule, a pinned
-    shape and the autotuner change only the speed, never a bit of the result."""
-    from p3s_gb300.autotune import tune_lanes
+    """Every CTA shape and every factorization schedule (chain caps: chains cut finer,
+    coarser or never) runs the same arithmetic per case: the batch-size rule, a pinned shape,
+    a chain cap and the autotuner change only the speed, never a bit of the result."""
+    from p3s_gb300.autotune import tune, tune_lanes
     from p3s_gb300.solver import GpuSolver
 
     g = grid2000
@@ -431,9 +437,19 @@ def test_results_do_not_depend_on_the_cta_shape(grid2000):
             assert s.stats["threads_per_cta"] == nt and s.stats["cases_per_cta"] == slots
             assert np.array_equal(r["V"], base["V"]) and np.array_equal(r["iterations"], base["iterations"])
         s.set_shape(96, 0, 0)
+        for cap in (0.0, 0.25, 2.0):
+            s.set_chain_cap(cap)
+            r = s.solve_lanes(S, g.V0, off, p)
+            assert np.array_equal(r["V"], base["V"]) and np.array_equal(r["iterations"], base["iterations"])
+        s.set_chain_cap(1.0)
     choice, timings = tune_lanes(s, S, g.V0, off, GpuSolver.params(precision="mixed"),
                                  candidates=((1024, 2), (512, 4)), reps=1)
     assert s.shape(96) == choice and set(timings) == {(1024, 2), (512, 4)}
+    p = GpuSolver.params(precision="mixed")
+    choice, timings = tune(s, 96, lambda: s.solve_lanes(S, g.V0, off, p), candidates=((512, 4),),
+                           chain_caps=(1.0, 0.0), reps=1)
+    assert set(timings) == {(512, 4, 1.0), (512, 4, 0.0)} and s.chain_cap == choice[2]
+    assert s.shape(96) == choice[:2]
 
 
 def test_uneven_grids_in_one_launch_match_their_own_solves():

@@ -41,7 +41,7 @@ def test_timeseries_and_lanes(grid118):
     assert off[0] == 0 and off[-1] == 8760 and len(off) == 1217 and set(np.diff(off)) <= {7, 8}
 
 
-def _selftest(g, workers, seed=1):
+def _selftest(g, workers, seed=1, chain_cap=1.0):
     L = _lib.load()
     rng = np.random.default_rng(seed)
     Vm = np.abs(g.V0) * (1 + 0.02 * rng.standard_normal(g.n))
@@ -53,7 +53,7 @@ def _selftest(g, workers, seed=1):
     S = np.ascontiguousarray(g.Sbus)
     rc = L.gbpf_plan_selftest(g.n, _lib.i32(g.Yp), _lib.i32(g.Yj), _lib.cview(Yx), g.nnz, _lib.i32(g.pv), len(g.pv),
                               _lib.i32(g.pq), len(g.pq), workers, _lib.d(Vm), _lib.d(Va), _lib.cview(S), _lib.d(dx),
-                              _lib.i32(shape), msg, 256)
+                              _lib.i32(shape), msg, 256, float(chain_cap))
     assert rc == 0, msg.value
     d = cpu.Solver(g.Yp, g.Yj, g.Yx, g.pv, g.pq).debug_J_at(g.Sbus, Vm * np.exp(1j * Va))
     J = sp.csc_matrix((d["Jx"], d["Ji"], d["Jp"]), shape=(d["m"], d["m"]))
@@ -71,6 +71,15 @@ def test_block_schedule_solves_the_power_flow_jacobian(workers):
     solves what scipy solves (the reference's test_plan_solves_power_flow_jacobian)."""
     for g in (grid_118(), grid_2000()):
         err, shape = _selftest(g, workers)
+        assert err < 1e-9, err
+
+
+@pytest.mark.parametrize("cap", [0.0, 0.25, 0.5, 2.0])
+def test_block_schedule_with_other_chain_caps(cap):
+    """Schedules with the chain segments cut finer, coarser or not at all (the tuner's knob)
+    keep every dependency (the per-level race check) and solve the same system."""
+    for g in (grid_118(), grid_2000()):
+        err, _ = _selftest(g, 64, chain_cap=cap)
         assert err < 1e-9, err
 
 
