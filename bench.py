@@ -463,6 +463,21 @@ def run_n1(args):
     solver = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     out = {"cases": g.n_branch + 1}
     for prec in ("mixed", "double"):
+        cap_ms = {}
+        if not args.no_tune:
+            # the factorization schedule's chain cap of this launch, measured (autotune.CHAIN_CAPS):
+            # the same results for every cap, only the time differs
+            from p3s_gb300 import autotune
+
+            for cap in autotune.CHAIN_CAPS:
+                solver._s.set_chain_cap(cap)
+                t = []
+                for _ in range(2):
+                    contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
+                                                    return_islands=False)
+                    t.append(solver.last_stats["kernel_ms"])
+                cap_ms[cap] = min(t)
+            solver._s.set_chain_cap(min(cap_ms, key=cap_ms.get))
         for _ in range(args.warmup):
             r = contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
                                                  return_islands=False)
@@ -479,6 +494,8 @@ def run_n1(args):
             "e2e_solves_per_s": round(L / np.mean(wall), 1), "e2e_ms": round(float(np.mean(wall)) * 1e3, 1),
             "iterations_mean": float(r.iterations.mean()), "converged": int(r.converged.sum()),
             "islanded_cases": int((r.served.sum(axis=0) < g.n).sum()),
+            "chain_cap": solver._s.chain_cap,
+            "chain_cap_ms": {f"{k:g}": round(v, 3) for k, v in cap_ms.items()} or None,
         }
     return out
 

@@ -23,7 +23,7 @@ CANDIDATES = ((1024, 1), (1024, 2), (1024, 4), (512, 2), (512, 4), (512, 8), (51
               (256, 8), (256, 16))
 
 
-CHAIN_CAPS = (1.0, 0.5, 2.0, 0.0)
+CHAIN_CAPS = (1.0, 0.75, 0.5, 0.35, 0.25, 2.0, 0.0)
 
 
 def tune(solver: GpuSolver, units: int, run, candidates=CANDIDATES, chain_caps=(1.0,), reps: int = 2):
