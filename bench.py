@@ -727,6 +727,8 @@ def gpu_line(args, res, rank, world):
             "polish": res["polish"], "vtol": res["vtol"], "jinv_norm_est": info["jinv_norm"],
             "single_factorizations": int(mixed["stats"]["single_factorizations"]),
             "double_factorizations": int(mixed["stats"]["double_factorizations"]),
+            "lazy_jacobians": int(mixed["stats"].get("lazy_jacobians", 0)),
+            "jacobian_sweeps": int(mixed["stats"].get("jacobian_sweeps", 0)),
         },
         "fp64": fp64,
         "warm_lanes": res["warm"],

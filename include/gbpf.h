@@ -52,6 +52,11 @@ typedef struct gbpf_params {
                             prologue on the launch's critical path: latency-bound serving) */
     int phase_timers;    /* 1: the Newton kernel sums SM clock cycles per phase over its CTAs into
                             gbpf_stats.phase_cycles (single-topology launches; 0: off, the default) */
+    int eager_jacobian;  /* mixed, vote_rule 1: 0 (default) leaves the float Jacobian out of an
+                            evaluation after which no factorization is expected (after a chord
+                            step, or a float step from below 100 x chord_tol) and builds it later
+                            only if a step factors after all -- the same values, so the same
+                            results; 1: every evaluation builds its Jacobian */
 } gbpf_params;
 
 /* Topology / schedule facts of a solver (for stats, rooflines and tests). */
@@ -81,6 +86,10 @@ typedef struct gbpf_stats {
                                            load, factorization with forward substitution, backward
                                            substitution, voltage update, mismatch / Jacobian
                                            evaluation, decision and write-back; 0 otherwise */
+    unsigned long long lazy_jacobians;  /* mixed: evaluations that left the float Jacobian out (a
+                                           chord step or the case's end was expected next) */
+    unsigned long long jacobian_sweeps; /* of those, Jacobians built afterwards because the next
+                                           step factored after all */
 } gbpf_stats;
 
 const char* gbpf_last_error(void);

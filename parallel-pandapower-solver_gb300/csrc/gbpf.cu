@@ -582,6 +582,8 @@ int finish_launch(const LaunchRes& R, int grid, int G, int NT, const char* who, 
     st->chord_steps = host_ctl[5];
     st->first_steps = host_ctl[6];
     for (int k = 0; k < 6; ++k) st->phase_cycles[k] = host_ctl[8 + k];
+    st->lazy_jacobians = host_ctl[14];
+    st->jacobian_sweeps = host_ctl[7];
     st->grid = grid;
     st->cases_per_cta = G;
     st->threads_per_cta = NT;
@@ -641,6 +643,7 @@ void fill_common(gbpf::Batch& b, const gbpf_solver* s, const gbpf_params& p) {
     // chord steps belong to the GB300 rule's float cases only (the double path refactors every
     // step like nr_klu)
     b.chord_tol = b.mixed && b.vote_rule == 1 && p.chord_tol > 0.0 ? p.chord_tol : 0.0;
+    b.lazy_jac = b.chord_tol > 0.0 && !p.eager_jacobian;
     b.share_ok = p.shared_start != 0;
     b.timers = p.phase_timers != 0;
     b.check_v0 = p.check_v0;
@@ -917,6 +920,8 @@ int group_run(gbpf_group* g, int nj, const gbpf_job* jobs, const gbpf_params& p,
         st.macro_steps += c[4];
         st.chord_steps += c[5];
         st.first_steps += c[6];
+        st.lazy_jacobians += c[14];
+        st.jacobian_sweeps += c[7];
     }
     st.grid = grid;
     st.cases_per_cta = Gmax;

@@ -101,6 +101,7 @@ struct Batch {
     int vote_rule;           // 0: the reference's precision votes; 1: GB300 rule (see the kernel)
     double tol_polish;       // GB300 rule: float-factor cases iterate until mismatch < tol_polish
     double chord_tol;        // GB300 rule: below this mismatch a step reuses the last float factors (0: never)
+    int lazy_jac;            // GB300 rule: evaluations expected to precede no factorization skip the float Jacobian
     // shared start (every case from the same V0 on the same Ybus, no pins): the injections and
     // the factors of J(V0), computed once by start_kernel; cases starting from V0 take their
     // first step with them (null: every case evaluates and factors its own start)

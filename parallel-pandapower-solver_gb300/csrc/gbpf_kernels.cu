@@ -31,6 +31,7 @@ namespace gbpf {
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
 constexpr double CHORD_RATE = 0.1; // a chord step must cut the mismatch tenfold for another one
+constexpr double JAC_LAZY = 100.0; // a float step from below this x chord_tol skips its Jacobian
 constexpr double BIG = DBL_MAX;    // nr_klu.cpp:434 NONFINITE_NORM
 
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
@@ -784,6 +785,9 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     __shared__ int s_st[MAX_SLOTS], s_case[MAX_SLOTS], s_it[MAX_SLOTS], s_vote[MAX_SLOTS], s_trial[MAX_SLOTS];
     __shared__ int s_conv[MAX_SLOTS], s_jprec[MAX_SLOTS], s_yprec[MAX_SLOTS], s_warm[MAX_SLOTS];
     __shared__ int s_on32[MAX_SLOTS], s_on64[MAX_SLOTS], s_reeval[MAX_SLOTS];
+    // s_nojac: the slot's last evaluation left the float Jacobian out (a chord step or the
+    // case's end was expected next); a step that factors after all builds it first
+    __shared__ int s_nojac[MAX_SLOTS];
     __shared__ long long s_lcur[MAX_SLOTS], s_lend[MAX_SLOTS];
     __shared__ double s_nrm[MAX_SLOTS], s_alpha[MAX_SLOTS], s_balpha[MAX_SLOTS], s_bnrm[MAX_SLOTS];
     __shared__ unsigned long long s_res[MAX_SLOTS], s_pmin[MAX_SLOTS], s_pmax[MAX_SLOTS];
@@ -813,6 +817,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         s_nst[tid] = 0;
         s_jprec[tid] = 0;
         s_vote[tid] = 0;
+        s_nojac[tid] = 0;
     }
     __syncthreads();
 
@@ -851,6 +856,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     s_fb[s] = 0;
                     s_chord[s] = 0;
                     s_first[s] = s_share && !s_warm[s];
+                    s_nojac[s] = 0;
                     s_it[s] = 0;
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
@@ -934,12 +940,17 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             } else if (Bt.v0_shared) {
                 // shared start: the state table built once per launch (v0_table_kernel)
                 const double4_32a t0 = RING ? ldcg4(Bt.v0tab + 2 * bus) : Bt.v0tab[2 * bus];
-                const double4_32a t1 = RING ? ldcg4(Bt.v0tab + 2 * bus + 1) : Bt.v0tab[2 * bus + 1];
                 Vb0[idx] = t0;
                 if (fixed) Vb1[idx] = t0;
-                Et[idx] = make_double2(t1.x, t1.y);
-                Ei[idx] = t1.z;
-                iv32[idx] = d2f_fast(t1.z);
+                // a case starting from the shared start evaluates its start with the shared
+                // injections (no (e, f) or 1 / Vm read) and its first step rewrites them at every
+                // moving bus before they are read: only the fixed buses' (e, f) are needed
+                if (fixed || !s_first[s]) {
+                    const double4_32a t1 = RING ? ldcg4(Bt.v0tab + 2 * bus + 1) : Bt.v0tab[2 * bus + 1];
+                    Et[idx] = make_double2(t1.x, t1.y);
+                    Ei[idx] = t1.z;
+                    iv32[idx] = d2f_fast(t1.z);
+                }
             } else {
                 const double2 v0 = Bt.V0[(size_t)bus * Bt.sV0 + c];
                 if (Bt.check_v0 && (!finite_d(v0.x) || !finite_d(v0.y))) {
@@ -1016,6 +1027,23 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
         }
         const int any32 = __syncthreads_or(tid < G && s_on32[tid]);
         if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 0);
+        // a float step that factors after an evaluation that left the Jacobian out: the
+        // Jacobian at the same point first (the values that evaluation would have written)
+        const int anylazy = __syncthreads_or(tid < G && s_on32[tid] && !s_nofac[tid] && s_nojac[tid]);
+        if (anylazy) {
+            for (int idx = tid; idx < nG; idx += NT) {
+                const int s = idx & (G - 1);
+                if (!(s_on32[s] && !s_nofac[s] && s_nojac[s])) continue;
+                const int bus = idx >> lg;
+                const int row = P.row_of_bus[bus];
+                if (row < 0) continue;
+                EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, s_case[s], s_nst[s], s_stk[s], s_stv[s]};
+                eval_row<2>(ec, bus, s, row, spin[idx] != 0, P.bus_pq[bus] != 0, make_double2(0.0, 0.0),
+                            s_fb[s] ? fac32 : fac32b, R, false);
+            }
+            __syncthreads();
+            if (tid < G && s_on32[tid] && !s_nofac[tid] && s_nojac[tid]) atomicAdd(&Bt.stats[7], 1ULL);
+        }
         if (any32) {
             // chord and first steps are decided per slot (a result never depends on the other
             // cases of its CTA); the factorization is left out altogether when no float slot
@@ -1180,10 +1208,28 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 }
             }
         }
+        // The float Jacobian of this evaluation is left out where the next step should not
+        // factor: after a chord step (another chord step or the case's end follows), or after a
+        // float step from below JAC_LAZY x chord_tol (it lands below chord_tol). The lanes of a
+        // warp are the case slots of one bus, so the choice is the CTA's: only when every
+        // float full step of the CTA qualifies (mixed choices would run both paths per warp).
+        int qual = 1;
         if (tid < G) {
             const int st = s_st[tid];
             if (st == SL_FRESH || st == SL_ACTIVE || st == SL_NEEDJ) s_jprec[tid] = (Bt.mixed && s_vote[tid] == 1) ? 1 : 0;
+            if (st == SL_ACTIVE && s_jprec[tid])
+                qual = Bt.lazy_jac && (s_chord[tid] || s_nrm[tid] < JAC_LAZY * Bt.chord_tol);
             s_res[tid] = 0ULL;
+        }
+        const int lazy = __syncthreads_and(qual);
+        if (tid < G) {
+            const int st = s_st[tid];
+            if (st == SL_ACTIVE) {
+                s_nojac[tid] = lazy && s_jprec[tid];
+                if (s_nojac[tid]) atomicAdd(&Bt.stats[14], 1ULL);
+            } else if (st == SL_FRESH || st == SL_NEEDJ) {
+                s_nojac[tid] = 0;
+            }
         }
         __syncthreads();
         if constexpr (TIMED) phase_mark(GBPF_PH, &s_clk, 3);
@@ -1216,6 +1262,8 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;
             if (st == SL_BACKTRACK)
+                worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
+            else if (Bt.mixed && s_jprec[s] && s_nojac[s])  // the mismatch only (lazy Jacobian)
                 worst = eval_row<0>(ec, bus, s, row, pinned, pq, Ssp, fac64, R, true);
             else if (Bt.mixed && s_jprec[s])  // into the buffer the slot's last float factors are not in
                 worst = eval_row<2>(ec, bus, s, row, pinned, pq, Ssp, s_fb[s] ? fac32 : fac32b, R, true);

@@ -38,6 +38,7 @@ class Params(C.Structure):
         ("chord_tol", C.c_double),
         ("shared_start", C.c_int),
         ("phase_timers", C.c_int),
+        ("eager_jacobian", C.c_int),
     ]
 
 
@@ -75,6 +76,8 @@ class Stats(C.Structure):
         ("chord_steps", C.c_ulonglong),
         ("first_steps", C.c_ulonglong),
         ("phase_cycles", C.c_ulonglong * 6),
+        ("lazy_jacobians", C.c_ulonglong),
+        ("jacobian_sweeps", C.c_ulonglong),
     ]
 
 

@@ -98,6 +98,8 @@ class PolarNewtonSolverCUDA:
             # counters of the persistent kernel (beyond the reference's chunk-loop statistics)
             "chord_steps": int(st.get("chord_steps", 0)),
             "first_steps": int(st.get("first_steps", 0)),
+            "lazy_jacobians": int(st.get("lazy_jacobians", 0)),
+            "jacobian_sweeps": int(st.get("jacobian_sweeps", 0)),
             "jinv_norm": jinv,
             "max_mismatch": max_mis,  # over the converged cases
             "error_bound": bound,     # jinv_norm x max_mismatch

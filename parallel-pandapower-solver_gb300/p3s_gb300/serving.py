@@ -412,36 +412,40 @@ class StreamServer:
             return self.backend.submit(tp.solver, r.S, tp.V_warm, outages=outages, reslack=True, precision=prec)
         return self.backend.submit(tp.solver, r.S, tp.V_warm, precision=prec)
 
-    def _time_alone(self, r: Request) -> float:
-        """Seconds from submitting `r` alone to the running launch until its flag is set (a
-        launch that is full, or has left at its idle limit, is renewed first)."""
+    def _time_copies(self, r: Request, copies: int) -> float:
+        """Seconds from submitting `copies` copies of `r` together to the running launch until
+        the last one's flag is set (a launch that is full, or has left at its idle limit, is
+        renewed first). Several copies weigh a request's GPU work as well as its latency: a
+        large grid's request runs one case per CTA, and its copies compete for the SMs."""
         for _ in range(3):
             if self.backend.full() or not self.backend.alive():
                 self.backend.stop()
                 self._start()
             t0 = time.perf_counter()
-            sub = self._submit(r)
-            if sub is None:  # staging still held by this launch's earlier jobs: renew the launch
+            subs = [self._submit(r) for _ in range(copies)]
+            if any(sub is None for sub in subs):  # staging held by earlier jobs: renew the launch
                 self.backend.stop()
                 self._start()
                 continue
-            q = sub[0]
-            while not self.backend.flags()[q] and self.backend.alive():
+            qs = [sub[0] for sub in subs]
+            while not all(self.backend.flags()[q] for q in qs) and self.backend.alive():
                 time.sleep(2e-5)
-            if self.backend.flags()[q]:
+            if all(self.backend.flags()[q] for q in qs):
                 dt = time.perf_counter() - t0
-                self.backend.done(q)
-                self.backend.release(q)
+                for q in qs:
+                    self.backend.done(q)
+                    self.backend.release(q)
                 return dt
-            self.backend.stop()  # the launch left before starting the job: renew and submit again
+            self.backend.stop()  # the launch left before starting the jobs: renew and submit again
             self._start()
         raise RuntimeError("tune: a request did not complete in three launches")
 
-    def tune(self, chunk: int = 96, n1_outages: int = 200, repeats: int = 3, seed: int = 0) -> dict:
+    def tune(self, chunk: int = 96, n1_outages: int = 200, repeats: int = 3, seed: int = 0,
+             copies: int = 3) -> dict:
         """For a mixed-precision server: per topology and request kind (single solve, chunk of
-        `chunk` steps, sweep of `n1_outages` outages), submit a request of that kind alone to a
-        running launch in each precision, `repeats` times, and keep the precision whose median
-        completion time is shorter. Returns {(topology, kind): precision}."""
+        `chunk` steps, sweep of `n1_outages` outages), submit `copies` requests of that kind
+        together to a running launch in each precision, `repeats` times, and keep the precision
+        whose median completion time is shorter. Returns {(topology, kind): precision}."""
         if self.params.precision != 1:
             return {}
         rng = np.random.default_rng(seed)
@@ -464,7 +468,7 @@ class StreamServer:
                 for prec in ("mixed", "double"):
                     self.precision_of[(r.topo, r.kind)] = prec
                     for _ in range(repeats):
-                        times.setdefault((r.topo, r.kind, prec), []).append(self._time_alone(r))
+                        times.setdefault((r.topo, r.kind, prec), []).append(self._time_copies(r, copies))
         finally:
             self.backend.stop()
         self.precision_of = {

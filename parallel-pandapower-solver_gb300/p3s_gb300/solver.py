@@ -205,13 +205,14 @@ class GpuSolver:
     @staticmethod
     def params(max_iter=30, tol=1e-8, line_search=True, precision="double", mixed_switch=1e-3, check_v0=False,
                pivot_ratio_double=1e-3, pivot_ratio_single=1e-3, vote_rule="gb300", polish=1e-3, vtol=1e-8,
-               chord_tol=1e-8, shared_start=True, phase_timers=False):
+               chord_tol=1e-8, shared_start=True, phase_timers=False, eager_jacobian=False):
         if precision not in ("double", "mixed"):
             raise ValueError(f"precision must be 'double' or 'mixed', got {precision!r}")
         return _lib.Params(int(max_iter), float(tol), int(bool(line_search)), 1 if precision == "mixed" else 0,
                            float(mixed_switch), int(bool(check_v0)), float(pivot_ratio_double),
                            float(pivot_ratio_single), 0 if vote_rule == "reference" else 1, float(polish),
-                           float(vtol), float(chord_tol), int(bool(shared_start)), int(bool(phase_timers)))
+                           float(vtol), float(chord_tol), int(bool(shared_start)), int(bool(phase_timers)),
+                           int(bool(eager_jacobian)))
 
     def set_branches(self, f, t, stamp_pos, stamp, is_slack, gen_prio=None):
         """Branch table for outage cases: ends (m,), stamp CSR positions (m, 4) and values (m, 4)

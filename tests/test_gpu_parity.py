@@ -537,6 +537,15 @@ def test_chord_polish_steps_keep_the_solution(grid2000):
         assert (_mismatch(g, r["V"][:, :8], S[:, :8]) <= 1e-8).all()
         out[ct] = r
     assert (out[1e-8]["iterations"] <= out[0.0]["iterations"] + 1).all()
+    # the lazy Jacobian (left out where no factorization is expected, built later if one
+    # follows after all) changes nothing: bit for bit the run that builds every Jacobian
+    lazy, st_lazy = out[1e-8], None
+    r = s.solve_lanes(S, g.V0, off, GpuSolver.params(precision="mixed", chord_tol=1e-8))
+    st_lazy = s.stats
+    eager = s.solve_lanes(S, g.V0, off, GpuSolver.params(precision="mixed", chord_tol=1e-8, eager_jacobian=True))
+    assert st_lazy["lazy_jacobians"] > 0 and s.stats["lazy_jacobians"] == 0
+    assert np.array_equal(r["V"], eager["V"]) and np.array_equal(r["iterations"], eager["iterations"])
+    assert np.array_equal(lazy["V"], eager["V"])
 
 
 def test_shared_start_equals_each_case_starting_on_its_own(grid2000):

@@ -242,8 +242,9 @@ def test_stream_server_resubmits_the_jobs_a_launch_left_at_its_idle_limit():
 
 
 def test_stream_server_tunes_the_precision_per_topology_and_kind():
-    """``tune`` times each request kind of each topology alone in the running launch in both
-    precisions and keeps the faster; later requests are submitted with that precision."""
+    """``tune`` times each request kind of each topology (a few copies together) in the running
+    launch in both precisions and keeps the faster; later requests are submitted with that
+    precision."""
 
     class Timed(_FakeStream):
         def submit(self, solver, S, V0, outages=None, reslack=True, precision=None):
