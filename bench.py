@@ -113,6 +113,8 @@ def shared_start(g):
 
 # autotune candidates of the headline launch: the rule's shape and its neighbours
 TUNE_SHAPES = ((512, 32), (512, 16), (1024, 32), (1024, 16))
+# ... and of the N-1 sweep's launch (3,001 cases; 0 = the group rule: 512 x 16)
+N1_SHAPES = ((0, 0), (512, 8), (512, 32), (1024, 8), (1024, 16), (256, 4), (256, 8))
 
 
 def n_lanes(T, cases_per_cta=32, threads_per_cta=512, nsm=None):
@@ -463,29 +465,42 @@ def run_n1(args):
     solver = PolarNewtonSolverCUDA(g.Yp, g.Yj, g.Yx, g.pv, g.pq)
     out = {"cases": g.n_branch + 1}
     for prec in ("mixed", "double"):
-        cap_ms = {}
+        cap_ms, shape_ms = {}, {}
+        shape = (0, 0)
         if not args.no_tune:
-            # the factorization schedule's chain cap of this launch, measured (autotune.CHAIN_CAPS):
-            # the same results for every cap, only the time differs
+            # the launch's CTA shape (threads, case slots per CTA) and the factorization schedule's
+            # chain cap, measured (autotune): the same results for every candidate, only the time
+            # differs
             from p3s_gb300 import autotune
 
-            for cap in autotune.CHAIN_CAPS:
-                solver._s.set_chain_cap(cap)
+            def timed(nt, cpc):
                 t = []
                 for _ in range(2):
                     contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
-                                                    return_islands=False)
+                                                    return_islands=False, cases_per_cta=cpc, threads_per_cta=nt)
                     t.append(solver.last_stats["kernel_ms"])
-                cap_ms[cap] = min(t)
+                return min(t)
+
+            solver._s.set_chain_cap(1.0)
+            for nt, cpc in N1_SHAPES:
+                shape_ms[(nt, cpc)] = timed(nt, cpc)
+            shape = min(shape_ms, key=shape_ms.get)
+            for cap in autotune.CHAIN_CAPS:
+                solver._s.set_chain_cap(cap)
+                cap_ms[cap] = timed(*shape)
             solver._s.set_chain_cap(min(cap_ms, key=cap_ms.get))
+
+        def solve():
+            return contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
+                                                   return_islands=False, cases_per_cta=shape[1],
+                                                   threads_per_cta=shape[0])
+
         for _ in range(args.warmup):
-            r = contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
-                                                 return_islands=False)
+            r = solve()
         wall, kern = [], []
         for _ in range(max(1, args.steps // 2)):
             t0 = time.perf_counter()
-            r = contingency.solve_contingencies(g, reslack_islands=True, precision=prec, solver=solver,
-                                                 return_islands=False)
+            r = solve()
             wall.append(time.perf_counter() - t0)
             kern.append(solver.last_stats["kernel_ms"])
         L = g.n_branch + 1
@@ -496,6 +511,8 @@ def run_n1(args):
             "islanded_cases": int((r.served.sum(axis=0) < g.n).sum()),
             "chain_cap": solver._s.chain_cap,
             "chain_cap_ms": {f"{k:g}": round(v, 3) for k, v in cap_ms.items()} or None,
+            "shape": list(shape) if shape != (0, 0) else "group rule",
+            "shape_ms": {f"{k[0]}x{k[1]}": round(v, 3) for k, v in shape_ms.items()} or None,
         }
     return out
 

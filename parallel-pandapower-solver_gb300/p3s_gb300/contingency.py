@@ -164,7 +164,7 @@ def single_outage_lists(n_branch: int):
 
 def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, max_iter: int = 30,
                         precision: str = "double", groups=None, gen_prio=None, v_start=None, solver=None,
-                        return_islands: bool = True):
+                        return_islands: bool = True, cases_per_cta: int = 0, threads_per_cta: int = 0):
     """Solve every N-1 case of ``grid`` on the device (``solve_contingencies_cuda`` semantics,
     solver_cuda.py:30-119, with ``init="flat"``).
 
@@ -172,7 +172,8 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
     islanding, the re-slack start and the outage-patched Ybus are all made on the device in the
     solve's launch (no per-case arrays cross the bus but the results). Unserved buses come back
     as NaN; ``served`` is the launch's own islanding mask. ``return_islands`` adds the island
-    labels and reference buses (one more islanding call)."""
+    labels and reference buses (one more islanding call). ``cases_per_cta`` /
+    ``threads_per_cta``: the launch's CTA shape (0: the group rule), e.g. from a tuner."""
     from .group import GpuGroup, GroupJob
 
     n = grid.n
@@ -203,9 +204,10 @@ def solve_contingencies(grid, reslack_islands: bool = False, tol: float = 1e-8, 
         solver._branch_key = key
     if getattr(solver, "_group", None) is None:
         solver._group = GpuGroup()
+    solver._group.set_shape(threads_per_cta, 0)
     solver.precision = precision
     job = GroupJob(gs, np.asarray(grid.Sbus), np.asarray(v_start), n_cases=len(groups), outages=outages,
-                   reslack=reslack_islands)
+                   reslack=reslack_islands, cases_per_cta=cases_per_cta)
     res = solver._group.solve([job], solver._params(max_iter, tol), pinned_out=True)[0]
     solver._record(len(groups), res, solver._group.stats)
     V = res["V"]
