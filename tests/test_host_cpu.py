@@ -262,3 +262,36 @@ def test_no_cpu_fallback_without_a_device(grid118):
                  lambda: nr_klu.solve_single(g.Yp, g.Yj, g.Yx, g.Sbus, g.V0, g.pv, g.pq), lambda: GpuGroup()):
         with pytest.raises(RuntimeError):
             make()
+
+
+def test_autotune_pins_the_fastest_shape_and_chain_cap():
+    """The tuner's selection: every (threads, slots, chain cap) candidate timed (best of its
+    runs, the first run discarded as the shape's build), the fastest pinned -- the shape for the
+    batch's size class, the cap for the solver -- and every timing returned."""
+    from p3s_gb300 import autotune
+
+    class FakeSolver:
+        def __init__(self):
+            self.chain_cap, self.shape, self.stats, self.pinned = 1.0, None, {}, []
+
+        def set_chain_cap(self, cap):
+            self.chain_cap = cap
+
+        def set_shape(self, units, nt, g):
+            self.shape = (units, nt, g)
+            self.pinned.append(self.shape)
+
+    s = FakeSolver()
+    cost = {(512, 32, 1.0): 10.0, (512, 32, 0.5): 9.5, (1024, 16, 1.0): 11.0, (1024, 16, 0.5): 12.0}
+    runs = []
+
+    def run():
+        key = (s.shape[1], s.shape[2], s.chain_cap)
+        runs.append(key)
+        # the first run of a candidate is slow (it builds the schedule): the tuner must not keep it
+        s.stats = {"kernel_ms": cost[key] + (100.0 if runs.count(key) == 1 else 0.0)}
+
+    choice, timings = autotune.tune(s, 8760, run, candidates=((512, 32), (1024, 16)), chain_caps=(1.0, 0.5), reps=2)
+    assert choice == (512, 32, 0.5) and timings == cost
+    assert s.chain_cap == 0.5 and s.shape == (8760, 512, 32)
+    assert len(runs) == 4 * 3
