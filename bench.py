@@ -113,6 +113,9 @@ def shared_start(g):
 
 # autotune candidates of the headline launch: the rule's shape and its neighbours
 TUNE_SHAPES = ((512, 32), (512, 16), (1024, 32), (1024, 16))
+# ... of the uneven multi-grid launch: (threads per CTA, 0 = the rule; variable buses x case
+# slots a CTA takes per job, the group rule's 16,384 and its neighbours)
+MG_PACKING = ((0, 16384), (0, 8192), (0, 32768), (512, 4096), (1024, 16384))
 # ... and of the N-1 sweep's launch (3,001 cases; 0 = the group rule: 512 x 16)
 N1_SHAPES = ((0, 0), (512, 8), (512, 32), (1024, 8), (1024, 16), (256, 4), (256, 8))
 
@@ -533,6 +536,39 @@ def run_multigrid(args):
     out = {"grids": len(grids), "cases": cases, "bus_range": [min(g.n for g in grids), max(g.n for g in grids)]}
     for prec in ("mixed", "double"):
         p = GpuSolver.params(precision=prec)
+        tuned = None
+        if not args.no_tune:
+            # the launch's packing (threads per CTA; variable buses x case slots a CTA takes per
+            # job, i.e. cases per CTA by grid size) and the factorization schedule's chain cap,
+            # measured (autotune): the same results for every candidate, only the time differs
+            from p3s_gb300 import autotune
+
+            def timed():
+                t = []
+                for _ in range(2):
+                    grp.solve(jobs, p)
+                    t.append(grp.stats["kernel_ms"])
+                return min(t)
+
+            for s in solvers:
+                s.set_chain_cap(1.0)
+            packing = {}
+            for nt, budget in MG_PACKING:
+                grp.set_shape(nt, budget)
+                packing[(nt, budget)] = timed()
+            best = min(packing, key=packing.get)
+            grp.set_shape(*best)
+            caps = {}
+            for cap in autotune.CHAIN_CAPS:
+                for s in solvers:
+                    s.set_chain_cap(cap)
+                caps[cap] = timed()
+            cap = min(caps, key=caps.get)
+            for s in solvers:
+                s.set_chain_cap(cap)
+            tuned = {"threads_per_cta": best[0] or "rule", "slot_budget": best[1], "chain_cap": cap,
+                     "packing_ms": {f"{k[0] or 'rule'}x{k[1]}": round(v, 3) for k, v in packing.items()},
+                     "chain_cap_ms": {f"{k:g}": round(v, 3) for k, v in caps.items()}}
         for _ in range(args.warmup):
             res = grp.solve(jobs, p)
         kern, call = [], []
@@ -552,6 +588,7 @@ def run_multigrid(args):
             "one_launch_per_grid_kernel_ms": round(per_grid, 2),
             "iterations_mean": float(its.mean()), "converged": int(cv.sum()),
             "threads_per_cta": grp.stats["threads_per_cta"], "grid_ctas": grp.stats["grid"],
+            "autotune": tuned,
         }
     return out
 

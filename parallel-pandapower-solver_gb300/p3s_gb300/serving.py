@@ -483,6 +483,9 @@ class StreamServer:
         responses: dict[int, Response] = {}
         pending: deque = deque()
         outstanding: dict[int, tuple] = {}
+        # the server is up -- its launch running -- before the stream's clock starts (a launch
+        # started later, when a ring fills or after an idle return, counts in the requests' time)
+        self._start()
         t0 = time.perf_counter()
 
         def now():
@@ -516,7 +519,6 @@ class StreamServer:
                     raise RuntimeError(f"stream launch stopped with job {q} unfinished")
             pending.extendleft(reversed(redo))
 
-        self._start()
         try:
             i = 0
             while i < len(reqs) or pending or outstanding:
