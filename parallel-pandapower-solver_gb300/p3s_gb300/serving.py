@@ -372,7 +372,8 @@ class StreamServer:
     flag is polled here. Requests therefore never wait for another launch to finish. Staging and
     result memory are reused as jobs finish (a request waits only while they are all held by
     running jobs); when a launch's ring of job slots is used up, the server stops it (it finishes
-    every job it took), starts a new one and goes on.
+    every job it took), starts a new one and goes on, and a launch that returned at its idle limit
+    is replaced the same way, its unstarted jobs submitted again.
 
     Same request and response types as ``Server``; every case runs the same arithmetic as in
     any other launch, so each result equals the one it gets alone (bit for bit). ``backend``:

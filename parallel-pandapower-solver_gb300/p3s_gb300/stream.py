@@ -2,13 +2,15 @@
 ``gbpf_stream_*``): requests are admitted as CTAs free up, not as whole launches finish.
 
 ``GpuStream`` wraps one stream launch: ``start`` launches the kernel for a set of resident
-topologies; ``submit`` stages one job (a topology's cases) and appends it to the launch's ring;
-the kernel writes the job's results straight into page-locked host arrays and sets the job's
-flag (``flags`` is a numpy view of the flags); ``stop`` waits for every submitted job and ends
-the launch. A launch takes at most ``capacity`` jobs (``full``: stop, start again); its
-staging arena, page-locked input staging and result memory are reused as jobs complete
-(``release`` hands a job's memory back once its results have been read), and ``submit``
-returns None while they are held by unfinished jobs.
+topologies; ``submit`` stages one job (a topology's cases, in the launch's precision or its
+own) and appends it to the launch's ring; the kernel writes the job's results straight into
+page-locked host arrays and sets the job's flag (``flags`` is a numpy view of the flags);
+``stop`` ends the launch once every job it started is done and returns 0, or 1 if its CTAs had
+left at their idle limit (no job published for ``idle_seconds``) -- a job whose flag is still
+0 then was never started and goes to the next launch. A launch takes at most ``capacity``
+jobs (``full``: stop, start again); its staging arena, page-locked input staging and result
+memory are reused as jobs complete (``release`` hands a job's memory back once its results
+have been read), and ``submit`` returns None while they are held by unfinished jobs.
 No reference counterpart: the reference has no serving loop.
 """
 
