@@ -9,17 +9,21 @@
 // batching inside the launch); there is no host round trip per Newton pass (the
 // reference reads a status word back every pass, nr_polar_solver.py:932-933), no
 // per-iteration launches, and no inter-CTA waiting of any kind (the only cross-CTA
-// operation is the atomicAdd that hands out work).
+// operation is the atomicAdd that hands out work; a stream launch's CTAs also poll the count
+// of jobs the host has published, with a bounded wait).
 //
-// The per-CTA working set lives in global memory and is reused case after case (it stays
-// L2-resident): factor blocks [blk][slot] (the G slots of one block are contiguous, so a
-// worker's G lanes read one 128/256-byte line per operand), residual and step [row][slot],
-// voltage state [bus][slot].
+// The per-CTA working set lives in global memory and is reused case after case: factor
+// blocks [blk][slot] (the G slots of one block are contiguous, so a worker's G lanes read one
+// 128/256-byte line per operand), residual and step [row][slot], voltage state [bus][slot].
+// At about 1 MB per slot for the 2,000-bus grid (~10 GB over all slots) it does not fit the
+// 129-MB L2: a pass streams it from DRAM (ncu: ~25 % L2 hit rate), which is what the
+// per-case-iteration traffic measures.
 //
-// Precision: mismatch, power injections, convergence norm and voltage update are always
-// double. With `mixed`, a slot's Jacobian, factors and substitutions are float while its
+// Precision: mismatch, power injections and convergence norm are always double, and so is the
+// voltage state. With `mixed`, a slot's Jacobian, factors and substitutions are float while its
 // vote says so (the vote rules of nr_polar_kernels.cu:209-228), double otherwise; a float
-// factorization that fails the pivot check is redone in double within the same step.
+// factorization that fails the pivot check is redone in double within the same step; the
+// phasor rotation of a float step at a PQ bus forms its increment in float (rotate_f32).
 #include <cfloat>
 #include <cstdint>
 
