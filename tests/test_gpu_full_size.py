@@ -204,9 +204,10 @@ def test_large_grids_of_the_multigrid_batch():
 def test_largest_serving_topologies_through_the_server():
     """The serving pool's three largest topologies: a single solve, a 96-step chunk and a
     200-outage N-1 sweep each, admitted together into the serving loop (both precisions),
-    against the oracle from the same warm start (the topology's converged base case)."""
+    against the oracle from the same warm start (the topology's converged base case); the
+    stream launch's server gives the same results bit for bit."""
     from p3s_gb300 import contingency
-    from p3s_gb300.serving import Request, Server, Topology
+    from p3s_gb300.serving import Request, Server, StreamServer, Topology
     from p3s_gb300.synthetic import make_grid
 
     sizes = _serving_sizes()
@@ -229,6 +230,15 @@ def test_largest_serving_topologies_through_the_server():
     for prec in ("double", "mixed"):
         srv = Server(topos, precision=prec, contexts=2)
         got[prec] = srv.run(reqs, realtime=False)
+        del srv
+        stream = StreamServer(topos, precision=prec, capacity=64, arena_bytes=2 << 30, result_bytes=2 << 30)
+        for a, b in zip(got[prec], stream.run(reqs, realtime=False)):
+            assert np.array_equal(a.iterations, b.iterations) and np.array_equal(a.converged, b.converged)
+            assert np.array_equal(np.isnan(a.V), np.isnan(b.V))
+            assert np.array_equal(np.nan_to_num(a.V), np.nan_to_num(b.V))
+            if a.served is not None:
+                assert np.array_equal(a.served, b.served)
+        del stream
     for q in reqs:
         tp = topos[q.topo]
         g = tp.grid
