@@ -1875,15 +1875,21 @@ struct gbpf_stream {
 namespace {
 constexpr unsigned STREAM_SLEEP_NS = 20000;  // a CTA without an open job polls every ~20 us
 
+// Case slots a CTA may take per job of this topology: the slot budget's count, and at least
+// two -- so that a large grid's job of more cases than the launch has CTAs runs in one wave of
+// two-slot CTAs instead of two waves of one-slot CTAs
 int stream_slots(const gbpf_stream* st, const gbpf_solver* s) {
-    return job_slots(gbpf::MAX_SLOTS, s->plan.nv, st->slot_budget);
+    return std::max(2, job_slots(gbpf::MAX_SLOTS, s->plan.nv, st->slot_budget));
 }
 
-// Case slots of a job's CTAs: the topology's slot count, but no more than the job has cases (a
-// single solve takes one slot, with all of the CTA's threads, for the lowest latency).
+// Case slots of a job's CTAs: the slot budget's count, but no more than the job has cases (a
+// single solve takes one slot, with all of the CTA's threads, for the lowest latency); and as
+// many as it takes (up to two) for the job's cases to fit the launch's CTAs in one wave.
 int stream_job_slots(const gbpf_stream* st, const gbpf_solver* s, int cases) {
+    const int budget = job_slots(gbpf::MAX_SLOTS, s->plan.nv, st->slot_budget);
     int g = 1;
-    while (g < cases && g < stream_slots(st, s)) g *= 2;
+    while (g < cases && g < budget) g *= 2;
+    if (g == 1 && cases > st->ctas) g = 2;
     return g;
 }
 
