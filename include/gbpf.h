@@ -302,8 +302,9 @@ int gbpf_group_stats(gbpf_group* g, gbpf_stats* out);
  *   threads = threads per CTA, 512 or 1024 (0: 1024); ctas = CTAs (0: as many as fit on all
  *   SMs but 8, which keep room for the submits' islanding and start-table kernels); slot_budget
  *   = variable buses x case slots a CTA takes per job (0: 8,192). A job's CTAs take the
- *   smallest power of two of slots that holds its cases, up to that budget: a single solve
- *   runs on all of a CTA's threads.
+ *   smallest power of two of slots that holds its cases, up to that budget (a single solve
+ *   runs on all of a CTA's threads), and two where one would leave more cases than the launch
+ *   has CTAs (one wave instead of two).
  * start: launches the kernel for the given topologies (schedules built, scratch sized for them,
  *   the kernels that submits launch loaded into the context first; gbpf_params as for the other
  *   calls, the shared start off). A CTA without an open job polls every ~20 us; once no job has
