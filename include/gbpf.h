@@ -54,7 +54,7 @@ typedef struct gbpf_params {
                             gbpf_stats.phase_cycles (single-topology launches; 0: off, the default) */
     int eager_jacobian;  /* mixed, vote_rule 1: 0 (default) leaves the float Jacobian out of an
                             evaluation after which no factorization is expected (after a chord
-                            step, or a float step from below 1e4 x chord_tol) and builds it later
+                            step, or a float step from below 100 x chord_tol) and builds it later
                             only if a step factors after all -- the same values, so the same
                             results; 1: every evaluation builds its Jacobian */
 } gbpf_params;

@@ -35,7 +35,7 @@ namespace gbpf {
 constexpr double ARMIJO_C = 1e-4;  // nr_klu.cpp:563
 constexpr int LS_MAX_TRIALS = 10;  // nr_klu.cpp:562
 constexpr double CHORD_RATE = 0.1; // a chord step must cut the mismatch tenfold for another one
-constexpr double JAC_LAZY = 1e4;   // a float step from below this x chord_tol skips its Jacobian
+constexpr double JAC_LAZY = 100.0; // a float step from below this x chord_tol skips its Jacobian
                                    // (near the solution such a step lands below chord_tol)
 constexpr double BIG = DBL_MAX;    // nr_klu.cpp:434 NONFINITE_NORM
 
