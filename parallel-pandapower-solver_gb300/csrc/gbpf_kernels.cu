@@ -826,6 +826,29 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
     }
     __syncthreads();
 
+    // nr_klu.cpp:590-595 loop head of slot s on its mismatch s_nrm[s]. Under the GB300 vote
+    // rule a case keeps stepping until its voltage is as exact as a double solve's: a float step
+    // lands anywhere below tol (it contracts the error by ~cond(J) 2^-24 instead of squaring
+    // it), so the case goes on until its mismatch is below tol_polish (the smaller of polish x
+    // tol and a bound on the voltage error divided by the grid's |J^-1| estimate). `converged`
+    // still means mismatch < tol.
+    auto loop_head = [&](int s) {
+        const bool polish = Bt.mixed && Bt.vote_rule == 1;
+        const bool done = s_nrm[s] < (polish ? Bt.tol_polish : Bt.tol);
+        if (s_it[s] >= Bt.max_iter) {
+            s_st[s] = SL_FINISH;
+            s_conv[s] = polish && s_nrm[s] < Bt.tol;
+        } else if (done) {
+            s_st[s] = SL_FINISH;
+            s_conv[s] = 1;
+        } else if (s_nrm[s] >= BIG) {
+            s_st[s] = SL_FINISH;
+            s_conv[s] = 0;
+        } else {
+            s_st[s] = SL_ACTIVE;
+        }
+    };
+
     for (;;) {
         // ---------------------------------------------------------------- refill
         if (tid < G) {
@@ -862,6 +885,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                     s_chord[s] = 0;
                     s_first[s] = s_share && !s_warm[s];
                     s_nojac[s] = 0;
+                    s_res[s] = 0ULL;
                     s_it[s] = 0;
                     s_conv[s] = 0;
                     s_vote[s] = Bt.mixed ? 1 : 0;
@@ -1016,6 +1040,34 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 }
             }
             spin[idx] = pinned;
+            if (s_first[s]) {
+                // a case from the shared start: its first mismatch S - S(V0) here, with S(V0)
+                // computed once (the operation eval_row does, Ssp - Pc = Ssp + (-Pc)) -- so
+                // it decides and takes its first step in this pass
+                const int row = P.row_of_bus[bus];
+                if (row >= 0) {
+                    const double2 Ssp = ld_in<RING>(Bt.s_shared ? Bt.S + bus : Bt.S + (size_t)bus * Bt.sS + c);
+                    const double2 r0 = __ldg(&Bt.R0[row]);
+                    const double rp = Ssp.x + r0.x;
+                    const double rq = P.bus_pq[bus] != 0 ? Ssp.y + r0.y : 0.0;
+                    R[((size_t)row << lg) + s] = make_double2(rp, rq);
+                    const unsigned long long a = abs_bits(rp), b = abs_bits(rq);
+                    atomicMax(&s_res[s], b > a ? b : a);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < G && s_st[tid] == SL_FRESH && s_first[tid]) {  // their loop head, now
+            const int s = tid;
+            double nw = bitsd(s_res[s]);
+            if (!(nw < BIG)) nw = BIG;
+            s_nrm[s] = nw;
+            s_vote[s] = !Bt.mixed ? 0 : (Bt.vote_rule == 1 ? 1 : (nw > Bt.mixed_switch ? 1 : 0));
+            // (what the start's own pass would have set: the precision of the start's Jacobian --
+            // the shared one, float on the mixed path -- and the step count)
+            s_jprec[s] = (Bt.mixed && s_vote[s] == 1) ? 1 : 0;
+            loop_head(s);
+            if (s_st[s] == SL_ACTIVE) s_it[s] = 1;
         }
 
         // ---------------------------------------------------------------- linear solve
@@ -1252,17 +1304,6 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
             const int c = s_case[s];
             const double2 Ssp = ld_in<RING>(Bt.s_shared ? Bt.S + bus : Bt.S + (size_t)bus * Bt.sS + c);
             const bool pq = P.bus_pq[bus] != 0;
-            if (st == SL_FRESH && s_first[s]) {
-                // from the shared start: S - S(V0) with S(V0) computed once (the same operation
-                // eval_row does, Ssp - Pc = Ssp + (-Pc)); the Jacobian is the shared one
-                const double2 r0 = __ldg(&Bt.R0[row]);
-                const double rp = Ssp.x + r0.x;
-                const double rq = pq ? Ssp.y + r0.y : 0.0;
-                R[((size_t)row << lg) + s] = make_double2(rp, rq);
-                const unsigned long long a = abs_bits(rp), b = abs_bits(rq);
-                atomicMax(&s_res[s], b > a ? b : a);
-                continue;
-            }
             const bool pinned = spin[((size_t)bus << lg) + s] != 0;
             EvalCtx ec{&P, Et, Ei, iv32, lg, Bt.ymode == 3 ? 1 : Bt.ymode, Bt.Yd, Bt.sYd, c, s_nst[s], s_stk[s], s_stv[s]};
             unsigned long long worst;
@@ -1350,28 +1391,7 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) newton_kernel(const Launch L)
                 s_nrm[s] = nw;
                 top = true;
             }
-            if (top) {  // nr_klu.cpp:590-595 loop head
-                // Under the GB300 vote rule a case keeps stepping until its voltage is as
-                // exact as a double solve's: a float step lands anywhere below tol (it
-                // contracts the error by ~cond(J) 2^-24 instead of squaring it), so the case
-                // goes on until its mismatch is below tol_polish (the smaller of polish x tol
-                // and a bound on the voltage error divided by the grid's |J^-1| estimate).
-                // `converged` still means mismatch < tol.
-                const bool polish = Bt.mixed && Bt.vote_rule == 1;
-                const bool done = s_nrm[s] < (polish ? Bt.tol_polish : Bt.tol);
-                if (s_it[s] >= Bt.max_iter) {
-                    s_st[s] = SL_FINISH;
-                    s_conv[s] = polish && s_nrm[s] < Bt.tol;
-                } else if (done) {
-                    s_st[s] = SL_FINISH;
-                    s_conv[s] = 1;
-                } else if (s_nrm[s] >= BIG) {
-                    s_st[s] = SL_FINISH;
-                    s_conv[s] = 0;
-                } else {
-                    s_st[s] = SL_ACTIVE;
-                }
-            }
+            if (top) loop_head(s);
         }
         if (tid == 0) atomicAdd(&Bt.stats[4], 1ULL);
         __syncthreads();
