@@ -46,3 +46,27 @@ def test_two_gloo_ranks_shard_and_reduce():
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert got[0][1:3] == (0, 1501) and got[1][1:3] == (1501, 3001)
     assert got[0][3] == got[1][3] == 11.0
+
+
+def test_reference_arm_prints_the_bench_contract():
+    """`bench.py --impl reference` (the CPU oracle on the host cores) prints one JSON line with
+    the bench contract's keys, the same metric and config as the GPU arm would, and its own
+    e2e / cpu_baseline blocks (no copies: a CPU arm)."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0", "--hours", "24", "--cpu-hours", "24"],
+                         capture_output=True, text=True, timeout=600, check=True).stdout
+    line = json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    import bench
+
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["unit"] == "solves/s" and line["config"]["hours"] == 24
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
